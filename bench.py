@@ -1,0 +1,415 @@
+#!/usr/bin/env python
+"""Benchmark of the distillation contraction engine on one GB300.
+
+Workload (one step): the rho two-point at production size, Nev=100, Lt=64,
+7 momenta |p|^2 <= 1, 3 polarisations (gamma_i (x) Phi at both ends), every
+(t_src, t_sink) pair: 64*64*3*7 = 86,016 spin-summed correlator entries
+("diagrams"), each a sum of 16 spin terms coef*Tr[(Phi(tf) tau_ab)^dag tau_cd Phi(ti)].
+Inputs are seeded synthetic perambulators / elementals (SURVEY shapes), resident
+in HBM for `value`; `e2e` re-copies them from pinned host memory every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--engine split|fp64]
+  python bench.py --impl reference ...   # the oracle (CPU FP64, all host threads)
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NT, NEV, MAXP2, SEED = 64, 100, 1, 1001
+METRIC = "diagrams/s @Nev=100,Lt=64: split-TC batched vs plain FP64, rel err ≤1e-9"
+WORKLOAD = "rho two-point, Nev=100, Lt=64, 7 momenta |p|^2<=1, 3 polarisations, all 64x64 (t_src,t_sink)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--engine", default="auto", choices=["auto", "split", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine (0 = skip)")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
+    ap.add_argument("--nt", type=int, default=NT)
+    ap.add_argument("--nev", type=int, default=NEV)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- helpers
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def fp64_peak_tflops():
+    """Measured FP64 peak on this GPU: cuBLAS DGEMM 8192^3 (best of 3), TFLOP/s."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def workload(nt, nev):
+    from contractions_code_scattering_gb300 import api, synth
+    moms = synth.momenta(MAXP2)
+    rows, coef, oi = api.rho_rows_for_momenta(len(moms))
+    return moms, rows, coef, oi, 3 * len(moms)
+
+
+def make_inputs(nt, nev, moms):
+    import torch
+    from contractions_code_scattering_gb300 import synth
+    tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
+    phi = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
+    torch.cuda.synchronize()
+    return tau, phi
+
+
+def cpu_sample(tau, phi, rows, coef, nout, target_s, max_ti):
+    """Time the oracle (reference chain order, every row recomputing its two
+    products) on t_sink = 0 and the first k source times; returns
+    (diagrams/s, cores, sample description, sample values [k, nout])."""
+    import numpy as np
+    from oracle import pyoracle as O
+    k_probe = 1
+    tau_row = tau[0].cpu().numpy()
+    phi_h = phi.cpu().numpy()
+    t0 = time.perf_counter()
+    O.twosided_rows(tau_row, phi_h, rows, coef, 0, 0, k_probe)
+    dt1 = time.perf_counter() - t0
+    k = int(max(1, min(max_ti, target_s / max(dt1, 1e-3))))
+    t0 = time.perf_counter()
+    vals = O.twosided_rows(tau_row, phi_h, rows, coef, 0, 0, k)
+    dt = time.perf_counter() - t0
+    diag = k * nout
+    cores = os.cpu_count() or 1
+    return diag / dt, cores, "t_sink=0, t_src=0..%d, %d rows each (%d diagrams), %.1f s" % (k - 1, len(rows), diag, dt), vals, k
+
+
+def rows_to_out(vals, oi, nout):
+    import numpy as np
+    out = np.zeros(vals.shape[:-1] + (nout,), np.complex128)
+    for r, o in enumerate(oi):
+        out[..., o] += vals[..., r]
+    return out
+
+
+# -------------------------------------------------------------- reference
+def run_reference(args):
+    """--impl reference: the reference's contraction algorithm on the host cores
+    (the oracle's OpenMP FP64 restatement; the reference's own kernels are
+    GPU-only), on a bounded sample of the workload per step."""
+    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    import numpy as np
+    from contractions_code_scattering_gb300 import synth
+    from oracle import pyoracle as O
+    moms, rows, coef, oi, nout = workload(args.nt, args.nev)
+    rng_seed = SEED
+    # Only t_sink = 0 is sampled: build tau(0, t) for t < k directly on the host.
+    k = 2
+    nev = args.nev
+    prop = synth.make_prop(k, nev, seed=rng_seed, decay=0.35)
+    phis = synth.make_phi_momenta(k, nev, moms, seed=rng_seed + 1)
+    phi = synth.mom_stack(phis, moms)
+    for _ in range(args.warmup):
+        O.twosided_rows(prop[0], phi, rows, coef, 0, 0, 1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.twosided_rows(prop[0], phi, rows, coef, 0, 0, k)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    diag = k * nout
+    val = diag / (ms / 1e3)
+    cores = os.cpu_count() or 1
+    sample = "t_sink=0, t_src=0..%d of the workload, %d rows each (%d diagrams) per step" % (k - 1, len(rows), diag)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "diagrams/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": val, "unit": "diagrams/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "diagrams/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# -------------------------------------------------------------------- ours
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import _lib, api
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    api.device_init(local)
+    nt, nev = args.nt, args.nev
+    moms, rows, coef, oi, nout = workload(nt, nev)
+    diagrams = nt * nt * nout
+    engine = args.engine
+    if engine == "auto":
+        engine = "split" if _split_available() else "fp64"
+
+    tau, phi = make_inputs(nt, nev, moms)
+    out = torch.empty((nt, nt, nout), dtype=torch.complex128, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step(eng, o=out):
+        api.twosided(tau, phi, rows, coef, oi, nout, engine=eng, out=o)
+
+    for _ in range(args.warmup):
+        step(engine)
+    torch.cuda.synchronize()
+    barrier(ws)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    _lib.timing_enable(True)
+    n0 = _lib.launch_count()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step(engine)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = _lib.launch_count() - n0
+    report = _lib.timing_report()
+    clk = clocks.stop()
+    elapsed = allmax(ws, ev0.elapsed_time(ev1) / 1e3)
+    ms_per_step = 1e3 * elapsed / args.steps
+    value = ws * diagrams * args.steps / elapsed
+    _lib.timing_enable(False)
+
+    res_main = out.cpu().numpy()
+
+    # Roofline of the dominant kernel.
+    roof = roofline(engine, report, args.steps, nt, nev, len(moms))
+
+    # Plain FP64 engine on the same workload (the metric's comparison arm).
+    fp64 = None
+    if engine == "split" and args.fp64_steps > 0:
+        out64 = torch.empty_like(out)
+        step("fp64", out64)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.fp64_steps):
+            step("fp64", out64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1) / 1e3 / args.fp64_steps
+        r64 = out64.cpu().numpy()
+        err = np.abs(res_main - r64) / np.maximum(np.abs(r64), 1e-300)
+        fp64 = {"value": diagrams / t64, "unit": "diagrams/s", "ms_per_step": 1e3 * t64,
+                "split_speedup": (diagrams / t64 and value / ws / (diagrams / t64)),
+                "split_vs_fp64_rel_err": {"max": float(err.max()), "median": float(np.median(err)),
+                                          "p99": float(np.quantile(err, 0.99)),
+                                          "max_over_maxabs": float(np.abs(res_main - r64).max() / np.abs(r64).max())}}
+        del out64
+
+    # End to end: host (pinned) inputs copied in and the result read back every step.
+    e2e = None
+    if args.e2e_steps > 0:
+        h_tau = torch.empty(tau.shape, dtype=tau.dtype, pin_memory=True)
+        h_tau.copy_(tau)
+        h_phi = torch.empty(phi.shape, dtype=phi.dtype, pin_memory=True)
+        h_phi.copy_(phi)
+        h_out = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            tau.copy_(h_tau, non_blocking=True)
+            phi.copy_(h_phi, non_blocking=True)
+            step(engine)
+            h_out.copy_(out, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        te = allmax(ws, e0.elapsed_time(e1) / 1e3) / args.e2e_steps
+        e2e = {"value": ws * diagrams / te, "unit": "diagrams/s",
+               "h2d_bytes_per_step": int(h_tau.numel() * 16 + h_phi.numel() * 16),
+               "d2h_bytes_per_step": int(h_out.numel() * 16), "ms_per_step": 1e3 * te}
+        del h_tau, h_phi, h_out
+
+    # CPU baseline (the oracle, reference chain order) on a bounded sample; the
+    # same sample also checks the GPU result at full size.
+    cpu = None
+    parity = None
+    if rank == 0 and args.cpu_seconds > 0:
+        rate, cores, sample, vals, k = cpu_sample(tau, phi, rows, coef, nout, args.cpu_seconds, nt)
+        ref = rows_to_out(vals, oi, nout)
+        got = res_main[0, :k]
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+        parity = {"entries": int(ref.size), "max_rel_err": float(rel.max()), "median_rel_err": float(np.median(rel)),
+                  "max_err_over_maxabs": float(np.abs(got - ref).max() / np.abs(ref).max())}
+        cpu = {"value": rate, "unit": "diagrams/s", "cores": cores, "kind": "port", "sample": sample}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "diagrams/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if engine == "fp64" else "f64-equivalent (bf16 x5 slices, fp32 acc)",
+        "data": "synthetic (seeded tau/Phi, SURVEY distributions)",
+        "config": {"workload": WORKLOAD, "engine": engine, "nev": nev, "lt": nt, "momenta": len(moms),
+                   "diagrams_per_step": diagrams, "l2": "inputs larger than L2 (tau 10.5 GB)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
+        "kernels": {k: {"launches": v[0], "ms": v[2]} for k, v in report.items()},
+        "fp64_engine": fp64, "parity_vs_oracle_sample": parity,
+    }
+    print(json.dumps(line))
+
+
+def _split_available():
+    try:
+        from contractions_code_scattering_gb300 import _lib
+        return bool(_lib.lib().ctr_split_available())
+    except Exception:
+        return False
+
+
+def roofline(engine, report, steps, nt, nev, nmom):
+    """Dominant kernel's achieved rate against its pipe's measured peak."""
+    n3 = float(nev) ** 3
+    prods = nt * nt * nmom * 32  # 16 source-side + 16 sink-side block products per (tf, ti, p)
+    if engine == "fp64":
+        launches, _, ms = report.get("zgemm_f64", (0, 0, 0.0))
+        if not launches or ms <= 0:
+            return None
+        flops = steps * prods * 8.0 * n3
+        per_launch_flops = flops / launches
+        achieved = per_launch_flops / (ms / launches / 1e3) / 1e12
+        peak = fp64_peak_tflops()
+        return {"kernel": "zgemm_f64", "bound": "fp64 pipe", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": "measured in bench.py: cuBLAS DGEMM 8192^3 (MEASURED_PEAKS.json has no FP64 figure)",
+                "algorithmic": "8*Nev^3 flops per block product, 32 products per (t_sink, t_src, momentum)"}
+    launches, _, ms = report.get("split_gemm", (0, 0, 0.0))
+    if not launches or ms <= 0:
+        return None
+    pk = measured_peaks()
+    peak = pk.get("bf16_tflops", 1924.8)
+    mma_flops = steps * prods * 8.0 * n3 * 15 * (112.0 / 100.0)
+    achieved = mma_flops / launches / (ms / launches / 1e3) / 1e12
+    return {"kernel": "split_gemm", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
+            "fp64_equivalent_tflops": achieved / 15 / 1.12,
+            "algorithmic": "15 bf16 slice-pair products x 8*Nev^3 flops (K padded 100->112) per block product"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,155 @@
+"""Python host-side mirror of the reference's contraction launchers.
+
+Each function takes device tensors (torch, complex128, contiguous, on the
+current CUDA device) in the reference layouts and calls the C ABI of
+libctr.so; the computation runs in the library's CUDA kernels.  Names and
+argument meanings follow the reference's run_Contract* launchers
+(include/contract.h:50-69) and Contract_* classes; errors raise CtrError
+instead of terminating the process.
+"""
+
+import ctypes
+
+import numpy as np
+
+from ._lib import ENGINE_FP64, ENGINE_SPLIT, CtrError, check, lib
+
+ENGINES = {"fp64": ENGINE_FP64, "split": ENGINE_SPLIT}
+
+
+def _engine(e):
+    if isinstance(e, int):
+        return e
+    try:
+        return ENGINES[e]
+    except KeyError:
+        raise ValueError("engine must be one of %s" % list(ENGINES))
+
+
+def _dev(t, name):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("%s must be a CUDA tensor" % name)
+    if t.dtype != torch.complex128:
+        raise TypeError("%s must be complex128" % name)
+    if not t.is_contiguous():
+        raise ValueError("%s must be contiguous" % name)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def device_init(device=0):
+    check(lib().ctr_device_init(device))
+
+
+def tables():
+    """The diagram tables generated by the library, keyed by the reference's array names."""
+    L = lib()
+    out = {}
+    s, lr, c = np.zeros((768, 4), np.int16), np.zeros((768, 2), np.int16), np.zeros((768, 2), np.float32)
+    check(L.ctr_table_rho(_np_ptr(s), _np_ptr(lr), _np_ptr(c)))
+    out.update(spinIndices_rho=s, lp_rp_rho=lr, coef_rho=c)
+    s, ip, c = np.zeros((768, 6), np.int16), np.zeros((768,), np.int16), np.zeros((768, 2), np.float32)
+    check(L.ctr_table_rhopi(_np_ptr(s), _np_ptr(ip), _np_ptr(c)))
+    out.update(spinIndices_rhopi=s, ip_rhopi=ip, coef_rhopi=c)
+    a = [np.zeros((256, 6), np.int16), np.zeros((256, 2), np.float32), np.zeros((256, 6), np.int16),
+         np.zeros((256, 2), np.float32), np.zeros((256, 4), np.int16), np.zeros((256, 2), np.float32)]
+    check(L.ctr_table_pipi(*[_np_ptr(x) for x in a]))
+    out.update(spinIndices_pipi_square=a[0], coef_pipi_square=a[1], spinIndices_pipi_doubleTriangle=a[2],
+               coef_pipi_doubleTriangle=a[3], spinIndices_pipi_doubleTriangle_hor=a[4],
+               coef_pipi_doubleTriangle_hor=a[5])
+    s, lr, c = np.zeros((64, 4), np.int16), np.zeros((64, 2), np.int16), np.zeros((64, 2), np.float32)
+    check(L.ctr_table_sigma(_np_ptr(s), _np_ptr(lr), _np_ptr(c)))
+    out.update(spinIndices_sigma=s, lp_rp_sigma=lr, coef_sigma=c)
+    a = [np.zeros((16, 2), np.int16), np.zeros((16, 2), np.float32), np.zeros((128, 5), np.int16),
+         np.zeros((128,), np.int16), np.zeros((128, 2), np.float32)]
+    check(L.ctr_table_sigmapi(*[_np_ptr(x) for x in a]))
+    out.update(spinIndices_sigmapi_hor_fish=a[0], coef_sigmapi_hor_fish=a[1], spinIndices_sigmapi_triangle=a[2],
+               ip_sigmapi_triangle=a[3], coef_sigmapi_triangle=a[4])
+    return out
+
+
+def twosided(prop_rows, phi, rows, coef, out_index, nout, engine="fp64", tf_range=None, out=None, stream=None):
+    """Generic two-sided contraction (include/ctr.h: ctr_twosided).
+
+    prop_rows: [n_rows_held, Nt, 4, 4, N, N] tau rows for t_sink in tf_range;
+    phi: [Nt, nphi, N, N]; rows: int16 [nrows, 6] = (a, b, c, d, L, R);
+    coef: float32 [nrows, 2]; out_index: int32 [nrows].
+    Returns out [n_rows_held, Nt, nout] complex128 (device)."""
+    import torch
+    nt, nev = phi.shape[0], phi.shape[-1]
+    tf0, tf1 = tf_range if tf_range is not None else (0, nt)
+    if out is None:
+        out = torch.empty((tf1 - tf0, nt, nout), dtype=torch.complex128, device=phi.device)
+    rows = np.ascontiguousarray(rows, np.int16)
+    coef = np.ascontiguousarray(coef, np.float32)
+    out_index = np.ascontiguousarray(out_index, np.int32)
+    check(lib().ctr_twosided(_engine(engine), nev, nt, tf0, tf1, _dev(prop_rows, "prop_rows"), _dev(phi, "phi"),
+                             phi.shape[1], rows.shape[0], _np_ptr(rows), _np_ptr(coef), _np_ptr(out_index), nout,
+                             _dev(out, "out"), _stream(stream)))
+    return out
+
+
+def run_contract_rho(prop_rows, mom5, engine="fp64", tf_range=None, out=None, stream=None):
+    """rho-rho for t_sink rows tf_range (run_ContractRho): corr [rows, Nt, 16, 3]."""
+    import torch
+    nt, nev = mom5.shape[0], mom5.shape[-1]
+    tf0, tf1 = tf_range if tf_range is not None else (0, nt)
+    if out is None:
+        out = torch.empty((tf1 - tf0, nt, 16, 3), dtype=torch.complex128, device=mom5.device)
+    check(lib().ctr_rho(_engine(engine), nev, nt, tf0, tf1, _dev(prop_rows, "prop_rows"), _dev(mom5, "mom5"),
+                        _dev(out, "out"), _stream(stream)))
+    return out
+
+
+def run_contract_sigma(prop_rows, mom2, engine="fp64", tf_range=None, out=None, stream=None):
+    """sigma-sigma one-fish for t_sink rows tf_range (run_ContractSigma): corr [rows, Nt, 4]."""
+    import torch
+    nt, nev = mom2.shape[0], mom2.shape[-1]
+    tf0, tf1 = tf_range if tf_range is not None else (0, nt)
+    if out is None:
+        out = torch.empty((tf1 - tf0, nt, 4), dtype=torch.complex128, device=mom2.device)
+    check(lib().ctr_sigma(_engine(engine), nev, nt, tf0, tf1, _dev(prop_rows, "prop_rows"), _dev(mom2, "mom2"),
+                          _dev(out, "out"), _stream(stream)))
+    return out
+
+
+def source_average(corr, scale=1.0, stream=None):
+    """dumpData's average over source times: [Nt, Nt, ...] -> [Nt, ...] (device)."""
+    import torch
+    nt = corr.shape[0]
+    tail = tuple(corr.shape[2:])
+    nc = int(np.prod(tail)) if tail else 1
+    avg = torch.empty((nt,) + tail, dtype=torch.complex128, device=corr.device)
+    check(lib().ctr_source_average(nt, nc, _dev(corr, "corr"), float(scale), _dev(avg, "avg"), _stream(stream)))
+    return avg
+
+
+def rho_rows_for_momenta(nmom, ico=0):
+    """Two-sided rows of the rho two-point with op pair `ico` for `nmom`
+    elementals stacked on the phi axis (one momentum each): returns
+    (rows [nmom*48, 6], coef, out_index) with out index = p*3 + polarisation."""
+    t = tables()
+    spin, lprp, coef = t["spinIndices_rho"], t["lp_rp_rho"], t["coef_rho"]
+    sel = np.arange(ico * 48, ico * 48 + 48)
+    rows, cf, oi = [], [], []
+    for p in range(nmom):
+        for r in sel:
+            s = spin[r]
+            rows.append((s[0], s[1], s[2], s[3], p, p))
+            cf.append(coef[r])
+            oi.append(p * 3 + (r % 48) // 16)
+    return np.array(rows, np.int16), np.array(cf, np.float32), np.array(oi, np.int32)
+
+
+__all__ = ["CtrError", "device_init", "tables", "twosided", "run_contract_rho", "run_contract_sigma",
+           "source_average", "rho_rows_for_momenta", "ENGINES"]

@@ -1,0 +1,96 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "ctr.h"
+
+namespace ctr {
+
+// ----------------------------------------------------------- error handling
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define CTR_CUDA(call)                                                   \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) return ::ctr::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define CTR_TRY(call)              \
+  do {                             \
+    int _rc = (call);              \
+    if (_rc != CTR_OK) return _rc; \
+  } while (0)
+
+// Counts (and, when enabled, times with CUDA events) one kernel launch.
+class TimedLaunch {
+ public:
+  TimedLaunch(cudaStream_t s, const char* name);
+  ~TimedLaunch();
+
+ private:
+  cudaStream_t stream_;
+  int idx_;
+};
+
+// --------------------------------------------------------------- tables
+struct Tables {
+  int16_t rho_spin[768][4];
+  int16_t rho_lprp[768][2];
+  float rho_coef[768][2];
+  int16_t rhopi_spin[768][6];
+  int16_t rhopi_ip[768];
+  float rhopi_coef[768][2];
+  int16_t sq_spin[256][6];
+  float sq_coef[256][2];
+  int16_t dt_spin[256][6];
+  float dt_coef[256][2];
+  int16_t dth_spin[256][4];
+  float dth_coef[256][2];
+  int16_t sigma_spin[64][4];
+  int16_t sigma_lprp[64][2];
+  float sigma_coef[64][2];
+  int16_t hf_spin[16][2];
+  float hf_coef[16][2];
+  int16_t tri_spin[128][5];
+  int16_t tri_ip[128];
+  float tri_coef[128][2];
+};
+const Tables& tables();
+
+// ------------------------------------------------------------ workspace
+// Device scratch owned by the library: one growable buffer per purpose,
+// reused across calls (every call on one stream uses it in order).
+struct Workspace {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int get(size_t need, void** out);
+  void release();
+};
+Workspace& workspace(int slot);
+enum { WS_SCRATCH = 0, WS_TASKS = 1, WS_ROWS = 2, WS_SLICES = 3, WS_MISC = 4, WS_COUNT = 5 };
+
+// Upload a host array into a workspace slot (async on stream, host buffer is
+// kept alive by a pinned staging copy owned by the slot).
+int upload(int slot, const void* host, size_t bytes, void** dev, cudaStream_t stream);
+
+// ------------------------------------------------------- two-sided plan
+struct TwoSidedRow {
+  int16_t a, b, c, d, L, R;  // sink block (a,b) with Phi_R(tf); source block (c,d) with Phi_L(ti)
+};
+
+int twosided_fp64(int nev, int nt, int tf_begin, int tf_end, const double* prop_rows, const double* phi,
+                  int nphi, const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
+                  const std::vector<int32_t>& out_index, int nout, double* out, cudaStream_t stream);
+int twosided_split(int nev, int nt, int tf_begin, int tf_end, const double* prop_rows, const double* phi,
+                   int nphi, const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
+                   const std::vector<int32_t>& out_index, int nout, double* out, cudaStream_t stream);
+
+}  // namespace ctr

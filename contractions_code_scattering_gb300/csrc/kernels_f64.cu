@@ -1,0 +1,201 @@
+// Plain FP64 engine kernels: batched complex block GEMM, fused Hadamard traces,
+// deterministic row sums and the source-time average.
+//
+// On GB300 the FP64 pipe delivers about 2 DFMA per clock per SM, so these
+// kernels are bound by that pipe, not by memory: the design goal is to keep the
+// pipe busy with no padded work (threads whose outputs fall outside the Nev x
+// Nev block issue no DFMA) and to keep the summation order of the reference
+// (k ascending for every matrix element).
+#include "kernels.h"
+
+namespace ctr {
+
+// ----------------------------------------------------------------- GEMM
+// C = sum_q w_q * op(A_q) * op(B_q) for Nev x Nev row-major blocks, where op is
+// identity or conjugate transpose (flags bit q: A_q, bit 4+q: B_q).  One CTA
+// computes a 32 x 32 output tile; 256 threads, 2 x 2 outputs each.
+constexpr int GT = 32;   // output tile edge
+constexpr int GK = 16;   // K chunk staged in shared memory
+
+__global__ void __launch_bounds__(256) zgemm_f64_kernel(const ZTask* __restrict__ tasks, int ntask, int N,
+                                                        int tiles_per_dim) {
+  __shared__ double2 As[GT][GK + 1];
+  __shared__ double2 Bs[GK][GT + 1];
+  const int tiles = tiles_per_dim * tiles_per_dim;
+  const int task_id = blockIdx.x / tiles;
+  if (task_id >= ntask) return;
+  const int tile = blockIdx.x % tiles;
+  const int i0 = (tile / tiles_per_dim) * GT, j0 = (tile % tiles_per_dim) * GT;
+  const ZTask& T = tasks[task_id];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+
+  double2 acc[2][2];
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++) acc[a][b] = make_double2(0.0, 0.0);
+
+  for (int q = 0; q < T.nterm; q++) {
+    const double2* A = T.A[q];
+    const double2* B = T.B[q];
+    const bool ca = (T.flags >> q) & 1, cb = (T.flags >> (4 + q)) & 1;
+    double2 part[2][2];
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++) part[a][b] = make_double2(0.0, 0.0);
+    for (int k0 = 0; k0 < N; k0 += GK) {
+      // stage A rows i0..i0+31, cols k0..k0+15 and B rows k0..k0+15, cols j0..j0+31
+      for (int e = threadIdx.x; e < GT * GK; e += 256) {
+        int r = e / GK, c = e % GK;
+        int gi = i0 + r, gk = k0 + c;
+        double2 v = make_double2(0.0, 0.0);
+        if (gi < N && gk < N) {
+          if (!ca) v = A[(size_t)gi * N + gk];
+          else { v = A[(size_t)gk * N + gi]; v.y = -v.y; }
+        }
+        As[r][c] = v;
+        int rk = e / GT, cj = e % GT;
+        int gk2 = k0 + rk, gj = j0 + cj;
+        double2 u = make_double2(0.0, 0.0);
+        if (gk2 < N && gj < N) {
+          if (!cb) u = B[(size_t)gk2 * N + gj];
+          else { u = B[(size_t)gj * N + gk2]; u.y = -u.y; }
+        }
+        Bs[rk][cj] = u;
+      }
+      __syncthreads();
+      const int kmax = min(GK, N - k0);
+      const bool r0 = i0 + ty < N, r1 = i0 + ty + 16 < N, c0 = j0 + tx < N, c1 = j0 + tx + 16 < N;
+      if (r0 || r1) {
+        for (int kk = 0; kk < kmax; kk++) {
+          double2 a0 = As[ty][kk], a1 = As[ty + 16][kk];
+          double2 b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+          if (r0 && c0) cmac(part[0][0], a0, b0);
+          if (r0 && c1) cmac(part[0][1], a0, b1);
+          if (r1 && c0) cmac(part[1][0], a1, b0);
+          if (r1 && c1) cmac(part[1][1], a1, b1);
+        }
+      }
+      __syncthreads();
+    }
+    const double2 w = make_double2((double)T.wre[q], (double)T.wim[q]);
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++) {
+        if (q == 0 && w.x == 1.0 && w.y == 0.0) acc[a][b] = part[a][b];
+        else {
+          double2 t = cmul(w, part[a][b]);
+          acc[a][b].x += t.x;
+          acc[a][b].y += t.y;
+        }
+      }
+  }
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++) {
+      int gi = i0 + ty + 16 * a, gj = j0 + tx + 16 * b;
+      if (gi < N && gj < N) T.C[(size_t)gi * N + gj] = acc[a][b];
+    }
+}
+
+// ---------------------------------------------------------------- trace
+// out = coef * sum_e X_e * conj(Y_e) over the Nev*Nev elements (mode 0), or
+// coef * sum_ij X_ij * Y_ji = coef * Tr[X Y] (mode 1).  One CTA per task; the
+// reduction tree is fixed, so results are bitwise reproducible.
+__global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restrict__ tasks, int ntask, int N) {
+  const int t = blockIdx.x;
+  if (t >= ntask) return;
+  const TraceTask& T = tasks[t];
+  const int n2 = N * N;
+  double re = 0.0, im = 0.0;
+  if (T.mode == 0) {
+    for (int e = threadIdx.x; e < n2; e += 256) {
+      double2 x = T.X[e], y = T.Y[e];
+      re += x.x * y.x + x.y * y.y;
+      im += x.y * y.x - x.x * y.y;
+    }
+  } else {
+    for (int e = threadIdx.x; e < n2; e += 256) {
+      int i = e / N, j = e % N;
+      double2 x = T.X[e], y = T.Y[(size_t)j * N + i];
+      re += x.x * y.x - x.y * y.y;
+      im += x.x * y.y + x.y * y.x;
+    }
+  }
+  re = block_sum_256(re);
+  im = block_sum_256(im);
+  if (threadIdx.x == 0) {
+    double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+    double2 s = make_double2(re, im);
+    *T.out = cmul(c, s);
+  }
+}
+
+// ------------------------------------------------------------- row sums
+// out[p][o] = sum_{k in [off[o], off[o+1])} rows[p][idx[k]]  (ascending idx)
+__global__ void rowsum_kernel(const double2* __restrict__ rows, int nrows, const int* __restrict__ off,
+                              const int* __restrict__ idx, int nout, int npair, double2* __restrict__ out,
+                              size_t out_pair_stride) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= npair * nout) return;
+  int p = g / nout, o = g % nout;
+  double re = 0.0, im = 0.0;
+  for (int k = off[o]; k < off[o + 1]; k++) {
+    double2 v = rows[(size_t)p * nrows + idx[k]];
+    re += v.x;
+    im += v.y;
+  }
+  out[(size_t)p * out_pair_stride + o] = make_double2(re, im);
+}
+
+// -------------------------------------------------------- source average
+__global__ void source_average_kernel(int Nt, int ncorr, const double2* __restrict__ corr, double scale,
+                                      double2* __restrict__ avg) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= Nt * ncorr) return;
+  int dt = g / ncorr, c = g % ncorr;
+  double re = 0.0, im = 0.0;
+  for (int ti = 0; ti < Nt; ti++) {
+    int tf = (ti + dt) % Nt;
+    double2 v = corr[((size_t)tf * Nt + ti) * ncorr + c];
+    re += v.x;
+    im += v.y;
+  }
+  avg[g] = make_double2(re / Nt * scale, im / Nt * scale);
+}
+
+// --------------------------------------------------------------- launchers
+int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s) {
+  if (ntask == 0) return CTR_OK;
+  int tpd = (N + GT - 1) / GT;
+  long long blocks = (long long)ntask * tpd * tpd;
+  if (blocks > 0x7fffffffLL) return fail(CTR_ERR_ARG, "zgemm_f64: too many tasks (%d)", ntask);
+  TimedLaunch tl(s, "zgemm_f64");
+  zgemm_f64_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_tasks, ntask, N, tpd);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_trace_f64(const TraceTask* d_tasks, int ntask, int N, cudaStream_t s) {
+  if (ntask == 0) return CTR_OK;
+  TimedLaunch tl(s, "trace_f64");
+  trace_f64_kernel<<<ntask, 256, 0, s>>>(d_tasks, ntask, N);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_rowsum(const double2* rows, int nrows, const int* off, const int* idx, int nout, int npair,
+                  double2* out, size_t out_pair_stride, cudaStream_t s) {
+  int n = npair * nout;
+  if (n == 0) return CTR_OK;
+  TimedLaunch tl(s, "rowsum");
+  rowsum_kernel<<<(n + 255) / 256, 256, 0, s>>>(rows, nrows, off, idx, nout, npair, out, out_pair_stride);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_source_average(int Nt, int ncorr, const double2* corr, double scale, double2* avg, cudaStream_t s) {
+  int n = Nt * ncorr;
+  if (n == 0) return CTR_OK;
+  TimedLaunch tl(s, "source_average");
+  source_average_kernel<<<(n + 255) / 256, 256, 0, s>>>(Nt, ncorr, corr, scale, avg);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+}  // namespace ctr

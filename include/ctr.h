@@ -1,0 +1,114 @@
+/*
+ * ctr.h -- C ABI of the GB300 distillation contraction engine (libctr.so).
+ *
+ * Plain C: pointers, sizes and int status codes.  Every routine returns CTR_OK
+ * (0) or an error code; ctr_last_error() gives the message of the last failure
+ * on the calling thread.  Nothing here terminates the process (the C++ layer in
+ * interface.h/contract.h turns errors into the reference's ABORT behaviour).
+ *
+ * Data are complex128 stored as interleaved (re, im) doubles, in the layouts of
+ * the reference library:
+ *   perambulator tau(t1,t2)_{s1 s2}^{v1 v2}: [t1][t2][s1][s2][v1][v2]
+ *       (lib/contract.cpp:531-534).  "prop rows" = the rows t1 in [tf_begin,
+ *       tf_end) of that array, i.e. a pointer to tau(tf_begin, 0).
+ *   tau(t,t) ("prop diag"): [t][s1][s2][v1][v2]   (lib/contract.cpp:565)
+ *   elementals Phi: [t][op][r][c]  with op count 5 (rho), 2 (sigma x2) or 1
+ *       (lib/interface.cpp:25, :258, :85).
+ * Device pointers must be 16-byte aligned.  "stream" is a cudaStream_t (NULL =
+ * legacy default stream).  Calls are asynchronous on that stream unless noted.
+ *
+ * Engines:
+ *   CTR_ENGINE_FP64   plain FP64 (the drop-in; <= 1e-12 relative to the oracle)
+ *   CTR_ENGINE_SPLIT  split-precision tensor-core form: FP64 operands sliced
+ *                     into BF16 pieces, tcgen05 MMA with FP32 accumulation in
+ *                     TMEM, float-float recombination (<= 1e-9 relative).
+ */
+#ifndef CTR_H
+#define CTR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTR_OK 0
+#define CTR_ERR_ARG 1          /* invalid argument (size, pointer, index) */
+#define CTR_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define CTR_ERR_ALLOC 3        /* device or host allocation failed */
+#define CTR_ERR_UNSUPPORTED 4  /* device is not sm_103 / feature not built */
+#define CTR_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
+#define CTR_ERR_IO 6           /* file missing, truncated or malformed */
+
+#define CTR_ENGINE_FP64 0
+#define CTR_ENGINE_SPLIT 1
+
+int ctr_version(void);
+const char* ctr_error_string(int code);
+const char* ctr_last_error(void);
+
+/* Select the CUDA device and check it is a Blackwell sm_103 part
+ * (replaces initDevice/initContract's device handling, lib/contract.cpp:25-70). */
+int ctr_device_init(int device);
+
+/* ---------------------------------------------------------------- tables
+ * The diagram tables of include/constants_*.h, generated by the library from
+ * the gamma matrices (devTools/comb_*.cpp).  Caller-owned host arrays. */
+int ctr_table_rho(int16_t* spin /*768x4*/, int16_t* lp_rp /*768x2*/, float* coef /*768x2*/);
+int ctr_table_rhopi(int16_t* spin /*768x6*/, int16_t* ip /*768*/, float* coef /*768x2*/);
+int ctr_table_pipi(int16_t* sq_spin /*256x6*/, float* sq_coef /*256x2*/, int16_t* dt_spin /*256x6*/,
+                   float* dt_coef /*256x2*/, int16_t* dth_spin /*256x4*/, float* dth_coef /*256x2*/);
+int ctr_table_sigma(int16_t* spin /*64x4*/, int16_t* lp_rp /*64x2*/, float* coef /*64x2*/);
+int ctr_table_sigmapi(int16_t* hf_spin /*16x2*/, float* hf_coef /*16x2*/, int16_t* tri_spin /*128x5*/,
+                      int16_t* tri_ip /*128*/, float* tri_coef /*128x2*/);
+
+/* ------------------------------------------------------ rho-type diagrams
+ * Generic two-sided contraction, the form of the rho-rho and sigma-sigma
+ * kernels (lib/calculate_rho_core.h, lib/calculate_sigma_one_fish_core.h):
+ *   row(tf,ti,r) = coef_r * sum_ij conj( (Phi_{R_r}(tf) tau(tf,ti)_{a_r b_r})_ij )
+ *                                    * (tau(tf,ti)_{c_r d_r} Phi_{L_r}(ti))_ij
+ *   out[tf][ti][o] = sum over rows r with out_index[r] == o (ascending r).
+ * rows: host array [nrows][6] = (a, b, c, d, L, R); coef host [nrows][2];
+ * out_index host [nrows].  phi: device [Nt][nphi][N][N].  out: device
+ * [tf_end-tf_begin][Nt][nout] complex. */
+int ctr_twosided(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
+                 const double* phi, int nphi, int nrows, const int16_t* rows, const float* coef,
+                 const int32_t* out_index, int nout, double* out, void* stream);
+
+/* rho-rho: run_ContractRho for t_sink rows [tf_begin, tf_end) (lib/contract_kernels_rho.cu:69-138).
+ * mom5 device [Nt][5][N][N]; corr device [tf_end-tf_begin][Nt][16][3]. */
+int ctr_rho(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
+            const double* mom5, double* corr, void* stream);
+
+/* sigma-sigma one-fish: run_ContractSigma (lib/contract_kernels_sigma.cu:69-147).
+ * mom2 device [Nt][2][N][N]; corr device [tf_end-tf_begin][Nt][4]. */
+int ctr_sigma(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
+              const double* mom2, double* corr, void* stream);
+
+/* On-device source-time average of the dumpData routines (lib/contract.cpp:616-643):
+ * avg[dt][c] = scale/Nt * sum_ti corr[(ti+dt)%Nt][ti][c]; corr device [Nt][Nt][ncorr]. */
+int ctr_source_average(int nt, int ncorr, const double* corr, double scale, double* avg, void* stream);
+
+/* 1 when the split-precision tensor-core engine is compiled in. */
+int ctr_split_available(void);
+
+/* Synchronise the stream and report the first device-side error flag. */
+int ctr_sync(void* stream);
+
+/* Free the library's cached device scratch buffers (synchronises the device). */
+void ctr_release_workspace(void);
+
+/* Launch accounting.  Every kernel launch of the library is counted per kernel
+ * name; with timing enabled a CUDA event pair is recorded on the launching
+ * stream around each launch.  ctr_timing_enable() clears previous records.
+ * ctr_timing_report() waits for the recorded events and writes JSON
+ * {"kernel": [launches, timed_launches, total_ms], ...} into buf. */
+void ctr_timing_enable(int on);
+long long ctr_launch_count(void);
+int ctr_timing_report(char* buf, int buflen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTR_H */

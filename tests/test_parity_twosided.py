@@ -1,0 +1,82 @@
+"""GPU parity of the rho-type (two-sided) contractions against the oracle.
+
+Plain FP64 engine: <= 1e-12 relative to the largest |entry| of the compared
+set (entry-wise relative errors of near-cancelling entries are reported by the
+bench, not gated here).  Split engine: <= 1e-9 on the same scale."""
+import numpy as np
+import pytest
+import torch
+
+from contractions_code_scattering_gb300 import api, synth
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "split": 1e-9}
+
+
+def _inputs(nt, n, seed, nops=5):
+    prop = synth.make_prop(nt, n, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    mom = np.stack([synth.make_phi_random(nt, n, rng) for _ in range(nops)], axis=1)
+    return prop, np.ascontiguousarray(mom)
+
+
+def _close(got, ref, tol):
+    scale = np.abs(ref).max()
+    err = np.abs(got - ref).max() / scale
+    assert err <= tol, "max error %.3e relative to max |entry| (tolerance %.1e)" % (err, tol)
+
+
+@pytest.mark.parametrize("engine", ["fp64"])
+@pytest.mark.parametrize("nt,n", [(3, 16), (2, 37), (1, 1), (4, 8)])
+def test_rho_matches_oracle(cuda, engine, nt, n):
+    prop, mom5 = _inputs(nt, n, seed=100 + n)
+    ref = O.rho(prop, mom5)
+    got = api.run_contract_rho(torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda), engine=engine)
+    _close(got.cpu().numpy(), ref, TOL[engine])
+
+
+@pytest.mark.parametrize("engine", ["fp64"])
+def test_rho_single_row_buffer(cuda, engine):
+    """Row-by-row use, as Contract_rho_rho::contractRho drives run_ContractRho (lib/contract.cpp:602-605)."""
+    nt, n = 4, 12
+    prop, mom5 = _inputs(nt, n, seed=7)
+    d_mom = torch.from_numpy(mom5).to(cuda)
+    for tf in range(nt):
+        row = torch.from_numpy(np.ascontiguousarray(prop[tf:tf + 1])).to(cuda)
+        got = api.run_contract_rho(row, d_mom, engine=engine, tf_range=(tf, tf + 1))
+        _, ref = O.rho_row(prop, mom5, tf)
+        _close(got[0].cpu().numpy(), ref, TOL[engine])
+
+
+@pytest.mark.parametrize("engine", ["fp64"])
+def test_sigma_matches_oracle(cuda, engine):
+    nt, n = 3, 20
+    prop, mom2 = _inputs(nt, n, seed=9, nops=2)
+    ref = O.sigma(prop, mom2)
+    got = api.run_contract_sigma(torch.from_numpy(prop).to(cuda), torch.from_numpy(mom2).to(cuda), engine=engine)
+    _close(got.cpu().numpy(), ref, TOL[engine])
+
+
+def test_rho_config0_shape(cuda):
+    """CPU-sized rho two-point: Nev=32, Lt=16, p=0 Hermitian elementals."""
+    nt, n = 16, 32
+    prop = synth.make_prop(nt, n, seed=1000)
+    phi0 = synth.make_phi_hermitian(nt, n, seed=1001)
+    rng = np.random.default_rng(1002)
+    mom5 = np.stack([phi0] + [synth.make_phi_random(nt, n, rng) for _ in range(4)], axis=1)
+    mom5 = np.ascontiguousarray(mom5)
+    ref = O.rho(prop, mom5)
+    got = api.run_contract_rho(torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda), engine="fp64")
+    got = got.cpu().numpy()
+    _close(got, ref, 1e-12)
+    avg = api.source_average(torch.from_numpy(got).to(cuda)).cpu().numpy()
+    _close(avg, O.source_average(ref), 1e-12)
+
+
+def test_source_average(cuda):
+    rng = np.random.default_rng(0)
+    corr = rng.normal(size=(6, 6, 4)) + 1j * rng.normal(size=(6, 6, 4))
+    got = api.source_average(torch.from_numpy(corr).to(cuda), scale=-2.0).cpu().numpy()
+    assert np.allclose(got, -2.0 * O.source_average(corr), rtol=1e-14, atol=1e-15)

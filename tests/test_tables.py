@@ -1,0 +1,58 @@
+"""Diagram tables: the oracle's generator and the library's generator both
+reproduce the reference's shipped include/constants_*.h token for token."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import tables as T
+from tests.golden.make_table_fixtures import digest, parse_header
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = json.load(open(os.path.join(HERE, "golden", "tables_ref.json")))
+
+
+def test_fixture_lists_every_table():
+    assert len(REF) == 20
+
+
+@pytest.mark.parametrize("name", sorted(REF))
+def test_oracle_generator_matches_reference_digest(name):
+    mine = T.all_tables()[name]
+    assert list(mine.shape) == REF[name]["shape"]
+    assert digest(T.format_values(mine)) == REF[name]["sha256"]
+
+
+def test_library_tables_match_oracle():
+    from contractions_code_scattering_gb300 import api
+    lib_t = api.tables()
+    ora = T.all_tables()
+    assert set(lib_t) == set(ora)
+    for k in ora:
+        a, b = lib_t[k], ora[k]
+        assert a.shape == b.shape, k
+        if b.dtype.kind == "f":
+            # float32 in the library, as in the reference's __constant__ copies; signs of zero included
+            assert T.format_values(a.astype(np.float64)) == T.format_values(b), k
+            assert np.array_equal(np.signbit(a), np.signbit(b.astype(np.float32))), k
+        else:
+            assert np.array_equal(a, b), k
+        assert digest(T.format_values(a)) == REF[k]["sha256"], k
+
+
+def test_gamma5_is_chiral_diag():
+    g1, g2, g3, g4, g5 = T.gamma_matrices()
+    assert np.allclose(g5, np.diag([1, 1, -1, -1]))
+    for g in (g1, g2, g3, g4):
+        assert np.allclose(g @ g, np.eye(4))
+        assert np.allclose(g, g.conj().T)
+        assert np.allclose(g @ g5, -g5 @ g)
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/include"), reason="reference tree not mounted")
+def test_direct_against_reference_headers():
+    import glob
+    for f in glob.glob("/root/reference/include/constants_*.h"):
+        for name, t in parse_header(f).items():
+            assert T.format_values(T.all_tables()[name]) == t["tokens"], name
