@@ -48,6 +48,8 @@ def lib(build_if_missing=True):
     L.ctr_sigma.argtypes = [i, i, i, i, i, vp, vp, vp, vp]
     L.ctr_source_average.argtypes = [i, i, vp, d, vp, vp]
     L.ctr_sync.argtypes = [vp]
+    L.ctr_zgemm_batched.argtypes = [i, i, i, vp, vp, vp, vp]
+    L.ctr_split_levels.argtypes = [i, vp, vp, vp, vp]
     L.ctr_split_available.restype = i
     L.ctr_release_workspace.restype = None
     L.ctr_timing_enable.argtypes = [i]

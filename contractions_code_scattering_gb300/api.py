@@ -123,6 +123,27 @@ def run_contract_sigma(prop_rows, mom2, engine="fp64", tf_range=None, out=None, 
     return out
 
 
+def zgemm_batched(x, y, engine="fp64", out=None, stream=None):
+    """Block products out[b] = x[b] @ y[b] for device tensors [nb, N, N] complex128."""
+    import torch
+    nb, n = x.shape[0], x.shape[-1]
+    if out is None:
+        out = torch.empty_like(x)
+    for t, nm in ((x, "x"), (y, "y"), (out, "out")):
+        _dev(t, nm)
+    stride = n * n * 16
+    px = (ctypes.c_void_p * nb)(*[x.data_ptr() + b * stride for b in range(nb)])
+    py = (ctypes.c_void_p * nb)(*[y.data_ptr() + b * stride for b in range(nb)])
+    pc = (ctypes.c_void_p * nb)(*[out.data_ptr() + b * stride for b in range(nb)])
+    check(lib().ctr_zgemm_batched(_engine(engine), n, nb, px, py, pc, _stream(stream)))
+    return out
+
+
+def sync(stream=None):
+    """Synchronise the stream and raise if a device-side wait of the split engine timed out."""
+    check(lib().ctr_sync(_stream(stream)))
+
+
 def source_average(corr, scale=1.0, stream=None):
     """dumpData's average over source times: [Nt, Nt, ...] -> [Nt, ...] (device)."""
     import torch
@@ -153,3 +174,14 @@ def rho_rows_for_momenta(nmom, ico=0):
 
 __all__ = ["CtrError", "device_init", "tables", "twosided", "run_contract_rho", "run_contract_sigma",
            "source_average", "rho_rows_for_momenta", "ENGINES"]
+
+
+def split_levels(x, y, stream=None):
+    """Diagnostics: raw tensor-core accumulators of the split product x @ y
+    ([N,N] complex128 device tensors) -> float32 [6, N, N] (Re l0, l1, l>=2, Im l0, l1, l>=2)."""
+    import torch
+    n = x.shape[-1]
+    lv = torch.zeros((6, n, 128), dtype=torch.float32, device=x.device)
+    check(lib().ctr_split_levels(n, _dev(x, "x"), _dev(y, "y"), ctypes.c_void_p(lv.data_ptr()), _stream(stream)))
+    sync(stream)
+    return lv[:, :, :n].transpose(1, 2)

@@ -75,7 +75,23 @@ struct Workspace {
   void release();
 };
 Workspace& workspace(int slot);
-enum { WS_SCRATCH = 0, WS_TASKS = 1, WS_ROWS = 2, WS_SLICES = 3, WS_MISC = 4, WS_COUNT = 5 };
+enum {
+  WS_SCRATCH = 0,   // per-batch products / sliced operands
+  WS_TASKS,         // uploaded task lists (several independent slots)
+  WS_TASKS2,
+  WS_GEMM_A,
+  WS_GEMM_B,
+  WS_ROWTASKS,
+  WS_ROWS,          // per-row partial results
+  WS_PHI,           // sliced elementals
+  WS_MISC,          // small tables (CSR of output rows)
+  WS_COUNT
+};
+
+// Reads (and clears) the device-side error flag of the split engine; syncs the stream.
+int split_error_check(cudaStream_t s);
+int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,
+                        cudaStream_t stream);
 
 // Upload a host array into a workspace slot (async on stream, host buffer is
 // kept alive by a pinned staging copy owned by the slot).

@@ -135,7 +135,7 @@ int twosided_fp64(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
     CTR_TRY(upload(WS_TASKS, gt.data(), gt.size() * sizeof(ZTask), &d_gt, stream));
     CTR_TRY(launch_zgemm_f64((const ZTask*)d_gt, (int)gt.size(), N, stream));
     // The trace tasks live behind the GEMM tasks in a second upload slot.
-    CTR_TRY(upload(WS_SLICES, tt.data(), tt.size() * sizeof(TraceTask), &d_tt, stream));
+    CTR_TRY(upload(WS_ROWTASKS, tt.data(), tt.size() * sizeof(TraceTask), &d_tt, stream));
     CTR_TRY(launch_trace_f64((const TraceTask*)d_tt, (int)tt.size(), N, stream));
     CTR_TRY(launch_rowsum(R, nrows, d_off, d_idx, nout, np, (double2*)out + (size_t)p0 * nout, nout, stream));
   }
@@ -245,7 +245,32 @@ int ctr_source_average(int nt, int ncorr, const double* corr, double scale, doub
 int ctr_sync(void* stream) {
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return ctr::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
-  return CTR_OK;
+  return ctr::split_error_check((cudaStream_t)stream);
+}
+
+int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, const double* const* y,
+                      double* const* c, void* stream) {
+  if (engine != CTR_ENGINE_FP64 && engine != CTR_ENGINE_SPLIT) return ctr::fail(CTR_ERR_ARG, "unknown engine %d", engine);
+  if (nev < 1 || nbatch < 0 || (nbatch > 0 && (!x || !y || !c)))
+    return ctr::fail(CTR_ERR_ARG, "ctr_zgemm_batched: bad arguments");
+  for (int b = 0; b < nbatch; b++)
+    if (!x[b] || !y[b] || !c[b] || (((uintptr_t)x[b] | (uintptr_t)y[b] | (uintptr_t)c[b]) & 15))
+      return ctr::fail(CTR_ERR_ARG, "ctr_zgemm_batched: null or misaligned pointer in entry %d", b);
+  if (nbatch == 0) return CTR_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (engine == CTR_ENGINE_SPLIT) return ctr::zgemm_split_batched(nev, nbatch, x, y, c, s);
+  std::vector<ctr::ZTask> t(nbatch);
+  for (int b = 0; b < nbatch; b++) {
+    t[b] = ctr::ZTask{};
+    t[b].A[0] = (const double2*)x[b];
+    t[b].B[0] = (const double2*)y[b];
+    t[b].C = (double2*)c[b];
+    t[b].wre[0] = 1.f;
+    t[b].nterm = 1;
+  }
+  void* d;
+  CTR_TRY(ctr::upload(ctr::WS_TASKS, t.data(), t.size() * sizeof(ctr::ZTask), &d, s));
+  return ctr::launch_zgemm_f64((const ctr::ZTask*)d, nbatch, nev, s);
 }
 
 }  // extern "C"

@@ -1,0 +1,332 @@
+// Host orchestration of the split-precision engine: two-sided (rho-type)
+// contractions and batched block products.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "kernels.h"
+#include "split.h"
+
+namespace ctr {
+
+namespace {
+
+int* g_err_dev = nullptr;
+
+int err_flag(int** out) {
+  if (!g_err_dev) {
+    CTR_CUDA(cudaMalloc(&g_err_dev, sizeof(int)));
+    CTR_CUDA(cudaMemset(g_err_dev, 0, sizeof(int)));
+  }
+  *out = g_err_dev;
+  return CTR_OK;
+}
+
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// ff complex (column-major, ld) -> complex128 row-major nev x nev
+__global__ void ff_to_f64_kernel(const float4* __restrict__ src, int ld, int nev, double2* __restrict__ dst) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nev * nev) return;
+  const int i = e / nev, j = e % nev;
+  const float4 v = src[(size_t)j * ld + i];
+  dst[e] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+
+}  // namespace
+
+int split_error_check(cudaStream_t s) {
+  if (!g_err_dev) return CTR_OK;
+  int h = 0;
+  CTR_CUDA(cudaMemcpyAsync(&h, g_err_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CTR_CUDA(cudaStreamSynchronize(s));
+  if (h != 0) {
+    CTR_CUDA(cudaMemsetAsync(g_err_dev, 0, sizeof(int), s));
+    return fail(CTR_ERR_TIMEOUT, "split GEMM pipeline wait timed out (stage %d)", h);
+  }
+  return CTR_OK;
+}
+
+// Slice Nt elementals stacked [op list] as left and right operands.
+struct PhiSlices {
+  int nblk = 0, mtiles = 0, ntiles = 0;
+  size_t left_bytes = 0, right_bytes = 0, lexp_n = 0, rexp_n = 0;
+  uint8_t* left = nullptr;   // [Nt][mtiles][nchunk][A_STAGE]
+  uint8_t* right = nullptr;  // [Nt][ntiles][nchunk][B_STAGE]
+  int* lexp = nullptr;       // [Nt][mtiles*128]
+  int* rexp = nullptr;       // [Nt][ntiles*80]
+};
+
+static size_t phi_bytes(int N, int Nt, int nL, int nR, int nchunk) {
+  const int mt = cdiv(nR * N, SPLIT_M), nt = cdiv(nL * N, SPLIT_N);
+  return align256((size_t)Nt * mt * nchunk * SPLIT_A_STAGE) + align256((size_t)Nt * nt * nchunk * SPLIT_B_STAGE) +
+         align256((size_t)Nt * mt * SPLIT_M * 4) + align256((size_t)Nt * nt * SPLIT_N * 4);
+}
+
+int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* phi, int nphi,
+                   const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
+                   const std::vector<int32_t>& out_index, int nout, double* out, cudaStream_t stream) {
+  if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d (got %d)", SPLIT_MAXK, N);
+  const int nrows = (int)rows.size();
+  for (int r = 0; r < nrows; r++) {
+    const TwoSidedRow& w = rows[r];
+    if (w.a < 0 || w.a > 3 || w.b < 0 || w.b > 3 || w.c < 0 || w.c > 3 || w.d < 0 || w.d > 3 || w.L < 0 ||
+        w.L >= nphi || w.R < 0 || w.R >= nphi || out_index[r] < 0 || out_index[r] >= nout)
+      return fail(CTR_ERR_ARG, "two-sided row %d out of range", r);
+  }
+  // distinct source blocks (c,d), source elementals L, sink blocks (a,b), sink elementals R
+  std::vector<int> cdl, Ll, abl, Rl;
+  auto idx = [](std::vector<int>& v, int x) {
+    auto it = std::find(v.begin(), v.end(), x);
+    if (it != v.end()) return (int)(it - v.begin());
+    v.push_back(x);
+    return (int)v.size() - 1;
+  };
+  std::vector<int> ia(nrows), il(nrows), ib(nrows), ir(nrows);
+  for (int r = 0; r < nrows; r++) {
+    ia[r] = idx(cdl, rows[r].c * 4 + rows[r].d);
+    il[r] = idx(Ll, rows[r].L);
+    ib[r] = idx(abl, rows[r].a * 4 + rows[r].b);
+    ir[r] = idx(Rl, rows[r].R);
+  }
+  if ((int)Ll.size() > SPLIT_MAXBLK || (int)Rl.size() > SPLIT_MAXBLK)
+    return fail(CTR_ERR_ARG, "too many distinct elementals (max %d)", SPLIT_MAXBLK);
+  const int nchunk = cdiv(N, SPLIT_K);
+  const int ncd = (int)cdl.size(), nab = (int)abl.size(), nL = (int)Ll.size(), nR = (int)Rl.size();
+  const size_t N2 = (size_t)N * N;
+  const double2* tau = (const double2*)prop_rows;
+  const double2* ph = (const double2*)phi;
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+
+  // ---- elementals, sliced once per call
+  PhiSlices F;
+  F.mtiles = cdiv(nR * N, SPLIT_M);
+  F.ntiles = cdiv(nL * N, SPLIT_N);
+  void* phimem;
+  CTR_TRY(workspace(WS_PHI).get(phi_bytes(N, Nt, nL, nR, nchunk), &phimem));
+  {
+    uint8_t* p = (uint8_t*)phimem;
+    F.left = p;
+    p += align256((size_t)Nt * F.mtiles * nchunk * SPLIT_A_STAGE);
+    F.right = p;
+    p += align256((size_t)Nt * F.ntiles * nchunk * SPLIT_B_STAGE);
+    F.lexp = (int*)p;
+    p += align256((size_t)Nt * F.mtiles * SPLIT_M * 4);
+    F.rexp = (int*)p;
+  }
+  {
+    std::vector<SliceLeftJob> lj(Nt);
+    std::vector<SliceRightJob> rj(Nt);
+    for (int t = 0; t < Nt; t++) {
+      SliceLeftJob& L = lj[t];
+      std::memset(&L, 0, sizeof(L));
+      for (int k = 0; k < nR; k++) L.blk[k] = ph + ((size_t)t * nphi + Rl[k]) * N2;
+      L.rows = nR * N;
+      L.out = F.left + (size_t)t * F.mtiles * nchunk * SPLIT_A_STAGE;
+      L.exps = F.lexp + (size_t)t * F.mtiles * SPLIT_M;
+      SliceRightJob& R = rj[t];
+      std::memset(&R, 0, sizeof(R));
+      for (int k = 0; k < nL; k++) R.blk[k] = ph + ((size_t)t * nphi + Ll[k]) * N2;
+      R.cols = nL * N;
+      R.out = F.right + (size_t)t * F.ntiles * nchunk * SPLIT_B_STAGE;
+      R.exps = F.rexp + (size_t)t * F.ntiles * SPLIT_N;
+    }
+    void *dl, *dr;
+    CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &dl, stream));
+    CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, Nt, N, nchunk, F.mtiles, stream));
+    CTR_TRY(upload(WS_TASKS2, rj.data(), rj.size() * sizeof(SliceRightJob), &dr, stream));
+    CTR_TRY(launch_slice_right((const SliceRightJob*)dr, Nt, N, nchunk, F.ntiles, stream));
+  }
+
+  // ---- per (t_sink, t_src) pair buffers
+  const int mtT = cdiv(ncd * N, SPLIT_M), ntT = cdiv(nab * N, SPLIT_N);
+  const int ldA = mtT * SPLIT_M, ldB = F.mtiles * SPLIT_M;
+  const size_t tl_b = align256((size_t)mtT * nchunk * SPLIT_A_STAGE), tr_b = align256((size_t)ntT * nchunk * SPLIT_B_STAGE);
+  const size_t tle_b = align256((size_t)mtT * SPLIT_M * 4), tre_b = align256((size_t)ntT * SPLIT_N * 4);
+  const size_t a_b = align256((size_t)F.ntiles * SPLIT_N * ldA * sizeof(float4));
+  const size_t b_b = align256((size_t)ntT * SPLIT_N * ldB * sizeof(float4));
+  const size_t per_pair = tl_b + tr_b + tle_b + tre_b + a_b + b_b;
+  const int npairs_total = (tf_end - tf_begin) * Nt;
+  const size_t budget = (size_t)6 << 30;
+  int batch = (int)std::max<size_t>(1, budget / per_pair);
+  batch = std::min(batch, npairs_total);
+
+  // CSR of output rows
+  std::vector<int> off(nout + 1, 0), ord(nrows);
+  for (int r = 0; r < nrows; r++) off[out_index[r] + 1]++;
+  for (int o = 0; o < nout; o++) off[o + 1] += off[o];
+  {
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (int r = 0; r < nrows; r++) ord[fill[out_index[r]]++] = r;
+  }
+  std::vector<int> csr(off);
+  csr.insert(csr.end(), ord.begin(), ord.end());
+  void* d_csr;
+  CTR_TRY(upload(WS_MISC, csr.data(), csr.size() * sizeof(int), &d_csr, stream));
+
+  std::vector<SliceLeftJob> lj;
+  std::vector<SliceRightJob> rj;
+  std::vector<SplitGemmInst> ga, gb;
+  std::vector<TraceFFTask> tt;
+  for (int p0 = 0; p0 < npairs_total; p0 += batch) {
+    const int np = std::min(batch, npairs_total - p0);
+    void *mem, *rowbuf;
+    CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * per_pair, &mem));
+    CTR_TRY(workspace(WS_ROWS).get((size_t)np * nrows * sizeof(double2), &rowbuf));
+    uint8_t* base = (uint8_t*)mem;
+    double2* R = (double2*)rowbuf;
+    lj.assign(np, SliceLeftJob{});
+    rj.assign(np, SliceRightJob{});
+    ga.resize(np);
+    gb.resize(np);
+    tt.resize((size_t)np * nrows);
+    for (int q = 0; q < np; q++) {
+      const int pr = p0 + q;
+      const int tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
+      const double2* tblk = tau + ((size_t)tfl * Nt + ti) * 16 * N2;
+      uint8_t* pb = base + (size_t)q * per_pair;
+      uint8_t* TL = pb;
+      uint8_t* TR = TL + tl_b;
+      int* TLe = (int*)(TR + tr_b);
+      int* TRe = (int*)((uint8_t*)TLe + tle_b);
+      float4* A = (float4*)((uint8_t*)TRe + tre_b);
+      float4* B = (float4*)((uint8_t*)A + a_b);
+      SliceLeftJob& L = lj[q];
+      std::memset(&L, 0, sizeof(L));
+      for (int k = 0; k < ncd; k++) L.blk[k] = tblk + (size_t)cdl[k] * N2;
+      L.rows = ncd * N;
+      L.out = TL;
+      L.exps = TLe;
+      SliceRightJob& Rj = rj[q];
+      std::memset(&Rj, 0, sizeof(Rj));
+      for (int k = 0; k < nab; k++) Rj.blk[k] = tblk + (size_t)abl[k] * N2;
+      Rj.cols = nab * N;
+      Rj.out = TR;
+      Rj.exps = TRe;
+      ga[q] = SplitGemmInst{TL, F.right + (size_t)ti * F.ntiles * nchunk * SPLIT_B_STAGE, TLe,
+                            F.rexp + (size_t)ti * F.ntiles * SPLIT_N, A};
+      gb[q] = SplitGemmInst{F.left + (size_t)tf * F.mtiles * nchunk * SPLIT_A_STAGE, TR,
+                            F.lexp + (size_t)tf * F.mtiles * SPLIT_M, TRe, B};
+      for (int r = 0; r < nrows; r++) {
+        TraceFFTask& t = tt[(size_t)q * nrows + r];
+        t.a = A + (size_t)il[r] * N * ldA + (size_t)ia[r] * N;
+        t.lda = ldA;
+        t.b = B + (size_t)ib[r] * N * ldB + (size_t)ir[r] * N;
+        t.ldb = ldB;
+        t.out = R + (size_t)q * nrows + r;
+        t.coef[0] = coef[2 * r];
+        t.coef[1] = coef[2 * r + 1];
+      }
+    }
+    void *d_lj, *d_rj, *d_ga, *d_gb, *d_tt;
+    CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &d_lj, stream));
+    CTR_TRY(launch_slice_left((const SliceLeftJob*)d_lj, np, N, nchunk, mtT, stream));
+    CTR_TRY(upload(WS_TASKS2, rj.data(), rj.size() * sizeof(SliceRightJob), &d_rj, stream));
+    CTR_TRY(launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream));
+    CTR_TRY(upload(WS_GEMM_A, ga.data(), ga.size() * sizeof(SplitGemmInst), &d_ga, stream));
+    CTR_TRY(upload(WS_GEMM_B, gb.data(), gb.size() * sizeof(SplitGemmInst), &d_gb, stream));
+    SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
+    CTR_TRY(launch_split_gemm(GA, np, d_err, stream));
+    SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
+    CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
+    CTR_TRY(upload(WS_ROWTASKS, tt.data(), tt.size() * sizeof(TraceFFTask), &d_tt, stream));
+    CTR_TRY(launch_trace_ff((const TraceFFTask*)d_tt, (int)tt.size(), N, stream));
+    CTR_TRY(launch_rowsum(R, nrows, (const int*)d_csr, (const int*)d_csr + (nout + 1), nout, np,
+                          (double2*)out + (size_t)p0 * nout, nout, stream));
+  }
+  return CTR_OK;
+}
+
+// Batched block products C_b = X_b Y_b through the split engine (unit-level access
+// to the tensor-core GEMM; results converted back to complex128).
+int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,
+                        cudaStream_t stream) {
+  if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d", SPLIT_MAXK);
+  const int nchunk = cdiv(N, SPLIT_K), nt = cdiv(N, SPLIT_N);
+  const size_t l_b = align256((size_t)nchunk * SPLIT_A_STAGE), r_b = align256((size_t)nt * nchunk * SPLIT_B_STAGE);
+  const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)nt * SPLIT_N * 4);
+  const int ldo = SPLIT_M;
+  const size_t o_b = align256((size_t)nt * SPLIT_N * ldo * sizeof(float4));
+  const size_t per = l_b + r_b + le_b + re_b + o_b;
+  void* mem;
+  CTR_TRY(workspace(WS_SCRATCH).get((size_t)nb * per, &mem));
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  std::vector<SliceLeftJob> lj(nb);
+  std::vector<SliceRightJob> rj(nb);
+  std::vector<SplitGemmInst> gi(nb);
+  for (int b = 0; b < nb; b++) {
+    uint8_t* p = (uint8_t*)mem + (size_t)b * per;
+    std::memset(&lj[b], 0, sizeof(SliceLeftJob));
+    std::memset(&rj[b], 0, sizeof(SliceRightJob));
+    lj[b].blk[0] = (const double2*)x[b];
+    lj[b].rows = N;
+    lj[b].out = p;
+    lj[b].exps = (int*)(p + l_b + r_b);
+    rj[b].blk[0] = (const double2*)y[b];
+    rj[b].cols = N;
+    rj[b].out = p + l_b;
+    rj[b].exps = (int*)(p + l_b + r_b + le_b);
+    gi[b] = SplitGemmInst{p, p + l_b, lj[b].exps, rj[b].exps, (float4*)(p + l_b + r_b + le_b + re_b)};
+  }
+  void *dl, *dr, *dg;
+  CTR_TRY(upload(WS_TASKS, lj.data(), nb * sizeof(SliceLeftJob), &dl, stream));
+  CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, nb, N, nchunk, 1, stream));
+  CTR_TRY(upload(WS_TASKS2, rj.data(), nb * sizeof(SliceRightJob), &dr, stream));
+  CTR_TRY(launch_slice_right((const SliceRightJob*)dr, nb, N, nchunk, nt, stream));
+  CTR_TRY(upload(WS_GEMM_A, gi.data(), nb * sizeof(SplitGemmInst), &dg, stream));
+  SplitGemmBatch G{(const SplitGemmInst*)dg, 1, nt, nchunk, N, N, ldo};
+  CTR_TRY(launch_split_gemm(G, nb, d_err, stream));
+  for (int b = 0; b < nb; b++) {
+    TimedLaunch tl(stream, "ff_to_f64");
+    ff_to_f64_kernel<<<cdiv(N * N, 256), 256, 0, stream>>>(gi[b].out, ldo, N, (double2*)c[b]);
+    CTR_CUDA(cudaGetLastError());
+  }
+  return CTR_OK;
+}
+
+// Diagnostics: the raw FP32 TMEM accumulators (Re/Im x levels 0, 1, >=2) of one
+// product x*y, before recombination and scaling.  Used by the tests to check
+// the tensor-core accumulation against an exact emulation of the slices.
+int split_levels(int N, const double* x, const double* y, float* levels, cudaStream_t stream) {
+  if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d", SPLIT_MAXK);
+  const int nchunk = cdiv(N, SPLIT_K), nt = cdiv(N, SPLIT_N);
+  const size_t l_b = align256((size_t)nchunk * SPLIT_A_STAGE), r_b = align256((size_t)nt * nchunk * SPLIT_B_STAGE);
+  const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)nt * SPLIT_N * 4);
+  void* mem;
+  CTR_TRY(workspace(WS_SCRATCH).get(l_b + r_b + le_b + re_b + 256, &mem));
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  uint8_t* p = (uint8_t*)mem;
+  SliceLeftJob lj;
+  SliceRightJob rj;
+  std::memset(&lj, 0, sizeof(lj));
+  std::memset(&rj, 0, sizeof(rj));
+  lj.blk[0] = (const double2*)x;
+  lj.rows = N;
+  lj.out = p;
+  lj.exps = (int*)(p + l_b + r_b);
+  rj.blk[0] = (const double2*)y;
+  rj.cols = N;
+  rj.out = p + l_b;
+  rj.exps = (int*)(p + l_b + r_b + le_b);
+  SplitGemmInst gi{p, p + l_b, lj.exps, rj.exps, nullptr};
+  void *dl, *dr, *dg;
+  CTR_TRY(upload(WS_TASKS, &lj, sizeof(lj), &dl, stream));
+  CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, 1, N, nchunk, 1, stream));
+  CTR_TRY(upload(WS_TASKS2, &rj, sizeof(rj), &dr, stream));
+  CTR_TRY(launch_slice_right((const SliceRightJob*)dr, 1, N, nchunk, nt, stream));
+  CTR_TRY(upload(WS_GEMM_A, &gi, sizeof(gi), &dg, stream));
+  SplitGemmBatch G{(const SplitGemmInst*)dg, 1, nt, nchunk, N, N, SPLIT_M, levels};
+  return launch_split_gemm(G, 1, d_err, stream);
+}
+
+}  // namespace ctr
+
+extern "C" int ctr_split_levels(int nev, const double* x, const double* y, float* levels, void* stream) {
+  if (nev < 1 || !x || !y || !levels) return ctr::fail(CTR_ERR_ARG, "ctr_split_levels: bad arguments");
+  return ctr::split_levels(nev, x, y, levels, (cudaStream_t)stream);
+}

@@ -1,13 +1,427 @@
-// Split-precision tensor-core engine (placeholder until the tcgen05 path lands).
+// Split-precision tensor-core engine.
+//
+// A complex FP64 product C = X * Y (Nev <= 128) is computed on the tcgen05
+// tensor cores as follows.
+//  * Slicing.  Every row of the left operand X (every column of the right
+//    operand Y) gets a power-of-two scale 2^E with all |entries| < 2^E.  The
+//    scaled magnitudes are cut into NSLICE = 5 pieces of 8 bits,
+//    x/2^E = sign * sum_s u_s 2^{-8(s+1)}, u_s in [0,255], taken straight from
+//    the FP64 bit pattern with integer operations (no FP64 arithmetic).  Each
+//    piece sign*u_s*2^{-8(s+1)} is exact in BF16.  Truncation error < 2^-40.
+//  * MMA.  Slice pairs (i,j) with i+j <= 4 (15 pairs) are multiplied with
+//    tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in TMEM); the complex
+//    product takes 4 real MMAs per pair (the -Xi*Yi term uses the A-negate bit).
+//    Pairs accumulate in three levels: i+j = 0 (exact: < 2^24 units for
+//    K <= 128), i+j = 1 (exact up to the last bit), i+j >= 2.  Level values are
+//    combined in float-float (two FP32 words, ~48 bits) and scaled by
+//    2^{E_row + E_col}.
+//  * Data movement.  Slices are stored pre-tiled in the UMMA K-major
+//    no-swizzle core-matrix layout, grouped by K-chunk of 16, so one pipeline
+//    stage (all slices and both real/imag planes of one K-chunk) is one
+//    contiguous bulk async copy per operand.
+#include <cstdint>
+#include <cstring>
+
 #include "kernels.h"
+#include "sm100_ptx.cuh"
+#include "split.h"
 
 namespace ctr {
 
-int twosided_split(int, int, int, int, const double*, const double*, int, const std::vector<TwoSidedRow>&,
-                   const std::vector<float>&, const std::vector<int32_t>&, int, double*, cudaStream_t) {
-  return fail(CTR_ERR_UNSUPPORTED, "split-precision engine not built yet");
+using namespace ptx;
+
+// ----------------------------------------------------------- slicing math
+__device__ __forceinline__ int f64_exp_bound(double x) {
+  // e with |x| < 2^e for normal x; very small for zero / subnormal
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7FF);
+  return be == 0 ? -30000 : be - 1022;
+}
+
+// 63-bit fixed-point magnitude of x / 2^E (|x| < 2^E) and its sign.
+__device__ __forceinline__ uint64_t f64_fixed(double x, int E, bool& neg) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  neg = (b >> 63) != 0;
+  const int be = (int)((b >> 52) & 0x7FF);
+  if (be == 0) return 0;
+  const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  const int sh = be - 1012 - E;  // <= 10 because |x| < 2^E
+  if (sh >= 0) return m << sh;
+  if (sh <= -64) return 0;
+  return m >> (-sh);
+}
+
+__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t U, int s, bool neg) {
+  const uint32_t u = (uint32_t)(U >> (55 - 8 * s)) & 0xFFu;
+  float v = (float)u * __int_as_float((127 - 8 * (s + 1)) << 23);
+  return __float2bfloat16_rn(neg ? -v : v);
+}
+
+// Byte offset of element (row, k) of one (slice, plane) sub-tile inside a
+// K-chunk stage: core matrices of 8 rows x 8 elements, K-adjacent at +128 B,
+// row-group-adjacent at +256 B.
+__device__ __forceinline__ uint32_t core_offset(int row, int k) {
+  return (uint32_t)((row >> 3) * 256 + ((k >> 3) & 1) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// Left operand: one M tile (128 stacked rows) of one operand instance.
+// Row r of the stack is row (r % nev) of block blk[r / nev]; element k of it
+// is blk[r/nev][(r%nev)*nev + k].  Output: [nchunk][SPLIT_A_STAGE] bytes and
+// 128 row exponents.
+__global__ void __launch_bounds__(256) slice_left_kernel(const SliceLeftJob* __restrict__ jobs, int nev,
+                                                         int nchunk, int mtiles) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  int* sexp = (int*)sm;
+  uint8_t* stage = sm + 512;
+  const SliceLeftJob& J = jobs[blockIdx.x / mtiles];
+  const int mt = blockIdx.x % mtiles;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // row exponents
+  for (int rr = warp; rr < SPLIT_M; rr += 8) {
+    const int r = mt * SPLIT_M + rr;
+    int e = -30000;
+    if (r < J.rows) {
+      const double2* row = J.blk[r / nev] + (size_t)(r % nev) * nev;
+      for (int k = lane; k < nev; k += 32) {
+        double2 v = row[k];
+        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
+      }
+    }
+    for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if (lane == 0) {
+      const int E = e < -1000 ? 0 : e;
+      sexp[rr] = E;
+      J.exps[mt * SPLIT_M + rr] = E;
+    }
+  }
+  __syncthreads();
+  uint8_t* dst_tile = J.out + (size_t)mt * nchunk * SPLIT_A_STAGE;
+  for (int kc = 0; kc < nchunk; kc++) {
+    // 128 rows x 16 k: 16 consecutive threads read one row segment (coalesced)
+    for (int e = threadIdx.x; e < SPLIT_M * SPLIT_K; e += 256) {
+      const int rr = e >> 4, kk = e & 15;
+      const int r = mt * SPLIT_M + rr, k = kc * SPLIT_K + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (r < J.rows && k < nev) v = J.blk[r / nev][(size_t)(r % nev) * nev + k];
+      const int E = sexp[rr];
+      bool nr, ni;
+      const uint64_t Ur = f64_fixed(v.x, E, nr), Ui = f64_fixed(v.y, E, ni);
+      const uint32_t off = core_offset(rr, kk);
+#pragma unroll
+      for (int s = 0; s < SPLIT_NSLICE; s++) {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_A_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_A_SUB + off) = slice_bf16(Ui, s, ni);
+      }
+    }
+    __syncthreads();
+    int4* d = (int4*)(dst_tile + (size_t)kc * SPLIT_A_STAGE);
+    const int4* src = (const int4*)stage;
+    for (int i = threadIdx.x; i < SPLIT_A_STAGE / 16; i += 256) d[i] = src[i];
+    __syncthreads();
+  }
+}
+
+// Right operand (stored N x K, K-major): one N tile of 80 stacked columns.
+// Column n of the stack is column (n % nev) of block blk[n / nev]; its element
+// k is blk[n/nev][k*nev + n%nev].  Exponent per column.
+__global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* __restrict__ jobs, int nev,
+                                                          int nchunk, int ntiles) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  int* sexp = (int*)sm;
+  uint8_t* stage = sm + 512;
+  const SliceRightJob& J = jobs[blockIdx.x / ntiles];
+  const int nt = blockIdx.x % ntiles;
+  // column exponents: thread n scans column n (consecutive threads read consecutive columns)
+  if (threadIdx.x < SPLIT_N) {
+    const int n = nt * SPLIT_N + threadIdx.x;
+    int e = -30000;
+    if (n < J.cols) {
+      const double2* col = J.blk[n / nev] + (n % nev);
+      for (int k = 0; k < nev; k++) {
+        double2 v = col[(size_t)k * nev];
+        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
+      }
+    }
+    const int E = e < -1000 ? 0 : e;
+    sexp[threadIdx.x] = E;
+    J.exps[n] = E;  // exps sized ntiles * SPLIT_N (padding columns get 0)
+  }
+  __syncthreads();
+  uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE;
+  for (int kc = 0; kc < nchunk; kc++) {
+    for (int e = threadIdx.x; e < SPLIT_N * SPLIT_K; e += 256) {
+      const int nn = e % SPLIT_N, kk = e / SPLIT_N;
+      const int n = nt * SPLIT_N + nn, k = kc * SPLIT_K + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (n < J.cols && k < nev) v = J.blk[n / nev][(size_t)k * nev + (n % nev)];
+      const int E = sexp[nn];
+      bool nr, ni;
+      const uint64_t Ur = f64_fixed(v.x, E, nr), Ui = f64_fixed(v.y, E, ni);
+      const uint32_t off = core_offset(nn, kk);
+#pragma unroll
+      for (int s = 0; s < SPLIT_NSLICE; s++) {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_B_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, ni);
+      }
+    }
+    __syncthreads();
+    int4* d = (int4*)(dst_tile + (size_t)kc * SPLIT_B_STAGE);
+    const int4* src = (const int4*)stage;
+    for (int i = threadIdx.x; i < SPLIT_B_STAGE / 16; i += 256) d[i] = src[i];
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ GEMM
+// One CTA computes one 128 x 80 output tile of one GEMM instance.
+// Warp 0: TMEM allocation and the bulk-copy producer; warp 1: MMA issue;
+// warps 2..5: epilogue (TMEM lanes 32*(warp%4) .. +31).
+constexpr int GEMM_THREADS = 192;
+constexpr int NSTAGE = 3;
+constexpr int NACC = 6;  // (re, im) x 3 levels
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
+
+constexpr size_t gemm_smem_bytes() {
+  return (size_t)NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE) + 256;
+}
+
+__device__ __forceinline__ float pow2f(int e) {
+  e = max(-126, min(127, e));
+  return __int_as_float((127 + e) << 23);
+}
+
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    split_gemm_kernel(SplitGemmBatch g, int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + NSTAGE * SPLIT_A_STAGE;
+  uint64_t* full = (uint64_t*)(smem + NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE));
+  uint64_t* empty = full + NSTAGE;
+  uint64_t* accb = empty + NSTAGE;
+  uint32_t* tslot = (uint32_t*)(accb + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tiles = g.mtiles * g.ntiles;
+  const int inst = blockIdx.x / tiles;
+  const int mt = (blockIdx.x % tiles) / g.ntiles;
+  const int nt = blockIdx.x % g.ntiles;
+  const SplitGemmInst I = g.inst[inst];
+  const uint8_t* gA = I.left + (size_t)mt * g.nchunk * SPLIT_A_STAGE;
+  const uint8_t* gB = I.right + (size_t)nt * g.nchunk * SPLIT_B_STAGE;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accb, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tslot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kc = 0; kc < g.nchunk; kc++) {
+        const int s = kc % NSTAGE;
+        if (kc >= NSTAGE) {
+          if (!mbar_wait(&empty[s], ((kc / NSTAGE) - 1) & 1, WAIT_NS)) {
+            atomicExch(err, 1);
+            break;
+          }
+        }
+        mbar_arrive_expect_tx(&full[s], SPLIT_A_STAGE + SPLIT_B_STAGE);
+        bulk_g2s(sA + s * SPLIT_A_STAGE, gA + (size_t)kc * SPLIT_A_STAGE, SPLIT_A_STAGE, &full[s]);
+        bulk_g2s(sB + s * SPLIT_B_STAGE, gB + (size_t)kc * SPLIT_B_STAGE, SPLIT_B_STAGE, &full[s]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, SPLIT_N, false);
+      constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, SPLIT_N, true);
+      bool ok = true;
+      for (int kc = 0; kc < g.nchunk && ok; kc++) {
+        const int s = kc % NSTAGE;
+        if (!mbar_wait(&full[s], (kc / NSTAGE) & 1, WAIT_NS)) {
+          atomicExch(err, 2);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(sA + s * SPLIT_A_STAGE);
+        const uint32_t b0 = smem_u32(sB + s * SPLIT_B_STAGE);
+#pragma unroll 1
+        for (int i = 0; i < SPLIT_NSLICE; i++) {
+#pragma unroll 1
+          for (int j = 0; j + i < SPLIT_NSLICE; j++) {
+            const int lvl = (i + j) < 2 ? (i + j) : 2;
+            // in loop order the first pair of level 0, 1, 2 is (0,0), (0,1), (0,2)
+            const uint32_t accum = (kc > 0 || !(i == 0 && j <= 2)) ? 1u : 0u;
+            const uint64_t ar = sdesc_kmajor_noswz(a0 + (i * 2 + 0) * SPLIT_A_SUB, 128, 256);
+            const uint64_t ai = sdesc_kmajor_noswz(a0 + (i * 2 + 1) * SPLIT_A_SUB, 128, 256);
+            const uint64_t br = sdesc_kmajor_noswz(b0 + (j * 2 + 0) * SPLIT_B_SUB, 128, 256);
+            const uint64_t bi = sdesc_kmajor_noswz(b0 + (j * 2 + 1) * SPLIT_B_SUB, 128, 256);
+            const uint32_t dre = tbase + (uint32_t)(lvl * SPLIT_N);
+            const uint32_t dim = tbase + (uint32_t)((3 + lvl) * SPLIT_N);
+            umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
+            umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
+            umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
+            umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
+          }
+        }
+        umma_commit(&empty[s]);  // stage s free once these MMAs have read it
+      }
+      umma_commit(accb);  // also arrives (with nothing in flight) after a timeout
+    }
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane quadrant warp % 4
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const bool ok = mbar_wait(accb, 0, 4 * WAIT_NS);
+    if (!ok) atomicExch(err, 3);
+    tc_fence_after();
+    const int grow = mt * SPLIT_M + row;
+    const bool rvalid = grow < g.mrows;
+    const float srow = pow2f(I.lexp[grow]);
+    float4* outp = I.out;
+    const int ldo = g.ldo;
+    for (int c0 = 0; c0 < SPLIT_N; c0 += 16) {
+      float v[NACC][16];
+#pragma unroll
+      for (int a = 0; a < NACC; a++) tmem_ld16(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * SPLIT_N + c0), v[a]);
+      tmem_ld_wait();
+      if (!ok || !rvalid) continue;
+#pragma unroll
+      for (int c = 0; c < 16; c++) {
+        const int gcol = nt * SPLIT_N + c0 + c;
+        if (gcol >= g.ncols) continue;
+        if (g.levels) {
+          for (int a = 0; a < NACC; a++) g.levels[((size_t)a * g.ncols + gcol) * ldo + grow] = v[a][c];
+          continue;
+        }
+        const float sc = srow * pow2f(I.rexp[gcol]);
+        float4 o;
+        {
+          float s, e;
+          two_sum(v[0][c], v[1][c], s, e);
+          e += v[2][c];
+          fast_two_sum(s, e, o.x, o.y);
+        }
+        {
+          float s, e;
+          two_sum(v[3][c], v[4][c], s, e);
+          e += v[5][c];
+          fast_two_sum(s, e, o.z, o.w);
+        }
+        o.x *= sc; o.y *= sc; o.z *= sc; o.w *= sc;
+        outp[(size_t)gcol * ldo + grow] = o;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tbase, TMEM_COLS);
+  }
+}
+
+// ------------------------------------------------------------- ff traces
+// *out = coef * sum_{i<nev, j<nev} A(i,j) * conj(B(i,j)); A(i,j) = a[j*lda + i],
+// B(i,j) = b[j*ldb + i] (float-float complex).  One CTA of 128 threads per
+// task; thread i walks column elements i (and i+128) over all j.
+__global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __restrict__ tasks, int ntask, int nev) {
+  const int t = blockIdx.x;
+  if (t >= ntask) return;
+  const TraceFFTask T = tasks[t];
+  float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+  for (int i = threadIdx.x; i < nev; i += 128) {
+    for (int j = 0; j < nev; j++) {
+      const float4 a = T.a[(size_t)j * T.lda + i];
+      const float4 b = T.b[(size_t)j * T.ldb + i];
+      ff_mac(sr, er, a.x, a.y, b.x, b.y);   // + ar br
+      ff_mac(sr, er, a.z, a.w, b.z, b.w);   // + ai bi
+      ff_mac(si, ei, a.z, a.w, b.x, b.y);   // + ai br
+      ff_mac(si, ei, -a.x, -a.y, b.z, b.w); // - ar bi
+    }
+  }
+  double re = (double)sr + (double)er, im = (double)si + (double)ei;
+  __shared__ double red[2][4];
+  for (int o = 16; o; o >>= 1) {
+    re += __shfl_down_sync(0xffffffffu, re, o);
+    im += __shfl_down_sync(0xffffffffu, im, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = re;
+    red[1][threadIdx.x >> 5] = im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    re = red[0][0] + red[0][1] + red[0][2] + red[0][3];
+    im = red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+    *T.out = cmul(c, make_double2(re, im));
+  }
+}
+
+// --------------------------------------------------------------- launchers
+int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s) {
+  if (njobs == 0) return CTR_OK;
+  const size_t smem = 512 + SPLIT_A_STAGE;
+  static bool attr = false;
+  if (!attr) {
+    CTR_CUDA(cudaFuncSetAttribute(slice_left_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  TimedLaunch tl(s, "slice_left");
+  slice_left_kernel<<<njobs * mtiles, 256, smem, s>>>(d_jobs, nev, nchunk, mtiles);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
+  if (njobs == 0) return CTR_OK;
+  const size_t smem = 512 + SPLIT_B_STAGE;
+  static bool attr = false;
+  if (!attr) {
+    CTR_CUDA(cudaFuncSetAttribute(slice_right_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  TimedLaunch tl(s, "slice_right");
+  slice_right_kernel<<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
+  if (ninst == 0) return CTR_OK;
+  const size_t smem = gemm_smem_bytes();
+  static bool attr = false;
+  if (!attr) {
+    CTR_CUDA(cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  TimedLaunch tl(s, "split_gemm");
+  split_gemm_kernel<<<ninst * g.mtiles * g.ntiles, GEMM_THREADS, smem, s>>>(g, d_err);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_trace_ff(const TraceFFTask* d_tasks, int ntask, int nev, cudaStream_t s) {
+  if (ntask == 0) return CTR_OK;
+  TimedLaunch tl(s, "trace_ff");
+  trace_ff_kernel<<<ntask, 128, 0, s>>>(d_tasks, ntask, nev);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
 }
 
 }  // namespace ctr
 
-extern "C" int ctr_split_available(void) { return 0; }
+extern "C" int ctr_split_available(void) { return 1; }

@@ -1,0 +1,97 @@
+// Shared definitions of the split-precision (BF16-slice tensor-core) engine.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ctr_internal.h"
+
+namespace ctr {
+
+// Tile geometry (see kernels_split.cu).
+constexpr int SPLIT_M = 128;     // rows of an output tile (TMEM lanes)
+constexpr int SPLIT_N = 80;      // columns of an output tile (6 accumulators x 80 <= 512 TMEM columns)
+constexpr int SPLIT_K = 16;      // K of one MMA / one pipeline chunk
+constexpr int SPLIT_NSLICE = 5;  // BF16 slices per FP64 value
+constexpr int SPLIT_MAXK = 128;  // largest Nev the engine takes (exactness bound of the leading level)
+constexpr int SPLIT_A_SUB = SPLIT_M * SPLIT_K * 2;                  // one (slice, plane) sub-tile, bytes
+constexpr int SPLIT_B_SUB = SPLIT_N * SPLIT_K * 2;
+constexpr int SPLIT_A_STAGE = SPLIT_NSLICE * 2 * SPLIT_A_SUB;       // 40960 B: all slices, re+im, one K chunk
+constexpr int SPLIT_B_STAGE = SPLIT_NSLICE * 2 * SPLIT_B_SUB;       // 25600 B
+constexpr int SPLIT_MAXBLK = 32;
+
+// Slicing of a stacked operand.  Left: rows r -> row r%nev of blk[r/nev].
+struct SliceLeftJob {
+  const double2* blk[SPLIT_MAXBLK];
+  int rows;        // stacked rows (nblk * nev)
+  int pad;
+  uint8_t* out;    // [mtiles][nchunk][SPLIT_A_STAGE]
+  int* exps;       // [mtiles * SPLIT_M]
+};
+
+// Right: columns n -> column n%nev of blk[n/nev].
+struct SliceRightJob {
+  const double2* blk[SPLIT_MAXBLK];
+  int cols;
+  int pad;
+  uint8_t* out;    // [ntiles][nchunk][SPLIT_B_STAGE]
+  int* exps;       // [ntiles * SPLIT_N]
+};
+
+struct SplitGemmInst {
+  const uint8_t* left;   // sliced left operand (all M tiles)
+  const uint8_t* right;  // sliced right operand (all N tiles)
+  const int* lexp;       // row exponents
+  const int* rexp;       // column exponents
+  float4* out;           // float-float complex, column-major: (r, c) at out[c * ldo + r]
+};
+
+struct SplitGemmBatch {
+  const SplitGemmInst* inst;
+  int mtiles, ntiles, nchunk;
+  int mrows, ncols;  // valid rows / columns of every instance
+  int ldo;           // column stride of the output (>= mtiles * SPLIT_M)
+  float* levels;     // diagnostics only (NULL in production): raw accumulators
+                     // [6][ncols][ldo] of instance 0 instead of the ff output
+};
+
+// *out = coef * sum_{i,j<nev} A(i,j) conj(B(i,j)), A(i,j) = a[j*lda+i] (float-float complex)
+struct TraceFFTask {
+  const float4* a;
+  const float4* b;
+  double2* out;
+  int lda, ldb;
+  float coef[2];
+};
+
+// ------------------------------------------------------ float-float helpers
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  e = b - (s - a);
+}
+
+// (S, E) += (xh + xl) * (yh + yl), products kept to ~2^-47 relative.
+__device__ __forceinline__ void ff_mac(float& S, float& E, float xh, float xl, float yh, float yl) {
+  const float p = xh * yh;
+  float e = fmaf(xh, yh, -p);
+  e = fmaf(xh, yl, e);
+  e = fmaf(xl, yh, e);
+  float s, t;
+  two_sum(S, p, s, t);
+  S = s;
+  E += t + e;
+}
+
+int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s);
+int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
+int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
+int launch_trace_ff(const TraceFFTask* d_tasks, int ntask, int nev, cudaStream_t s);
+
+}  // namespace ctr

@@ -85,6 +85,19 @@ int ctr_rho(int engine, int nev, int nt, int tf_begin, int tf_end, const double*
 int ctr_sigma(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
               const double* mom2, double* corr, void* stream);
 
+/* Batched complex block products c[b] = x[b] * y[b] (nev x nev, row-major
+ * complex128, device pointers given in host arrays of length nbatch).  The unit
+ * both engines build the diagram chains from (the 25x25-tiled GEMM loops of every
+ * lib/calculate_*_core.h). */
+int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, const double* const* y,
+                      double* const* c, void* stream);
+
+/* Diagnostics of the split engine: for one product x*y (nev x nev, device),
+ * write the raw FP32 tensor-core accumulators before recombination, as
+ * levels[6][nev][128] (Re level 0, 1, >=2, Im level 0, 1, >=2; element (i,j)
+ * at [a][j][i]), in units of the per-row / per-column power-of-two scales. */
+int ctr_split_levels(int nev, const double* x, const double* y, float* levels, void* stream);
+
 /* On-device source-time average of the dumpData routines (lib/contract.cpp:616-643):
  * avg[dt][c] = scale/Nt * sum_ti corr[(ti+dt)%Nt][ti][c]; corr device [Nt][Nt][ncorr]. */
 int ctr_source_average(int nt, int ncorr, const double* corr, double scale, double* avg, void* stream);

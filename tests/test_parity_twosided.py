@@ -28,7 +28,7 @@ def _close(got, ref, tol):
     assert err <= tol, "max error %.3e relative to max |entry| (tolerance %.1e)" % (err, tol)
 
 
-@pytest.mark.parametrize("engine", ["fp64"])
+@pytest.mark.parametrize("engine", ["fp64", "split"])
 @pytest.mark.parametrize("nt,n", [(3, 16), (2, 37), (1, 1), (4, 8)])
 def test_rho_matches_oracle(cuda, engine, nt, n):
     prop, mom5 = _inputs(nt, n, seed=100 + n)
@@ -37,7 +37,7 @@ def test_rho_matches_oracle(cuda, engine, nt, n):
     _close(got.cpu().numpy(), ref, TOL[engine])
 
 
-@pytest.mark.parametrize("engine", ["fp64"])
+@pytest.mark.parametrize("engine", ["fp64", "split"])
 def test_rho_single_row_buffer(cuda, engine):
     """Row-by-row use, as Contract_rho_rho::contractRho drives run_ContractRho (lib/contract.cpp:602-605)."""
     nt, n = 4, 12
@@ -50,7 +50,7 @@ def test_rho_single_row_buffer(cuda, engine):
         _close(got[0].cpu().numpy(), ref, TOL[engine])
 
 
-@pytest.mark.parametrize("engine", ["fp64"])
+@pytest.mark.parametrize("engine", ["fp64", "split"])
 def test_sigma_matches_oracle(cuda, engine):
     nt, n = 3, 20
     prop, mom2 = _inputs(nt, n, seed=9, nops=2)

@@ -1,0 +1,120 @@
+"""The split-precision tensor-core GEMM (BF16 slices, tcgen05, float-float
+recombination) against numpy complex128 products.
+
+Tolerance: the products carry ~40 bits (5 slices of 8 bits, levels 0 and 1
+accumulated exactly in FP32, the rest in FP32); the error bound tested is
+1e-11 relative to max|C|, far inside the 1e-9 correlator tolerance."""
+import numpy as np
+import pytest
+import torch
+
+from contractions_code_scattering_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-11
+
+
+def _rand(rng, shape, scale=1.0):
+    return (rng.normal(size=shape) + 1j * rng.normal(size=shape)) * scale
+
+
+def _check(x, y, cuda, engine="split", tol=TOL):
+    got = api.zgemm_batched(torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda), engine=engine)
+    api.sync()
+    ref = np.einsum("bij,bjk->bik", x, y)
+    err = np.abs(got.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err <= tol, "split GEMM error %.3e > %.1e" % (err, tol)
+    return err
+
+
+@pytest.mark.parametrize("n", [100, 16, 37, 80, 81, 128, 1])
+def test_split_gemm_random(cuda, n):
+    rng = np.random.default_rng(n)
+    _check(_rand(rng, (3, n, n)), _rand(rng, (3, n, n)), cuda)
+
+
+def test_split_gemm_identity_is_exact(cuda):
+    n = 100
+    eye = np.eye(n, dtype=np.complex128)[None]
+    rng = np.random.default_rng(1)
+    # values with <= 40 significant bits are reproduced exactly
+    y = np.round(_rand(rng, (1, n, n)) * 2 ** 20) / 2 ** 20
+    got = api.zgemm_batched(torch.from_numpy(eye).to(cuda), torch.from_numpy(y).to(cuda), engine="split")
+    api.sync()
+    assert np.array_equal(got.cpu().numpy(), y)
+
+
+def test_split_gemm_row_and_column_scales(cuda):
+    """Rows of X and columns of Y spanning 1e-12 .. 1e3: per-row/column power-of-two scaling."""
+    n = 100
+    rng = np.random.default_rng(2)
+    x = _rand(rng, (2, n, n)) * np.logspace(-12, 3, n)[None, :, None]
+    y = _rand(rng, (2, n, n)) * np.logspace(3, -12, n)[None, None, :]
+    got = api.zgemm_batched(torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda), engine="split")
+    api.sync()
+    ref = np.einsum("bij,bjk->bik", x, y)
+    # entry-wise relative error against the scale of the entry's row and column
+    scale = np.abs(x).max(axis=2)[:, :, None] * np.abs(y).max(axis=1)[:, None, :] * n
+    assert (np.abs(got.cpu().numpy() - ref) / scale).max() < 1e-12
+
+
+def test_split_gemm_zero_and_sparse(cuda):
+    n = 64
+    x = np.zeros((2, n, n), np.complex128)
+    y = np.zeros((2, n, n), np.complex128)
+    x[1, 3, 5] = 2.5 - 1j
+    y[1, 5, 7] = -0.75j
+    got = api.zgemm_batched(torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda), engine="split").cpu().numpy()
+    api.sync()
+    assert np.array_equal(got[0], np.zeros((n, n)))
+    ref = np.einsum("bij,bjk->bik", x, y)
+    assert np.array_equal(got[1], ref[1])
+
+
+def test_fp64_engine_gemm(cuda):
+    rng = np.random.default_rng(3)
+    _check(_rand(rng, (2, 100, 100)), _rand(rng, (2, 100, 100)), cuda, engine="fp64", tol=1e-14)
+
+
+def _emulate_slices(X, axis, nslice=5):
+    """Exact emulation of the slicer: per-row (axis=1) or per-column (axis=0)
+    power-of-two scale, 8-bit truncated slices of the 63-bit fixed-point magnitude."""
+    re, im = X.real, X.imag
+    er = np.where(re != 0, np.frexp(re)[1], -30000)
+    ei = np.where(im != 0, np.frexp(im)[1], -30000)
+    e = np.maximum(er, ei).max(axis=axis, keepdims=True)
+    E = np.where(e < -1000, 0, e)
+
+    def cut(a):
+        U = np.floor(np.abs(a) * np.ldexp(1.0, 63 - E)).astype(np.uint64)
+        return [np.sign(a) * ((U >> np.uint64(55 - 8 * s)) & np.uint64(0xFF)).astype(np.float64) * 2.0 ** (-8 * (s + 1))
+                for s in range(nslice)]
+    return cut(re), cut(im)
+
+
+def test_tensor_core_accumulation_levels(cuda):
+    """Levels 0 and 1 are sums of < 2^24 integer units: the FP32 tensor-core
+    accumulation must reproduce them exactly; level >= 2 to FP32 rounding."""
+    n = 100
+    rng = np.random.default_rng(11)
+    x, y = _rand(rng, (n, n)), _rand(rng, (n, n))
+    lv = api.split_levels(torch.from_numpy(x).to(cuda), torch.from_numpy(y).to(cuda)).cpu().numpy().astype(np.float64)
+    (xr, xi), (yr, yi) = _emulate_slices(x, 1), _emulate_slices(y, 0)
+    exact = np.zeros((6, n, n))
+    for i in range(5):
+        for j in range(5 - i):
+            l = min(i + j, 2)
+            exact[l] += xr[i] @ yr[j] - xi[i] @ yi[j]
+            exact[3 + l] += xr[i] @ yi[j] + xi[i] @ yr[j]
+    report = []
+    for a in range(6):
+        d = np.abs(lv[a] - exact[a])
+        report.append("acc%d: max|diff| %.3e (max|exact| %.3e, mismatches %d)" % (a, d.max(), np.abs(exact[a]).max(), (d > 0).sum()))
+    print("\n".join(report))
+    for a in (0, 3):
+        assert np.array_equal(lv[a], exact[a]), report[a]
+    for a in (1, 4):
+        assert np.abs(lv[a] - exact[a]).max() <= 2.0 ** -22 * np.abs(exact[a]).max(), report[a]
+    for a in (2, 5):
+        assert np.abs(lv[a] - exact[a]).max() <= 2.0 ** -20 * np.abs(exact[a]).max(), report[a]
