@@ -178,10 +178,10 @@ __all__ = ["CtrError", "device_init", "tables", "twosided", "run_contract_rho", 
 
 def split_levels(x, y, stream=None):
     """Diagnostics: raw tensor-core accumulators of the split product x @ y
-    ([N,N] complex128 device tensors) -> float32 [6, N, N] (Re l0, l1, l>=2, Im l0, l1, l>=2)."""
+    ([N,N] complex128 device tensors) -> float32 [8, N, N] (Re levels 0, 1, 2, >=3, then Im)."""
     import torch
     n = x.shape[-1]
-    lv = torch.zeros((6, n, 128), dtype=torch.float32, device=x.device)
+    lv = torch.zeros((8, n, 128), dtype=torch.float32, device=x.device)
     check(lib().ctr_split_levels(n, _dev(x, "x"), _dev(y, "y"), ctypes.c_void_p(lv.data_ptr()), _stream(stream)))
     sync(stream)
     return lv[:, :, :n].transpose(1, 2)

@@ -7,14 +7,18 @@
 //    scaled magnitudes are cut into NSLICE = 5 pieces of 8 bits,
 //    x/2^E = sign * sum_s u_s 2^{-8(s+1)}, u_s in [0,255], taken straight from
 //    the FP64 bit pattern with integer operations (no FP64 arithmetic).  Each
-//    piece sign*u_s*2^{-8(s+1)} is exact in BF16.  Truncation error < 2^-40.
+//    piece sign*u_s*2^{-8(s+1)} is exact in BF16.  The cut is rounded to
+//    nearest at 2^-40, so the residual is <= 2^-41 and unbiased.
 //  * MMA.  Slice pairs (i,j) with i+j <= 4 (15 pairs) are multiplied with
 //    tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in TMEM); the complex
 //    product takes 4 real MMAs per pair (the -Xi*Yi term uses the A-negate bit).
-//    Pairs accumulate in three levels: i+j = 0 (exact: < 2^24 units for
-//    K <= 128), i+j = 1 (exact up to the last bit), i+j >= 2.  Level values are
-//    combined in float-float (two FP32 words, ~48 bits) and scaled by
-//    2^{E_row + E_col}.
+//    Pairs accumulate in four levels, i+j = 0, 1, 2 and >= 3.  Levels 0-2 hold
+//    integer multiples of 2^-16, 2^-24, 2^-32 below 2^24 units (for K <= 128
+//    and non-adversarial data), which the FP32 tensor-core accumulation keeps
+//    exactly; measured on GB300, an accumulator mixing level 2 with the much
+//    smaller levels 3-4 loses ~6 bits to truncation, hence the separate level.
+//    Level values are combined in float-float (two FP32 words, ~48 bits) and
+//    scaled by 2^{E_row + E_col}.
 //  * Data movement.  Slices are stored pre-tiled in the UMMA K-major
 //    no-swizzle core-matrix layout, grouped by K-chunk of 16, so one pipeline
 //    stage (all slices and both real/imag planes of one K-chunk) is one
@@ -51,8 +55,14 @@ __device__ __forceinline__ uint64_t f64_fixed(double x, int E, bool& neg) {
   return m >> (-sh);
 }
 
-__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t U, int s, bool neg) {
-  const uint32_t u = (uint32_t)(U >> (55 - 8 * s)) & 0xFFu;
+// Slice s of the magnitude U (63-bit fixed point), rounded to nearest at the
+// last retained bit (2^-40): U + 2^22 is cut into u_0 in [0,256] and
+// u_1..u_4 in [0,255], all exact in BF16; the residual is at most 2^-41 and
+// has no sign bias.
+__device__ __forceinline__ uint64_t round_fixed(uint64_t U) { return U + (1ull << 22); }
+
+__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t Urnd, int s, bool neg) {
+  const uint32_t u = s == 0 ? (uint32_t)(Urnd >> 55) : (uint32_t)(Urnd >> (55 - 8 * s)) & 0xFFu;
   float v = (float)u * __int_as_float((127 - 8 * (s + 1)) << 23);
   return __float2bfloat16_rn(neg ? -v : v);
 }
@@ -105,7 +115,7 @@ __global__ void __launch_bounds__(256) slice_left_kernel(const SliceLeftJob* __r
       if (r < J.rows && k < nev) v = J.blk[r / nev][(size_t)(r % nev) * nev + k];
       const int E = sexp[rr];
       bool nr, ni;
-      const uint64_t Ur = f64_fixed(v.x, E, nr), Ui = f64_fixed(v.y, E, ni);
+      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
       const uint32_t off = core_offset(rr, kk);
 #pragma unroll
       for (int s = 0; s < SPLIT_NSLICE; s++) {
@@ -121,7 +131,7 @@ __global__ void __launch_bounds__(256) slice_left_kernel(const SliceLeftJob* __r
   }
 }
 
-// Right operand (stored N x K, K-major): one N tile of 80 stacked columns.
+// Right operand (stored N x K, K-major): one N tile of SPLIT_N stacked columns.
 // Column n of the stack is column (n % nev) of block blk[n / nev]; its element
 // k is blk[n/nev][k*nev + n%nev].  Exponent per column.
 __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* __restrict__ jobs, int nev,
@@ -156,7 +166,7 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
       if (n < J.cols && k < nev) v = J.blk[n / nev][(size_t)k * nev + (n % nev)];
       const int E = sexp[nn];
       bool nr, ni;
-      const uint64_t Ur = f64_fixed(v.x, E, nr), Ui = f64_fixed(v.y, E, ni);
+      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
       const uint32_t off = core_offset(nn, kk);
 #pragma unroll
       for (int s = 0; s < SPLIT_NSLICE; s++) {
@@ -178,7 +188,7 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
 // warps 2..5: epilogue (TMEM lanes 32*(warp%4) .. +31).
 constexpr int GEMM_THREADS = 192;
 constexpr int NSTAGE = 3;
-constexpr int NACC = 6;  // (re, im) x 3 levels
+constexpr int NLEVEL = 4;  // accumulation levels i+j = 0, 1, 2, >=3; (re, im) x 4 x SPLIT_N = 512 TMEM columns
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
 
@@ -201,6 +211,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   uint64_t* accb = empty + NSTAGE;
   uint32_t* tslot = (uint32_t*)(accb + 1);
 
+  // A CTA that starts after another one recorded a failure does nothing.
+  if (*(volatile int*)err) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = g.mtiles * g.ntiles;
   const int inst = blockIdx.x / tiles;
@@ -232,7 +244,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       for (int kc = 0; kc < g.nchunk; kc++) {
         const int s = kc % NSTAGE;
         if (kc >= NSTAGE) {
-          if (!mbar_wait(&empty[s], ((kc / NSTAGE) - 1) & 1, WAIT_NS)) {
+          if (!mbar_wait(&empty[s], ((kc / NSTAGE) - 1) & 1, WAIT_NS, err)) {
             atomicExch(err, 1);
             break;
           }
@@ -249,7 +261,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       bool ok = true;
       for (int kc = 0; kc < g.nchunk && ok; kc++) {
         const int s = kc % NSTAGE;
-        if (!mbar_wait(&full[s], (kc / NSTAGE) & 1, WAIT_NS)) {
+        if (!mbar_wait(&full[s], (kc / NSTAGE) & 1, WAIT_NS, err)) {
           atomicExch(err, 2);
           ok = false;
           break;
@@ -261,15 +273,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         for (int i = 0; i < SPLIT_NSLICE; i++) {
 #pragma unroll 1
           for (int j = 0; j + i < SPLIT_NSLICE; j++) {
-            const int lvl = (i + j) < 2 ? (i + j) : 2;
-            // in loop order the first pair of level 0, 1, 2 is (0,0), (0,1), (0,2)
-            const uint32_t accum = (kc > 0 || !(i == 0 && j <= 2)) ? 1u : 0u;
+            const int lvl = (i + j) < NLEVEL - 1 ? (i + j) : NLEVEL - 1;
+            // in loop order the first pair of level 0..3 is (0,0), (0,1), (0,2), (0,3)
+            const uint32_t accum = (kc > 0 || !(i == 0 && j <= NLEVEL - 1)) ? 1u : 0u;
             const uint64_t ar = sdesc_kmajor_noswz(a0 + (i * 2 + 0) * SPLIT_A_SUB, 128, 256);
             const uint64_t ai = sdesc_kmajor_noswz(a0 + (i * 2 + 1) * SPLIT_A_SUB, 128, 256);
             const uint64_t br = sdesc_kmajor_noswz(b0 + (j * 2 + 0) * SPLIT_B_SUB, 128, 256);
             const uint64_t bi = sdesc_kmajor_noswz(b0 + (j * 2 + 1) * SPLIT_B_SUB, 128, 256);
             const uint32_t dre = tbase + (uint32_t)(lvl * SPLIT_N);
-            const uint32_t dim = tbase + (uint32_t)((3 + lvl) * SPLIT_N);
+            const uint32_t dim = tbase + (uint32_t)((NLEVEL + lvl) * SPLIT_N);
             umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
             umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
             umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
@@ -292,36 +304,41 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const float srow = pow2f(I.lexp[grow]);
     float4* outp = I.out;
     const int ldo = g.ldo;
+    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
     for (int c0 = 0; c0 < SPLIT_N; c0 += 16) {
-      float v[NACC][16];
+      // Re then Im: 4 level accumulators of 16 columns each -> float-float
+      float hi[2][16], lo[2][16];
 #pragma unroll
-      for (int a = 0; a < NACC; a++) tmem_ld16(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * SPLIT_N + c0), v[a]);
-      tmem_ld_wait();
-      if (!ok || !rvalid) continue;
+      for (int part = 0; part < 2; part++) {
+        float v[NLEVEL][16];
+#pragma unroll
+        for (int l = 0; l < NLEVEL; l++) tmem_ld16(tl + (uint32_t)((part * NLEVEL + l) * SPLIT_N + c0), v[l]);
+        tmem_ld_wait();
+        if (g.levels && ok && rvalid) {
+          for (int c = 0; c < 16; c++) {
+            const int gcol = nt * SPLIT_N + c0 + c;
+            if (gcol < g.ncols)
+              for (int l = 0; l < NLEVEL; l++)
+                g.levels[((size_t)(part * NLEVEL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          // levels 0..2 are exact multiples of 2^-16, 2^-24, 2^-32; level 3 carries the rest
+          float s, e;
+          two_sum(v[0][c], v[1][c], s, e);
+          e += v[2][c] + v[3][c];
+          fast_two_sum(s, e, hi[part][c], lo[part][c]);
+        }
+      }
+      if (!ok || !rvalid || g.levels) continue;
 #pragma unroll
       for (int c = 0; c < 16; c++) {
         const int gcol = nt * SPLIT_N + c0 + c;
         if (gcol >= g.ncols) continue;
-        if (g.levels) {
-          for (int a = 0; a < NACC; a++) g.levels[((size_t)a * g.ncols + gcol) * ldo + grow] = v[a][c];
-          continue;
-        }
         const float sc = srow * pow2f(I.rexp[gcol]);
-        float4 o;
-        {
-          float s, e;
-          two_sum(v[0][c], v[1][c], s, e);
-          e += v[2][c];
-          fast_two_sum(s, e, o.x, o.y);
-        }
-        {
-          float s, e;
-          two_sum(v[3][c], v[4][c], s, e);
-          e += v[5][c];
-          fast_two_sum(s, e, o.z, o.w);
-        }
-        o.x *= sc; o.y *= sc; o.z *= sc; o.w *= sc;
-        outp[(size_t)gcol * ldo + grow] = o;
+        outp[(size_t)gcol * ldo + grow] =
+            make_float4(hi[0][c] * sc, lo[0][c] * sc, hi[1][c] * sc, lo[1][c] * sc);
       }
     }
   }

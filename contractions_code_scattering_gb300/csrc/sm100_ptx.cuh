@@ -47,13 +47,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Wait for the phase with the given parity to complete, for at most
-// timeout_ns of wall time.  Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t timeout_ns) {
+// timeout_ns of wall time, or until *abort becomes non-zero (when given).
+// Returns false on timeout or abort.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t timeout_ns,
+                                          const volatile int* abort = nullptr) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (;;) {
     for (int i = 0; i < 64; i++)
       if (mbar_try_wait(bar, parity)) return true;
+    if (abort && *abort) return false;
     if (globaltimer() - t0 > timeout_ns) return false;
   }
 }

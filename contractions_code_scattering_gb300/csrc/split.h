@@ -11,7 +11,7 @@ namespace ctr {
 
 // Tile geometry (see kernels_split.cu).
 constexpr int SPLIT_M = 128;     // rows of an output tile (TMEM lanes)
-constexpr int SPLIT_N = 80;      // columns of an output tile (6 accumulators x 80 <= 512 TMEM columns)
+constexpr int SPLIT_N = 64;      // columns of an output tile (8 accumulators x 64 = 512 TMEM columns)
 constexpr int SPLIT_K = 16;      // K of one MMA / one pipeline chunk
 constexpr int SPLIT_NSLICE = 5;  // BF16 slices per FP64 value
 constexpr int SPLIT_MAXK = 128;  // largest Nev the engine takes (exactness bound of the leading level)
