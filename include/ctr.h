@@ -94,8 +94,8 @@ int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, c
 
 /* Diagnostics of the split engine: for one product x*y (nev x nev, device),
  * write the raw FP32 tensor-core accumulators before recombination, as
- * levels[6][nev][128] (Re level 0, 1, >=2, Im level 0, 1, >=2; element (i,j)
- * at [a][j][i]), in units of the per-row / per-column power-of-two scales. */
+ * levels[8][nev][128] (Re levels 0, 1, 2, >=3, then Im; element (i,j) at
+ * [a][j][i]), in units of the per-row / per-column power-of-two scales. */
 int ctr_split_levels(int nev, const double* x, const double* y, float* levels, void* stream);
 
 /* On-device source-time average of the dumpData routines (lib/contract.cpp:616-643):
