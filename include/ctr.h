@@ -26,6 +26,7 @@
 #ifndef CTR_H
 #define CTR_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -97,6 +98,24 @@ int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, c
  * levels[8][nev][128] (Re levels 0, 1, 2, >=3, then Im; element (i,j) at
  * [a][j][i]), in units of the per-row / per-column power-of-two scales. */
 int ctr_split_levels(int nev, const double* x, const double* y, float* levels, void* stream);
+
+/* Allocation-free rho-rho for one t_sink row: the same correlators as
+ * ctr_rho(CTR_ENGINE_FP64, nev, nt, tf, tf+1, prop_row, mom5, corr, stream),
+ * for callers that cannot allocate device memory when they call (their memory
+ * budget is held by a fixed pool, or they must not trigger the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  This entry point has no
+ * counterpart in the reference.  Its only scratch is a fixed 32 MiB device
+ * array inside the library (enough for Nev <= 114), held by every GPU that
+ * loads the library until the process exits; larger Nev are rejected with
+ * CTR_ERR_ARG.  It calls no cudaMalloc/cudaFree or other allocating routine.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU (different streams, or threads) race.
+ * prop_row: tau(tf, .) [Nt][4][4][N][N]; mom5 [Nt][5][N][N]; corr [Nt][16][3]. */
+int ctr_rho_noalloc(int nev, int nt, int tf, const double* prop_row, const double* mom5, double* corr,
+                    void* stream);
+/* Size in bytes of ctr_rho_noalloc's fixed device scratch array. */
+size_t ctr_rho_noalloc_scratch_bytes(void);
 
 /* On-device source-time average of the dumpData routines (lib/contract.cpp:616-643):
  * avg[dt][c] = scale/Nt * sum_ti corr[(ti+dt)%Nt][ti][c]; corr device [Nt][Nt][ncorr]. */
