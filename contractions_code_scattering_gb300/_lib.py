@@ -50,6 +50,10 @@ def lib(build_if_missing=True):
     L.ctr_sync.argtypes = [vp]
     L.ctr_zgemm_batched.argtypes = [i, i, i, vp, vp, vp, vp]
     L.ctr_split_levels.argtypes = [i, vp, vp, vp, vp]
+    L.ctr_rhopi.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp]
+    L.ctr_pipi.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.ctr_loop_unity.argtypes = [i, i, i, vp, vp, vp, vp]
+    L.ctr_sigmapi.argtypes = [i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
     L.ctr_split_available.restype = i
     L.ctr_release_workspace.restype = None
     L.ctr_timing_enable.argtypes = [i]

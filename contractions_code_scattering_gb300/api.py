@@ -123,6 +123,66 @@ def run_contract_sigma(prop_rows, mom2, engine="fp64", tf_range=None, out=None, 
     return out
 
 
+def prop_diag(prop):
+    """tau(t,t) gathered on the device from the full perambulator [Nt,Nt,4,4,N,N]
+    (LapH_prop::copyToDeviceExtraDiag, lib/contract.cpp:549-570)."""
+    import torch
+    nt = prop.shape[0]
+    idx = torch.arange(nt, device=prop.device)
+    return prop[idx, idx].contiguous()
+
+
+def _rows(tf_range, nt):
+    return tf_range if tf_range is not None else (0, nt)
+
+
+def run_contract_rhopi(prop_rows, diag, p1, p2, mom5_p1p2, idir, engine="fp64", tf_range=None, stream=None):
+    """rho -> pi pi (run_ContractRhoPi): corr [rows, Nt, 4]."""
+    import torch
+    nt, nev = p1.shape[0], p1.shape[-1]
+    tf0, tf1 = _rows(tf_range, nt)
+    out = torch.empty((tf1 - tf0, nt, 4), dtype=torch.complex128, device=p1.device)
+    check(lib().ctr_rhopi(_engine(engine), nev, nt, tf0, tf1, idir, _dev(prop_rows, "prop_rows"), _dev(diag, "diag"),
+                          _dev(p1, "p1"), _dev(p2, "p2"), _dev(mom5_p1p2, "mom5_p1p2"), _dev(out, "out"),
+                          _stream(stream)))
+    return out
+
+
+def run_contract_pipi(prop_rows, diag, p1, p2, p3, p4, isospin, engine="fp64", tf_range=None, stream=None):
+    """pi pi -> pi pi (run_ContractPiPi / run_ContractPiPi_I0; isospin 1 or 0): corr [rows, Nt, 5]."""
+    import torch
+    nt, nev = p1.shape[0], p1.shape[-1]
+    tf0, tf1 = _rows(tf_range, nt)
+    out = torch.empty((tf1 - tf0, nt, 5), dtype=torch.complex128, device=p1.device)
+    check(lib().ctr_pipi(_engine(engine), nev, nt, tf0, tf1, isospin, _dev(prop_rows, "prop_rows"), _dev(diag, "diag"),
+                         _dev(p1, "p1"), _dev(p2, "p2"), _dev(p3, "p3"), _dev(p4, "p4"), _dev(out, "out"),
+                         _stream(stream)))
+    return out
+
+
+def run_contract_loop_unity(diag, mom, engine="fp64", stream=None):
+    """Loop-unity (run_ContractLoopUnity): loop [Nt]."""
+    import torch
+    nt, nev = mom.shape[0], mom.shape[-1]
+    out = torch.empty((nt,), dtype=torch.complex128, device=mom.device)
+    check(lib().ctr_loop_unity(_engine(engine), nev, nt, _dev(diag, "diag"), _dev(mom, "mom"), _dev(out, "out"),
+                               _stream(stream)))
+    return out
+
+
+def run_contract_sigmapi(prop_rows, diag, p1, p2, mom2_p1p2, engine="fp64", tf_range=None, stream=None):
+    """sigma -> pi pi (hor fish + triangle): (hor_fish [Nt], triangle [rows, Nt, 2])."""
+    import torch
+    nt, nev = p1.shape[0], p1.shape[-1]
+    tf0, tf1 = _rows(tf_range, nt)
+    hf = torch.empty((nt,), dtype=torch.complex128, device=p1.device)
+    tri = torch.empty((tf1 - tf0, nt, 2), dtype=torch.complex128, device=p1.device)
+    check(lib().ctr_sigmapi(_engine(engine), nev, nt, tf0, tf1, _dev(prop_rows, "prop_rows"), _dev(diag, "diag"),
+                            _dev(p1, "p1"), _dev(p2, "p2"), _dev(mom2_p1p2, "mom2_p1p2"), _dev(hf, "hor_fish"),
+                            _dev(tri, "triangle"), _stream(stream)))
+    return hf, tri
+
+
 def zgemm_batched(x, y, engine="fp64", out=None, stream=None):
     """Block products out[b] = x[b] @ y[b] for device tensors [nb, N, N] complex128."""
     import torch

@@ -88,6 +88,9 @@ enum {
   WS_COUNT
 };
 
+// Perambulator file payload (complex128, file order) -> host buffer in the library layout.
+int reorder_prop_device(int N, int Nt, const double* file_payload, int single, void* host_out);
+
 // Reads (and clears) the device-side error flag of the split engine; syncs the stream.
 int split_error_check(cudaStream_t s);
 int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,

@@ -23,6 +23,7 @@
 //    no-swizzle core-matrix layout, grouped by K-chunk of 16, so one pipeline
 //    stage (all slices and both real/imag planes of one K-chunk) is one
 //    contiguous bulk async copy per operand.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 
@@ -183,9 +184,12 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
 }
 
 // ------------------------------------------------------------------ GEMM
-// One CTA computes one 128 x 80 output tile of one GEMM instance.
-// Warp 0: TMEM allocation and the bulk-copy producer; warp 1: MMA issue;
-// warps 2..5: epilogue (TMEM lanes 32*(warp%4) .. +31).
+// Persistent kernel: each CTA walks output tiles t = blockIdx.x, +gridDim.x, ...
+// of 128 x SPLIT_N.  Warp 0: TMEM allocation and the bulk-copy producer, which
+// runs ahead across tile boundaries through an NSTAGE ring; warp 1: MMA issue;
+// warps 2..5: epilogue (TMEM lanes 32*(warp%4) .. +31).  The MMA warp and the
+// epilogue hand the TMEM accumulators back and forth with two mbarriers
+// (tmem_full after the last MMA of a tile, tmem_empty once drained).
 constexpr int GEMM_THREADS = 192;
 constexpr int NSTAGE = 3;
 constexpr int NLEVEL = 4;  // accumulation levels i+j = 0, 1, 2, >=3; (re, im) x 4 x SPLIT_N = 512 TMEM columns
@@ -193,7 +197,7 @@ constexpr uint32_t TMEM_COLS = 512;
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
 
 constexpr size_t gemm_smem_bytes() {
-  return (size_t)NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE) + 256;
+  return (size_t)NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE) + 512;
 }
 
 __device__ __forceinline__ float pow2f(int e) {
@@ -201,35 +205,67 @@ __device__ __forceinline__ float pow2f(int e) {
   return __int_as_float((127 + e) << 23);
 }
 
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// All MMAs of one K chunk: 15 slice pairs x 4 real products into the 8 level
+// accumulators.  adesc / bdesc describe sub-tile (slice 0, re) of the stage;
+// the other sub-tiles are constant byte offsets (added as offset >> 4 to the
+// start-address field, which cannot carry: shared addresses are < 2^18).
+__device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
+  constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, SPLIT_N, false);
+  constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, SPLIT_N, true);
+#pragma unroll
+  for (int i = 0; i < SPLIT_NSLICE; i++) {
+#pragma unroll
+    for (int j = 0; j + i < SPLIT_NSLICE; j++) {
+      const int lvl = (i + j) < NLEVEL - 1 ? (i + j) : NLEVEL - 1;
+      // in loop order the first pair of level 0..3 is (0,0), (0,1), (0,2), (0,3)
+      const uint32_t accum = (!first_chunk || !(i == 0 && j <= NLEVEL - 1)) ? 1u : 0u;
+      const uint64_t ar = adesc + (uint64_t)(((i * 2 + 0) * SPLIT_A_SUB) >> 4);
+      const uint64_t ai = adesc + (uint64_t)(((i * 2 + 1) * SPLIT_A_SUB) >> 4);
+      const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * SPLIT_B_SUB) >> 4);
+      const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * SPLIT_B_SUB) >> 4);
+      const uint32_t dre = tbase + (uint32_t)(lvl * SPLIT_N);
+      const uint32_t dim = tbase + (uint32_t)((NLEVEL + lvl) * SPLIT_N);
+      umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
+      umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
+      umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
+      umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
+    }
+  }
+}
+
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
-    split_gemm_kernel(SplitGemmBatch g, int* __restrict__ err) {
+    split_gemm_kernel(SplitGemmBatch g, int ntiles_total, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;
   uint8_t* sB = smem + NSTAGE * SPLIT_A_STAGE;
   uint64_t* full = (uint64_t*)(smem + NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE));
   uint64_t* empty = full + NSTAGE;
-  uint64_t* accb = empty + NSTAGE;
-  uint32_t* tslot = (uint32_t*)(accb + 1);
+  uint64_t* tfull = empty + NSTAGE;
+  uint64_t* tempty = tfull + 1;
+  uint64_t* drainb = tempty + 1;
+  uint32_t* tslot = (uint32_t*)(drainb + 1);
+  int* sexp = (int*)(tslot + 4);  // SPLIT_N column exponents of the current tile
 
-  // A CTA that starts after another one recorded a failure does nothing.
-  if (*(volatile int*)err) return;
+  volatile int* status = (volatile int*)(tslot + 1);  // block-uniform decisions
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles = g.mtiles * g.ntiles;
-  const int inst = blockIdx.x / tiles;
-  const int mt = (blockIdx.x % tiles) / g.ntiles;
-  const int nt = blockIdx.x % g.ntiles;
-  const SplitGemmInst I = g.inst[inst];
-  const uint8_t* gA = I.left + (size_t)mt * g.nchunk * SPLIT_A_STAGE;
-  const uint8_t* gB = I.right + (size_t)nt * g.nchunk * SPLIT_B_STAGE;
+  const int per_inst = g.mtiles * g.ntiles;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accb, 1);
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 4);  // one arrival per epilogue warp
+    mbar_init(drainb, 1);
     fence_mbar_init();
+    // A CTA that starts after another one recorded a failure does nothing.
+    status[0] = *(volatile int*)err;
   }
+  __syncthreads();
+  if (status[0]) return;  // uniform: every thread read the same shared value
   if (warp == 0) {
     tmem_alloc(tslot, TMEM_COLS);
     tmem_relinquish();
@@ -241,105 +277,126 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      for (int kc = 0; kc < g.nchunk; kc++) {
-        const int s = kc % NSTAGE;
-        if (kc >= NSTAGE) {
-          if (!mbar_wait(&empty[s], ((kc / NSTAGE) - 1) & 1, WAIT_NS, err)) {
+      uint32_t g_chunk = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x) {
+        const int inst = tile / per_inst, mt = (tile % per_inst) / g.ntiles, nt = tile % g.ntiles;
+        const SplitGemmInst* I = &g.inst[inst];
+        const uint8_t* gA = I->left + (size_t)mt * g.nchunk * SPLIT_A_STAGE;
+        const uint8_t* gB = I->right + (size_t)nt * g.nchunk * SPLIT_B_STAGE;
+        for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
+          const int s = g_chunk % NSTAGE;
+          if (g_chunk >= NSTAGE && !mbar_wait(&empty[s], ((g_chunk / NSTAGE) - 1) & 1, WAIT_NS, err)) {
             atomicExch(err, 1);
+            ok = false;
             break;
           }
+          mbar_arrive_expect_tx(&full[s], SPLIT_A_STAGE + SPLIT_B_STAGE);
+          bulk_g2s(sA + s * SPLIT_A_STAGE, gA + (size_t)kc * SPLIT_A_STAGE, SPLIT_A_STAGE, &full[s]);
+          bulk_g2s(sB + s * SPLIT_B_STAGE, gB + (size_t)kc * SPLIT_B_STAGE, SPLIT_B_STAGE, &full[s]);
         }
-        mbar_arrive_expect_tx(&full[s], SPLIT_A_STAGE + SPLIT_B_STAGE);
-        bulk_g2s(sA + s * SPLIT_A_STAGE, gA + (size_t)kc * SPLIT_A_STAGE, SPLIT_A_STAGE, &full[s]);
-        bulk_g2s(sB + s * SPLIT_B_STAGE, gB + (size_t)kc * SPLIT_B_STAGE, SPLIT_B_STAGE, &full[s]);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, SPLIT_N, false);
-      constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, SPLIT_N, true);
+      uint32_t g_chunk = 0, local = 0;
       bool ok = true;
-      for (int kc = 0; kc < g.nchunk && ok; kc++) {
-        const int s = kc % NSTAGE;
-        if (!mbar_wait(&full[s], (kc / NSTAGE) & 1, WAIT_NS, err)) {
-          atomicExch(err, 2);
+      const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
+      const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
+      for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x, local++) {
+        // wait until the epilogue drained the previous tile's accumulators
+        if (local > 0 && !mbar_wait(tempty, (local - 1) & 1, 2 * WAIT_NS, err)) {
+          atomicExch(err, 4);
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t a0 = smem_u32(sA + s * SPLIT_A_STAGE);
-        const uint32_t b0 = smem_u32(sB + s * SPLIT_B_STAGE);
-#pragma unroll 1
-        for (int i = 0; i < SPLIT_NSLICE; i++) {
-#pragma unroll 1
-          for (int j = 0; j + i < SPLIT_NSLICE; j++) {
-            const int lvl = (i + j) < NLEVEL - 1 ? (i + j) : NLEVEL - 1;
-            // in loop order the first pair of level 0..3 is (0,0), (0,1), (0,2), (0,3)
-            const uint32_t accum = (kc > 0 || !(i == 0 && j <= NLEVEL - 1)) ? 1u : 0u;
-            const uint64_t ar = sdesc_kmajor_noswz(a0 + (i * 2 + 0) * SPLIT_A_SUB, 128, 256);
-            const uint64_t ai = sdesc_kmajor_noswz(a0 + (i * 2 + 1) * SPLIT_A_SUB, 128, 256);
-            const uint64_t br = sdesc_kmajor_noswz(b0 + (j * 2 + 0) * SPLIT_B_SUB, 128, 256);
-            const uint64_t bi = sdesc_kmajor_noswz(b0 + (j * 2 + 1) * SPLIT_B_SUB, 128, 256);
-            const uint32_t dre = tbase + (uint32_t)(lvl * SPLIT_N);
-            const uint32_t dim = tbase + (uint32_t)((NLEVEL + lvl) * SPLIT_N);
-            umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
-            umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
-            umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
-            umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
+        for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
+          const int s = g_chunk % NSTAGE;
+          if (!mbar_wait(&full[s], (g_chunk / NSTAGE) & 1, WAIT_NS, err)) {
+            atomicExch(err, 2);
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          issue_chunk(tbase, adesc0 + (uint64_t)((s * SPLIT_A_STAGE) >> 4),
+                      bdesc0 + (uint64_t)((s * SPLIT_B_STAGE) >> 4), kc == 0);
+          umma_commit(&empty[s]);  // stage s free once these MMAs have read it
         }
-        umma_commit(&empty[s]);  // stage s free once these MMAs have read it
+        if (ok) umma_commit(tfull);
       }
-      umma_commit(accb);  // also arrives (with nothing in flight) after a timeout
+      // wait for every issued MMA before the accumulators are released
+      umma_commit(drainb);
+      if (!mbar_wait(drainb, 0, WAIT_NS)) atomicExch(err, 5);
     }
   } else {
     // epilogue: warps 2..5 -> TMEM lane quadrant warp % 4
     const int q = warp & 3;
+    const int et = threadIdx.x - 64;  // 0..127 within the epilogue group
     const int row = q * 32 + lane;
-    const bool ok = mbar_wait(accb, 0, 4 * WAIT_NS);
-    if (!ok) atomicExch(err, 3);
-    tc_fence_after();
-    const int grow = mt * SPLIT_M + row;
-    const bool rvalid = grow < g.mrows;
-    const float srow = pow2f(I.lexp[grow]);
-    float4* outp = I.out;
-    const int ldo = g.ldo;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
-    for (int c0 = 0; c0 < SPLIT_N; c0 += 16) {
-      // Re then Im: 4 level accumulators of 16 columns each -> float-float
-      float hi[2][16], lo[2][16];
+    uint32_t local = 0;
+    for (int tile = blockIdx.x; tile < ntiles_total; tile += gridDim.x, local++) {
+      const int inst = tile / per_inst, mt = (tile % per_inst) / g.ntiles, nt = tile % g.ntiles;
+      const SplitGemmInst* I = &g.inst[inst];
+      // stage this tile's column exponents; the barrier also keeps the previous
+      // tile's values until every epilogue thread has used them
+      epi_bar();
+      if (et < SPLIT_N) sexp[et] = I->rexp[nt * SPLIT_N + et];
+      const int grow = mt * SPLIT_M + row;
+      const bool rvalid = grow < g.mrows;
+      const float srow = pow2f(I->lexp[grow]);
+      // one thread waits for the accumulators; the outcome is shared so that
+      // all epilogue threads leave the loop together
+      if (et == 0) {
+        const bool done = mbar_wait(tfull, local & 1, 4 * WAIT_NS, err);
+        if (!done) atomicExch(err, 3);
+        status[1] = done ? 0 : 1;
+      }
+      epi_bar();
+      if (status[1]) break;
+      tc_fence_after();
+      float4* outp = I->out;
+      const int ldo = g.ldo;
+      for (int c0 = 0; c0 < SPLIT_N; c0 += 16) {
+        // Re then Im: 4 level accumulators of 16 columns each -> float-float
+        float hi[2][16], lo[2][16];
 #pragma unroll
-      for (int part = 0; part < 2; part++) {
-        float v[NLEVEL][16];
+        for (int part = 0; part < 2; part++) {
+          float v[NLEVEL][16];
 #pragma unroll
-        for (int l = 0; l < NLEVEL; l++) tmem_ld16(tl + (uint32_t)((part * NLEVEL + l) * SPLIT_N + c0), v[l]);
-        tmem_ld_wait();
-        if (g.levels && ok && rvalid) {
+          for (int l = 0; l < NLEVEL; l++) tmem_ld16(tl + (uint32_t)((part * NLEVEL + l) * SPLIT_N + c0), v[l]);
+          tmem_ld_wait();
+          if (g.levels && rvalid) {
+            for (int c = 0; c < 16; c++) {
+              const int gcol = nt * SPLIT_N + c0 + c;
+              if (gcol < g.ncols)
+                for (int l = 0; l < NLEVEL; l++)
+                  g.levels[((size_t)(part * NLEVEL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
+            }
+          }
+#pragma unroll
           for (int c = 0; c < 16; c++) {
-            const int gcol = nt * SPLIT_N + c0 + c;
-            if (gcol < g.ncols)
-              for (int l = 0; l < NLEVEL; l++)
-                g.levels[((size_t)(part * NLEVEL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
+            // levels 0..2 are exact multiples of 2^-16, 2^-24, 2^-32; level 3 carries the rest
+            float s, e;
+            two_sum(v[0][c], v[1][c], s, e);
+            e += v[2][c] + v[3][c];
+            fast_two_sum(s, e, hi[part][c], lo[part][c]);
           }
         }
+        if (!rvalid || g.levels) continue;
 #pragma unroll
         for (int c = 0; c < 16; c++) {
-          // levels 0..2 are exact multiples of 2^-16, 2^-24, 2^-32; level 3 carries the rest
-          float s, e;
-          two_sum(v[0][c], v[1][c], s, e);
-          e += v[2][c] + v[3][c];
-          fast_two_sum(s, e, hi[part][c], lo[part][c]);
+          const int gcol = nt * SPLIT_N + c0 + c;
+          if (gcol >= g.ncols) continue;
+          const float sc = srow * pow2f(sexp[c0 + c]);
+          outp[(size_t)gcol * ldo + grow] = make_float4(hi[0][c] * sc, lo[0][c] * sc, hi[1][c] * sc, lo[1][c] * sc);
         }
       }
-      if (!ok || !rvalid || g.levels) continue;
-#pragma unroll
-      for (int c = 0; c < 16; c++) {
-        const int gcol = nt * SPLIT_N + c0 + c;
-        if (gcol >= g.ncols) continue;
-        const float sc = srow * pow2f(I.rexp[gcol]);
-        outp[(size_t)gcol * ldo + grow] =
-            make_float4(hi[0][c] * sc, lo[0][c] * sc, hi[1][c] * sc, lo[1][c] * sc);
-      }
+      // accumulators drained: hand TMEM back to the MMA warp
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty);
     }
   }
   tc_fence_before();
@@ -425,8 +482,17 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
     CTR_CUDA(cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    CTR_CUDA(cudaGetDevice(&dev));
+    CTR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const long long total = (long long)ninst * g.mtiles * g.ntiles;
+  if (total > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
+  const int grid = (int)std::min<long long>(total, nsm);
   TimedLaunch tl(s, "split_gemm");
-  split_gemm_kernel<<<ninst * g.mtiles * g.ntiles, GEMM_THREADS, smem, s>>>(g, d_err);
+  split_gemm_kernel<<<grid, GEMM_THREADS, smem, s>>>(g, (int)total, d_err);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

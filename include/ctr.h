@@ -86,6 +86,60 @@ int ctr_rho(int engine, int nev, int nt, int tf_begin, int tf_end, const double*
 int ctr_sigma(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
               const double* mom2, double* corr, void* stream);
 
+/* ---------------------------------------------------- chain diagrams (FP64)
+ * prop_diag: tau(t,t) [Nt][4][4][N][N] (the reference's "extra" device buffer,
+ * lib/contract.cpp:549-570).  Elementals [Nt][N][N] unless noted.  The split
+ * engine returns CTR_ERR_UNSUPPORTED for these families. */
+
+/* rho -> pi pi for gamma_idir (run_ContractRhoPi, lib/contract_kernels_rhopi.cu:64-137):
+ * mom5_p1p2 [Nt][5][N][N]; corr [tf_end-tf_begin][Nt][4] (one entry per rho operator). */
+int ctr_rhopi(int engine, int nev, int nt, int tf_begin, int tf_end, int idir, const double* prop_rows,
+              const double* prop_diag, const double* mom_p1, const double* mom_p2, const double* mom5_p1p2,
+              double* corr, void* stream);
+
+/* pi pi -> pi pi (run_ContractPiPi, isospin 1; run_ContractPiPi_I0, isospin 0;
+ * lib/contract_kernels_pipi.cu:170-502): corr [rows][Nt][5] = square, double triangle, star,
+ * fish, horizontal double triangle, with the isospin weights of the reference. */
+int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin, const double* prop_rows,
+             const double* prop_diag, const double* p1, const double* p2, const double* p3, const double* p4,
+             double* corr, void* stream);
+
+/* Loop with unit spin structure (run_ContractLoopUnity, lib/contract_kernels_loop_unity.cu:45-107):
+ * loop[t] = sum_s Tr[tau(t,t)_{ss} Phi(t)]. */
+int ctr_loop_unity(int engine, int nev, int nt, const double* prop_diag, const double* mom, double* loop,
+                   void* stream);
+
+/* sigma -> pi pi (run_ContractSigmaPi_fish_hor and run_ContractSigmaPi_triangle,
+ * lib/contract_kernels_sigmapi.cu:97-222): hor_fish [Nt] (may be NULL), triangle
+ * [rows][Nt][2] (may be NULL); mom2_p1p2 [Nt][2][N][N]. */
+int ctr_sigmapi(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
+                const double* prop_diag, const double* mom_p1, const double* mom_p2, const double* mom2_p1p2,
+                double* hor_fish, double* triangle, void* stream);
+
+/* ------------------------------------------------ host-level API (status codes)
+ * The non-terminating forms of the reference's public API; interface.h and
+ * contract.h wrap them and terminate on error as the reference does.
+ * single != 0: prop holds complex64 (float) data, widened on the device; the
+ * rho and sigma contractions then run on the split engine. */
+int ctr_contract_init(int nev, int nt, int dev);             /* initContract (lib/contract.cpp:58-70) */
+int ctr_contract_destroy(void);                              /* destroyContract (lib/contract.cpp:72-88) */
+/* readPropH (lib/contract.cpp:91-160): 100-byte name, uint32 Nt, uint32 Nvec, complex128 payload in
+ * (s1,v1,t1,s2,v2,t2) order -> host_out [t1][t2][s1][s2][v1][v2] (complex64 if single);
+ * CTR_ERR_IO on a missing/short file or a size mismatch. */
+int ctr_read_prop(const char* path, int nev, int nt, int single, void* host_out);
+/* Momentum list (lib/catchOpts.cpp:108-233): momcomb lines of nmom*3 integers, nmom in {1,2,4};
+ * p [4][3][momcomb]; for nmom = 2 the third momentum is p1 + p2. */
+int ctr_read_momenta(const char* path, int nmom, int momcomb, int* p);
+/* calculate* bodies (lib/interface.cpp:6-390): host inputs, results appended to outfile. */
+int ctr_calculate_rho(int nev, int nt, const void* prop, const double* mom, int single, const char* outfile);
+int ctr_calculate_rhopi(int idir, int nev, int nt, const void* prop, const double* p1, const double* p2,
+                        const double* p1p2, int single, const char* outfile);
+int ctr_calculate_pipi(int nev, int nt, const void* prop, const double* p1, const double* p2, const double* p3,
+                       const double* p4, int single, const char* outfile, int isospin);
+int ctr_calculate_sigma(int nev, int nt, const void* prop, const double* mom, int single, const char* outfile);
+int ctr_calculate_sigmapi(int nev, int nt, const void* prop, const double* p1, const double* p2,
+                          const double* p1p2, int single, const char* outfile);
+
 /* Batched complex block products c[b] = x[b] * y[b] (nev x nev, row-major
  * complex128, device pointers given in host arrays of length nbatch).  The unit
  * both engines build the diagram chains from (the 25x25-tiled GEMM loops of every
