@@ -5,7 +5,7 @@ Workload (one step): the rho two-point at production size, Nev=100, Lt=64,
 7 momenta |p|^2 <= 1, 3 polarisations (gamma_i (x) Phi at both ends), every
 (t_src, t_sink) pair: 64*64*3*7 = 86,016 spin-summed correlator entries
 ("diagrams"), each a sum of 16 spin terms coef*Tr[(Phi(tf) tau_ab)^dag tau_cd Phi(ti)].
-Inputs are seeded synthetic perambulators / elementals (SURVEY shapes), resident
+Inputs are seeded synthetic perambulators / elementals of those shapes, resident
 in HBM for `value`; `e2e` re-copies them from pinned host memory every step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--engine split|fp64]
@@ -361,8 +361,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "diagrams/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if engine == "fp64" else "f64-equivalent (bf16 x5 slices, fp32 acc)",
-        "data": "synthetic (seeded tau/Phi, SURVEY distributions)",
+        "vs_baseline": None, "dtype": "f64" if engine == "fp64" else "f64-equivalent (bf16 x5 balanced 9-bit slices, fp32 acc)",
+        "data": "synthetic (seeded tau/Phi: complex Gaussian N(0,1/Nev) x exp(-0.35|dt|), gamma5-hermitian; Phi(-p)=Phi(p)^dagger)",
         "config": {"workload": WORKLOAD, "engine": engine, "nev": nev, "lt": nt, "momenta": len(moms),
                    "diagrams_per_step": diagrams, "l2": "inputs larger than L2 (tau 10.5 GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},

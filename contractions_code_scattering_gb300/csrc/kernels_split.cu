@@ -4,21 +4,24 @@
 // tensor cores as follows.
 //  * Slicing.  Every row of the left operand X (every column of the right
 //    operand Y) gets a power-of-two scale 2^E with all |entries| < 2^E.  The
-//    scaled magnitudes are cut into NSLICE = 5 pieces of 8 bits,
-//    x/2^E = sign * sum_s u_s 2^{-8(s+1)}, u_s in [0,255], taken straight from
-//    the FP64 bit pattern with integer operations (no FP64 arithmetic).  Each
-//    piece sign*u_s*2^{-8(s+1)} is exact in BF16.  The cut is rounded to
-//    nearest at 2^-40, so the residual is <= 2^-41 and unbiased.
+//    scaled magnitude |x|/2^E is written in balanced base-512 digits,
+//    |x|/2^E = sum_s d_s 2^{-8-9s}, d_0 in [0,256], d_s in [-256,255] (s >= 1),
+//    taken straight from the FP64 bit pattern with integer operations (no FP64
+//    arithmetic).  Every |d_s| <= 256 is an integer of at most 8 significant
+//    bits, so each piece sign*d_s*2^{-8-9s} is exact in BF16 while carrying 9
+//    bits.  The digits are rounded to nearest at the last one: with
+//    NSLICE = 5 the residual is <= 2^-45 of 2^E and unbiased.
 //  * MMA.  Slice pairs (i,j) with i+j <= 4 (15 pairs) are multiplied with
 //    tcgen05.mma kind::f16 (BF16 in, FP32 accumulate in TMEM); the complex
 //    product takes 4 real MMAs per pair (the -Xi*Yi term uses the A-negate bit).
 //    Pairs accumulate in four levels, i+j = 0, 1, 2 and >= 3.  Levels 0-2 hold
-//    integer multiples of 2^-16, 2^-24, 2^-32 below 2^24 units (for K <= 128
-//    and non-adversarial data), which the FP32 tensor-core accumulation keeps
-//    exactly; measured on GB300, an accumulator mixing level 2 with the much
-//    smaller levels 3-4 loses ~6 bits to truncation, hence the separate level.
-//    Level values are combined in float-float (two FP32 words, ~48 bits) and
-//    scaled by 2^{E_row + E_col}.
+//    integer multiples of 2^-16, 2^-25, 2^-34 below 2^24 units (level 0 for any
+//    data with K <= 128, levels 1-2 for non-adversarial data), which the FP32
+//    tensor-core accumulation keeps exactly; measured on GB300, an accumulator
+//    mixing magnitudes loses low bits to truncation (~2^-17 of its size over a
+//    full K loop), which the separate levels confine to level >= 3, i.e. to
+//    ~2^-44 of the result.  Level values are combined in float-float (two FP32
+//    words, ~48 bits) and scaled by 2^{E_row + E_col}.
 //  * Data movement.  Slices are stored pre-tiled in the UMMA K-major
 //    no-swizzle core-matrix layout, grouped by K-chunk of 16, so one pipeline
 //    stage (all slices and both real/imag planes of one K-chunk) is one
@@ -56,15 +59,26 @@ __device__ __forceinline__ uint64_t f64_fixed(double x, int E, bool& neg) {
   return m >> (-sh);
 }
 
-// Slice s of the magnitude U (63-bit fixed point), rounded to nearest at the
-// last retained bit (2^-40): U + 2^22 is cut into u_0 in [0,256] and
-// u_1..u_4 in [0,255], all exact in BF16; the residual is at most 2^-41 and
-// has no sign bias.
-__device__ __forceinline__ uint64_t round_fixed(uint64_t U) { return U + (1ull << 22); }
+// Balanced digits of the magnitude U (63-bit fixed point, U < 2^63).  Digit s
+// sits at bit slice_shift(s) = 55 - 9s.  Adding 256 at every digit position
+// s >= 1 and half a unit of the last one turns the balanced digits into the
+// plain base-512 digits of W = U + digit_offset():
+//   d_0 = W >> 55 in [0, 256],  d_s = ((W >> (55 - 9s)) & 511) - 256,
+// and sum_s d_s 2^{55-9s} is U rounded to nearest at the last digit
+// (W < 2^63 + 2^55, no overflow).
+__host__ __device__ constexpr int slice_shift(int s) { return 55 - 9 * s; }
 
-__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t Urnd, int s, bool neg) {
-  const uint32_t u = s == 0 ? (uint32_t)(Urnd >> 55) : (uint32_t)(Urnd >> (55 - 8 * s)) & 0xFFu;
-  float v = (float)u * __int_as_float((127 - 8 * (s + 1)) << 23);
+__host__ __device__ constexpr uint64_t digit_offset(int nslice) {
+  uint64_t o = 1ull << (slice_shift(nslice - 1) - 1);
+  for (int s = 1; s < nslice; s++) o += 256ull << slice_shift(s);
+  return o;
+}
+
+__device__ __forceinline__ uint64_t round_fixed(uint64_t U) { return U + digit_offset(SPLIT_NSLICE); }
+
+__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t W, int s, bool neg) {
+  const int d = s == 0 ? (int)(W >> 55) : (int)((W >> slice_shift(s)) & 511u) - 256;
+  const float v = (float)d * __int_as_float((127 + slice_shift(s) - 63) << 23);  // d * 2^{-8-9s}, exact
   return __float2bfloat16_rn(neg ? -v : v);
 }
 
@@ -377,11 +391,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           }
 #pragma unroll
           for (int c = 0; c < 16; c++) {
-            // levels 0..2 are exact multiples of 2^-16, 2^-24, 2^-32; level 3 carries the rest
-            float s, e;
-            two_sum(v[0][c], v[1][c], s, e);
-            e += v[2][c] + v[3][c];
-            fast_two_sum(s, e, hi[part][c], lo[part][c]);
+            // levels 0..2 are exact multiples of 2^-16, 2^-25, 2^-34: two exact
+            // two-sums keep them; the rounding errors and level >= 3 (~2^-27 of
+            // the result) go to the low word, rounded at ~2^-48 of the result
+            float s1, e1, s2, e2;
+            two_sum(v[0][c], v[1][c], s1, e1);
+            two_sum(s1, v[2][c], s2, e2);
+            fast_two_sum(s2, (e1 + e2) + v[3][c], hi[part][c], lo[part][c]);
           }
         }
         if (!rvalid || g.levels) continue;

@@ -13,12 +13,12 @@ namespace ctr {
 constexpr int SPLIT_M = 128;     // rows of an output tile (TMEM lanes)
 constexpr int SPLIT_N = 64;      // columns of an output tile (8 accumulators x 64 = 512 TMEM columns)
 constexpr int SPLIT_K = 16;      // K of one MMA / one pipeline chunk
-constexpr int SPLIT_NSLICE = 5;  // BF16 slices per FP64 value
+constexpr int SPLIT_NSLICE = 5;  // BF16 slices (balanced base-512 digits) per FP64 value
 constexpr int SPLIT_MAXK = 128;  // largest Nev the engine takes (exactness bound of the leading level)
 constexpr int SPLIT_A_SUB = SPLIT_M * SPLIT_K * 2;                  // one (slice, plane) sub-tile, bytes
 constexpr int SPLIT_B_SUB = SPLIT_N * SPLIT_K * 2;
 constexpr int SPLIT_A_STAGE = SPLIT_NSLICE * 2 * SPLIT_A_SUB;       // 40960 B: all slices, re+im, one K chunk
-constexpr int SPLIT_B_STAGE = SPLIT_NSLICE * 2 * SPLIT_B_SUB;       // 25600 B
+constexpr int SPLIT_B_STAGE = SPLIT_NSLICE * 2 * SPLIT_B_SUB;       // 20480 B
 constexpr int SPLIT_MAXBLK = 32;
 
 // Slicing of a stacked operand.  Left: rows r -> row r%nev of blk[r/nev].
