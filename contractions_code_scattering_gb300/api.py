@@ -245,3 +245,121 @@ def split_levels(x, y, stream=None):
     check(lib().ctr_split_levels(n, _dev(x, "x"), _dev(y, "y"), ctypes.c_void_p(lv.data_ptr()), _stream(stream)))
     sync(stream)
     return lv[:, :, :n].transpose(1, 2)
+
+
+# ------------------------------------------------------ distillation profile
+FACTOR_TAU, FACTOR_PHI = 0, 1
+
+
+class ctr_factor(ctypes.Structure):
+    """One chain factor (include/ctr.h): tau(a, b)_{s1 s2} or diag(f) phi[a][b] diag(f)."""
+    _fields_ = [("kind", ctypes.c_int32), ("dag", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32),
+                ("s1", ctypes.c_int32), ("s2", ctypes.c_int32)]
+
+
+def _real(t, name):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError("%s must be a contiguous float64 CUDA tensor" % name)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def apply_profile(f, phi, out=None, stream=None):
+    """diag(f) phi[m] diag(f) for every matrix of phi [..., N, N] (device)."""
+    import torch
+    if out is None:
+        out = torch.empty_like(phi)
+    n = phi.shape[-1]
+    check(lib().ctr_apply_profile(n, phi.numel() // (n * n), _real(f, "f"), _dev(phi, "phi"), _dev(out, "out"),
+                                  _stream(stream)))
+    return out
+
+
+def chain_adjoint(prop, phi, f, chains, weights=None, values=True, grad=True, stream=None):
+    """Generic chain traces and their profile gradient (include/ctr.h: ctr_chain_adjoint).
+
+    chains: list of lists of (kind, dag, a, b, s1, s2); weights: complex per chain.
+    Returns (values [nchain] complex128 or None, grad [N] float64 or None)."""
+    import torch
+    nt, nev = prop.shape[0], prop.shape[-1]
+    nphi = phi.shape[1] if phi is not None else 0
+    off = np.zeros(len(chains) + 1, np.int32)
+    flat = []
+    for c, ch in enumerate(chains):
+        off[c + 1] = off[c] + len(ch)
+        flat += [ctr_factor(*fa) for fa in ch]
+    fac = (ctr_factor * max(1, len(flat)))(*flat)
+    w = None
+    if weights is not None:
+        w = np.ascontiguousarray(np.asarray(weights, np.complex128))
+    vals = torch.zeros(len(chains), dtype=torch.complex128, device=prop.device) if values else None
+    g = torch.zeros(nev, dtype=torch.float64, device=prop.device) if grad else None
+    check(lib().ctr_chain_adjoint(nev, nt, nphi, _dev(prop, "prop"), _dev(phi, "phi") if phi is not None else None,
+                                  _real(f, "f"), len(chains), _np_ptr(off), ctypes.cast(fac, ctypes.c_void_p),
+                                  _np_ptr(w) if w is not None else None,
+                                  _dev(vals, "values") if vals is not None else None,
+                                  _real(g, "grad") if g is not None else None, _stream(stream)))
+    return vals, g
+
+
+def rho_profile_vjp(prop, mom5, f, w, corr=True, grad=True, stream=None):
+    """rho-rho with profiled elementals: forward correlators [Nt, Nt, 48] of the entries
+    with nonzero weight w [Nt, Nt, 48] (complex, device) and grad [N] = Re sum w dcorr/df."""
+    import torch
+    nt, nev = prop.shape[0], prop.shape[-1]
+    c = torch.zeros((nt, nt, 48), dtype=torch.complex128, device=prop.device) if corr else None
+    g = torch.zeros(nev, dtype=torch.float64, device=prop.device) if grad else None
+    check(lib().ctr_rho_profile_vjp(nev, nt, _dev(prop, "prop"), _dev(mom5, "mom5"), _real(f, "f"),
+                                    _dev(w.contiguous(), "w"), _dev(c, "corr") if c is not None else None,
+                                    _real(g, "grad") if g is not None else None, _stream(stream)))
+    return c, g
+
+
+def pipi_profile_vjp(prop, p1, p2, p3, p4, f, w, isospin, corr=True, grad=True, stream=None):
+    """pi pi with profiled elementals: forward correlators [Nt, Nt, 5] (isospin-weighted
+    square, double triangle, star, fish, horizontal double triangle) of the pairs with
+    nonzero weight w [Nt, Nt, 5] and grad [N] = Re sum w dcorr/df."""
+    import torch
+    nt, nev = prop.shape[0], prop.shape[-1]
+    c = torch.zeros((nt, nt, 5), dtype=torch.complex128, device=prop.device) if corr else None
+    g = torch.zeros(nev, dtype=torch.float64, device=prop.device) if grad else None
+    check(lib().ctr_pipi_profile_vjp(nev, nt, isospin, _dev(prop, "prop"), _dev(p1, "p1"), _dev(p2, "p2"),
+                                     _dev(p3, "p3"), _dev(p4, "p4"), _real(f, "f"), _dev(w.contiguous(), "w"),
+                                     _dev(c, "corr") if c is not None else None,
+                                     _real(g, "grad") if g is not None else None, _stream(stream)))
+    return c, g
+
+
+class ctr_ztask(ctypes.Structure):
+    """One multi-term block product (include/ctr.h)."""
+    _fields_ = [("a", ctypes.c_void_p * 4), ("b", ctypes.c_void_p * 4), ("c", ctypes.c_void_p),
+                ("wre", ctypes.c_float * 4), ("wim", ctypes.c_float * 4), ("nterm", ctypes.c_int),
+                ("flags", ctypes.c_int)]
+
+
+def zgemm_tasks(x, y, tasks, weights=None, a_dagger=False, b_dagger=False, engine="fp64", out=None, stream=None):
+    """out[c] = sum_q w_q op(x[a_q]) op(y[b_q]) for tasks (a_list, b_list, c) on blocks of
+    x, y [nb, N, N] (device complex128); weights per term (real), op = conjugate transpose
+    where requested (include/ctr.h: ctr_zgemm_tasks)."""
+    import torch
+    n = x.shape[-1]
+    _dev(x, "x")
+    _dev(y, "y")
+    nc = 1 + max(t[2] for t in tasks)
+    if out is None:
+        out = torch.zeros((nc, n, n), dtype=torch.complex128, device=x.device)
+    stride = n * n * 16
+    arr = (ctr_ztask * len(tasks))()
+    for i, (al, bl, c) in enumerate(tasks):
+        z = arr[i]
+        z.nterm = len(al)
+        flags = 0
+        for q, (a, b) in enumerate(zip(al, bl)):
+            z.a[q] = x.data_ptr() + a * stride
+            z.b[q] = y.data_ptr() + b * stride
+            z.wre[q] = 1.0 if weights is None else float(weights[q])
+            flags |= (1 << q if a_dagger else 0) | (1 << (4 + q) if b_dagger else 0)
+        z.flags = flags
+        z.c = out.data_ptr() + c * stride
+    check(lib().ctr_zgemm_tasks(_engine(engine), n, len(tasks), ctypes.cast(arr, ctypes.c_void_p), _stream(stream)))
+    return out

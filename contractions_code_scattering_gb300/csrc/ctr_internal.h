@@ -85,6 +85,12 @@ enum {
   WS_ROWS,          // per-row partial results
   WS_PHI,           // sliced elementals
   WS_MISC,          // small tables (CSR of output rows)
+  WS_ROWABS,        // per-row error scales of the split engine
+  WS_REFINE,        // refinement list / patches of the split engine
+  WS_SPLITTASK,     // sliced operands of split-engine task stages
+  WS_SPLITJOBS,     // their job / instance / pointer tables
+  WS_SPLITJOBS2,
+  WS_SPLITJOBS3,
   WS_COUNT
 };
 
@@ -95,6 +101,10 @@ int reorder_prop_device(int N, int Nt, const double* file_payload, int single, v
 int split_error_check(cudaStream_t s);
 int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,
                         cudaStream_t stream);
+// A stage of FP64-engine GEMM tasks (struct ZTask, kernels.h) on the split
+// engine: C = sum_q w_q op(A_q) op(B_q) with real power-of-two weights.
+struct ZTask;
+int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream);
 
 // Upload a host array into a workspace slot (async on stream, host buffer is
 // kept alive by a pinned staging copy owned by the slot).
@@ -111,5 +121,12 @@ int twosided_fp64(int nev, int nt, int tf_begin, int tf_end, const double* prop_
 int twosided_split(int nev, int nt, int tf_begin, int tf_end, const double* prop_rows, const double* phi,
                    int nphi, const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
                    const std::vector<int32_t>& out_index, int nout, double* out, cudaStream_t stream);
+
+// Traces of chains of perambulator blocks and plain elementals in FP64
+// (the chain program of the profile adjoint, without a profile):
+// values[c] = Tr[F_1 ... F_n] for chain c = factors[off[c] .. off[c+1]);
+// perambulator factors index prop [rows][Nt][4][4][N][N] by (a = row, b = t2).
+int chain_values(int N, int Nt, int nphi, const double* prop, const double* phi, const std::vector<ctr_factor>& factors,
+                 const std::vector<int>& off, double* values, cudaStream_t s);
 
 }  // namespace ctr

@@ -274,3 +274,21 @@ int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, c
 }
 
 }  // extern "C"
+
+extern "C" int ctr_zgemm_tasks(int engine, int nev, int ntask, const ctr_ztask* tasks, void* stream) {
+  static_assert(sizeof(ctr_ztask) == sizeof(ctr::ZTask), "ctr_ztask and ZTask must match");
+  if (nev < 1 || ntask < 0 || (ntask > 0 && !tasks)) return ctr::fail(CTR_ERR_ARG, "ctr_zgemm_tasks: bad arguments");
+  for (int t = 0; t < ntask; t++) {
+    const ctr_ztask& z = tasks[t];
+    if (z.nterm < 1 || z.nterm > 4 || !z.c) return ctr::fail(CTR_ERR_ARG, "ctr_zgemm_tasks: task %d malformed", t);
+    for (int q = 0; q < z.nterm; q++)
+      if (!z.a[q] || !z.b[q]) return ctr::fail(CTR_ERR_ARG, "ctr_zgemm_tasks: task %d operand %d is null", t, q);
+  }
+  const ctr::ZTask* zt = reinterpret_cast<const ctr::ZTask*>(tasks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (engine == CTR_ENGINE_SPLIT) return ctr::zgemm_split_tasks(nev, zt, ntask, s);
+  if (engine != CTR_ENGINE_FP64) return ctr::fail(CTR_ERR_ARG, "unknown engine %d", engine);
+  void* d;
+  CTR_TRY(ctr::upload(ctr::WS_GEMM_A, zt, (size_t)ntask * sizeof(ctr::ZTask), &d, s));
+  return ctr::launch_zgemm_f64((const ctr::ZTask*)d, ntask, nev, s);
+}

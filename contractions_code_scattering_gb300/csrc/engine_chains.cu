@@ -1,5 +1,7 @@
 // Chain diagrams: rho->pipi, pipi->pipi (I=1, I=0), loop-unity, sigma->pipi,
-// on the plain FP64 engine.
+// on either engine: every GEMM stage below is a list of block-product tasks
+// that runs on the FP64 tile kernel or on the split-precision tensor-core
+// engine (zgemm_split_tasks); the closing traces are FP64 in both.
 //
 // The reference evaluates every spin row as an independent chain of 2-6 Nev^3
 // products (lib/calculate_{rhopi,pipi_*,sigmapi_*,loop_unity}_core.h).  The
@@ -30,6 +32,7 @@ struct Ctx {
   int N, Nt;
   size_t N2;
   cudaStream_t s;
+  int engine = CTR_ENGINE_FP64;
 };
 
 inline ZTask zt(const double2* A, const double2* B, double2* C, int flags = 0) {
@@ -46,6 +49,7 @@ inline ZTask zt(const double2* A, const double2* B, double2* C, int flags = 0) {
 // Stage = one launch of the batched GEMM; stages run in order on the stream.
 int run_stage(const Ctx& c, const std::vector<ZTask>& tasks, int slot) {
   if (tasks.empty()) return CTR_OK;
+  if (c.engine == CTR_ENGINE_SPLIT) return zgemm_split_tasks(c.N, tasks.data(), (int)tasks.size(), c.s);
   void* d;
   CTR_TRY(upload(slot, tasks.data(), tasks.size() * sizeof(ZTask), &d, c.s));
   return launch_zgemm_f64((const ZTask*)d, (int)tasks.size(), c.N, c.s);
@@ -143,9 +147,10 @@ int batch_pairs(size_t per_pair, int npairs) {
 }  // namespace
 
 // ------------------------------------------------------------------ pi pi
-int pipi_fp64(int N, int Nt, int tf_begin, int tf_end, int iso, const double* prop_rows, const double* prop_diag,
-              const double* p1, const double* p2, const double* p3, const double* p4, double* corr, cudaStream_t s) {
-  Ctx c{N, Nt, (size_t)N * N, s};
+int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* prop_rows, const double* prop_diag,
+              const double* p1, const double* p2, const double* p3, const double* p4, double* corr, cudaStream_t s,
+              int engine) {
+  Ctx c{N, Nt, (size_t)N * N, s, engine};
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)p1, *P2 = (const double2*)p2, *P3 = (const double2*)p3,
@@ -251,10 +256,10 @@ int pipi_fp64(int N, int Nt, int tf_begin, int tf_end, int iso, const double* pr
 // Row form (lib/calculate_rhopi_core.h): coef * Tr[Phi^{P1P2}_ip(tf) tau_{s5s6}
 // Phi_P2(ti) taud(ti)_{s1s2} Phi_P1(ti) tau_{s3s2}^dag] with s6 = s1, s4 = s3;
 // coef = c(iop, s3, s5) * g5(s1), so the sum over s1 is (T G R)_{s5 s2}.
-int rhopi_fp64(int N, int Nt, int tf_begin, int tf_end, int idir, const double* prop_rows, const double* prop_diag,
-               const double* mp1, const double* mp2, const double* mom5, double* corr, cudaStream_t s) {
+int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double* prop_rows, const double* prop_diag,
+               const double* mp1, const double* mp2, const double* mom5, double* corr, cudaStream_t s, int engine) {
   if (idir < 0 || idir > 2) return fail(CTR_ERR_ARG, "idir %d not in {0,1,2}", idir);
-  Ctx c{N, Nt, (size_t)N * N, s};
+  Ctx c{N, Nt, (size_t)N * N, s, engine};
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)mp1, *P2 = (const double2*)mp2, *P12 = (const double2*)mom5;
@@ -338,10 +343,10 @@ int rhopi_fp64(int N, int Nt, int tf_begin, int tf_end, int idir, const double* 
 // sum_ab coef * sum R_ab (.) conj taud_ab with R = Phi_P2 taud Phi_P1.
 // Triangle (lib/calculate_sigmapi_triangle_core.h): rows with s2 = s1, s4 = s3,
 // coef = g5(s1) g5(s3): sum_s3 g5(s3) tau_{s1s3} R_{s3s5} = (T G R)_{s1 s5}.
-int sigmapi_fp64(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* prop_diag,
+int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* prop_diag,
                  const double* mp1, const double* mp2, const double* mom2, double* hor_fish, double* tri,
-                 cudaStream_t s) {
-  Ctx c{N, Nt, (size_t)N * N, s};
+                 cudaStream_t s, int engine) {
+  Ctx c{N, Nt, (size_t)N * N, s, engine};
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)mp1, *P2 = (const double2*)mp2, *Px2 = (const double2*)mom2;
@@ -413,7 +418,7 @@ int sigmapi_fp64(int N, int Nt, int tf_begin, int tf_end, const double* prop_row
 // -------------------------------------------------------------- loop unity
 // lib/calculate_loop_unity_core.h: L(t) = sum_s Tr[taud(t)_{ss} Phi(t)] (trace of a product: Nev^2 work).
 int loop_unity_fp64(int N, int Nt, const double* prop_diag, const double* mom, double* loop, cudaStream_t s) {
-  Ctx c{N, Nt, (size_t)N * N, s};
+  Ctx c{N, Nt, (size_t)N * N, s, CTR_ENGINE_FP64};
   const double2 *diag = (const double2*)prop_diag, *P = (const double2*)mom;
   void* trm;
   CTR_TRY(workspace(WS_ROWS).get((size_t)Nt * 4 * sizeof(double2), &trm));
@@ -437,8 +442,6 @@ int loop_unity_fp64(int N, int Nt, const double* prop_diag, const double* mom, d
 // ------------------------------------------------------------------ C ABI
 static int chain_args(int engine, int nev, int nt, int tf_begin, int tf_end) {
   if (engine != CTR_ENGINE_FP64 && engine != CTR_ENGINE_SPLIT) return ctr::fail(CTR_ERR_ARG, "unknown engine %d", engine);
-  if (engine == CTR_ENGINE_SPLIT)
-    return ctr::fail(CTR_ERR_UNSUPPORTED, "this diagram family runs on the FP64 engine only");
   if (nev < 1 || nt < 1 || tf_begin < 0 || tf_end > nt || tf_begin >= tf_end)
     return ctr::fail(CTR_ERR_ARG, "bad sizes (nev=%d nt=%d t_sink [%d,%d))", nev, nt, tf_begin, tf_end);
   return CTR_OK;
@@ -455,8 +458,8 @@ int ctr_rhopi(int engine, int nev, int nt, int tf_begin, int tf_end, int idir, c
   if (!aligned(prop_rows) || !aligned(prop_diag) || !aligned(mom_p1) || !aligned(mom_p2) || !aligned(mom5_p1p2) ||
       !aligned(corr))
     return ctr::fail(CTR_ERR_ARG, "ctr_rhopi: null or misaligned pointer");
-  return ctr::rhopi_fp64(nev, nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mom_p1, mom_p2, mom5_p1p2, corr,
-                         (cudaStream_t)stream);
+  return ctr::rhopi_chain(nev, nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mom_p1, mom_p2, mom5_p1p2, corr,
+                         (cudaStream_t)stream, engine);
 }
 
 int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin, const double* prop_rows,
@@ -467,8 +470,8 @@ int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin,
   if (!aligned(prop_rows) || !aligned(prop_diag) || !aligned(p1) || !aligned(p2) || !aligned(p3) || !aligned(p4) ||
       !aligned(corr))
     return ctr::fail(CTR_ERR_ARG, "ctr_pipi: null or misaligned pointer");
-  return ctr::pipi_fp64(nev, nt, tf_begin, tf_end, isospin, prop_rows, prop_diag, p1, p2, p3, p4, corr,
-                        (cudaStream_t)stream);
+  return ctr::pipi_chain(nev, nt, tf_begin, tf_end, isospin, prop_rows, prop_diag, p1, p2, p3, p4, corr,
+                        (cudaStream_t)stream, engine);
 }
 
 int ctr_loop_unity(int engine, int nev, int nt, const double* prop_diag, const double* mom, double* loop,
@@ -485,8 +488,8 @@ int ctr_sigmapi(int engine, int nev, int nt, int tf_begin, int tf_end, const dou
   if (!aligned(prop_diag) || !aligned(mom_p1) || !aligned(mom_p2) || (triangle && (!aligned(prop_rows) ||
       !aligned(mom2_p1p2) || !aligned(triangle))) || (hor_fish && !aligned(hor_fish)))
     return ctr::fail(CTR_ERR_ARG, "ctr_sigmapi: null or misaligned pointer");
-  return ctr::sigmapi_fp64(nev, nt, tf_begin, tf_end, prop_rows, prop_diag, mom_p1, mom_p2, mom2_p1p2, hor_fish,
-                           triangle, (cudaStream_t)stream);
+  return ctr::sigmapi_chain(nev, nt, tf_begin, tf_end, prop_rows, prop_diag, mom_p1, mom_p2, mom2_p1p2, hor_fish,
+                           triangle, (cudaStream_t)stream, engine);
 }
 
 }  // extern "C"

@@ -1,6 +1,7 @@
 // Host orchestration of the split-precision engine: two-sided (rho-type)
 // contractions and batched block products.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -33,6 +34,45 @@ __global__ void ff_to_f64_kernel(const float4* __restrict__ src, int ld, int nev
   const int i = e / nev, j = e % nev;
   const float4 v = src[(size_t)j * ld + i];
   dst[e] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+}
+
+// Error model of a split-engine correlator entry: its rounding error is at
+// most REFINE_EPS * sum_r |coef_r| sum_ij |A_r(i,j)| |B_r(i,j)| (the products'
+// digits reach 2^-45 of the row/column scales; level >= 3 and the float-float
+// recombination add ~2^-47).  Entries whose estimate exceeds rel_tol * |value|
+// -- the few with heavy cancellation between their spin rows or inside their
+// traces -- are recomputed in FP64.
+constexpr double REFINE_EPS = 1.0 / 140737488355328.0;  // 2^-47
+double g_refine_tol = 1e-9;
+long long g_refined_last = 0;
+
+// out[p][o] = sum of the rows of output o; entries whose error estimate
+// exceeds tol * |out| are appended to list (as (pair_base + p) * nout + o).
+__global__ void rowsum_refine_kernel(const double2* __restrict__ rows, const double* __restrict__ rabs, int nrows,
+                                     const int* __restrict__ off, const int* __restrict__ idx, int nout, int npair,
+                                     double2* __restrict__ out, double eps_over_tol, int* __restrict__ count,
+                                     int* __restrict__ list, int pair_base) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= npair * nout) return;
+  const int p = g / nout, o = g % nout;
+  double re = 0.0, im = 0.0, sc = 0.0;
+  for (int k = off[o]; k < off[o + 1]; k++) {
+    const size_t r = (size_t)p * nrows + idx[k];
+    re += rows[r].x;
+    im += rows[r].y;
+    sc += rabs[r];
+  }
+  out[(size_t)p * nout + o] = make_double2(re, im);
+  if (eps_over_tol > 0.0 && sc * eps_over_tol > sqrt(re * re + im * im)) {
+    const int slot = atomicAdd(count, 1);
+    list[slot] = (pair_base + p) * nout + o;
+  }
+}
+
+__global__ void scatter_kernel(const int* __restrict__ where, const double2* __restrict__ vals, int n,
+                               double2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[where[i]] = vals[i];
 }
 
 }  // namespace
@@ -166,6 +206,13 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   csr.insert(csr.end(), ord.begin(), ord.end());
   void* d_csr;
   CTR_TRY(upload(WS_MISC, csr.data(), csr.size() * sizeof(int), &d_csr, stream));
+  // refinement list: one slot per output entry of the call, plus the counter
+  void* d_ref;
+  const size_t nentries = (size_t)npairs_total * nout;
+  CTR_TRY(workspace(WS_REFINE).get((nentries + 1) * sizeof(int), &d_ref));
+  int* d_count = (int*)d_ref;
+  int* d_list = d_count + 1;
+  CTR_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
 
   std::vector<SliceLeftJob> lj;
   std::vector<SliceRightJob> rj;
@@ -173,11 +220,13 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   std::vector<TraceFFTask> tt;
   for (int p0 = 0; p0 < npairs_total; p0 += batch) {
     const int np = std::min(batch, npairs_total - p0);
-    void *mem, *rowbuf;
+    void *mem, *rowbuf, *absbuf;
     CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * per_pair, &mem));
     CTR_TRY(workspace(WS_ROWS).get((size_t)np * nrows * sizeof(double2), &rowbuf));
+    CTR_TRY(workspace(WS_ROWABS).get((size_t)np * nrows * sizeof(double), &absbuf));
     uint8_t* base = (uint8_t*)mem;
     double2* R = (double2*)rowbuf;
+    double* Rabs = (double*)absbuf;
     lj.assign(np, SliceLeftJob{});
     rj.assign(np, SliceRightJob{});
     ga.resize(np);
@@ -217,6 +266,7 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
         t.b = B + (size_t)ib[r] * N * ldB + (size_t)ir[r] * N;
         t.ldb = ldB;
         t.out = R + (size_t)q * nrows + r;
+        t.absout = Rabs + (size_t)q * nrows + r;
         t.coef[0] = coef[2 * r];
         t.coef[1] = coef[2 * r + 1];
       }
@@ -234,9 +284,83 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
     CTR_TRY(upload(WS_ROWTASKS, tt.data(), tt.size() * sizeof(TraceFFTask), &d_tt, stream));
     CTR_TRY(launch_trace_ff((const TraceFFTask*)d_tt, (int)tt.size(), N, stream));
-    CTR_TRY(launch_rowsum(R, nrows, (const int*)d_csr, (const int*)d_csr + (nout + 1), nout, np,
-                          (double2*)out + (size_t)p0 * nout, nout, stream));
+    {
+      TimedLaunch tl(stream, "rowsum_refine");
+      const int n = np * nout;
+      rowsum_refine_kernel<<<cdiv(n, 256), 256, 0, stream>>>(
+          R, Rabs, nrows, (const int*)d_csr, (const int*)d_csr + (nout + 1), nout, np, (double2*)out + (size_t)p0 * nout,
+          g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0, d_count, d_list, p0);
+      CTR_CUDA(cudaGetLastError());
+    }
   }
+  g_refined_last = 0;
+  if (g_refine_tol <= 0.0) return CTR_OK;
+
+  // ---- FP64 recomputation of the flagged entries
+  int nflag = 0;
+  CTR_CUDA(cudaMemcpyAsync(&nflag, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CTR_CUDA(cudaStreamSynchronize(stream));
+  if (nflag == 0) return CTR_OK;
+  std::vector<int> flagged(nflag);
+  CTR_CUDA(cudaMemcpyAsync(flagged.data(), d_list, nflag * sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CTR_CUDA(cudaStreamSynchronize(stream));
+  std::sort(flagged.begin(), flagged.end());
+  std::vector<ctr_factor> fac;
+  std::vector<int> foff(1, 0), chain_row;
+  auto mkf = [](int kind, int dag, int a, int b, int s1, int s2) {
+    ctr_factor x;
+    x.kind = kind;
+    x.dag = dag;
+    x.a = a;
+    x.b = b;
+    x.s1 = s1;
+    x.s2 = s2;
+    return x;
+  };
+  for (int e : flagged) {
+    const int pr = e / nout, o = e % nout, tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
+    for (int k = off[o]; k < off[o + 1]; k++) {
+      const int r = ord[k];
+      const TwoSidedRow& w = rows[r];
+      // coef * Tr[tau_cd Phi_L(ti) (Phi_R(tf) tau_ab)^dagger]
+      fac.push_back(mkf(CTR_FACTOR_TAU, 0, tfl, ti, w.c, w.d));
+      fac.push_back(mkf(CTR_FACTOR_PHI, 0, ti, w.L, 0, 0));
+      fac.push_back(mkf(CTR_FACTOR_TAU, 1, tfl, ti, w.a, w.b));
+      fac.push_back(mkf(CTR_FACTOR_PHI, 1, tf, w.R, 0, 0));
+      foff.push_back((int)fac.size());
+      chain_row.push_back(r);
+    }
+  }
+  void* dv;
+  CTR_TRY(workspace(WS_REFINE).get(chain_row.size() * sizeof(double2), &dv));
+  CTR_TRY(chain_values(N, Nt, nphi, prop_rows, phi, fac, foff, (double*)dv, stream));
+  std::vector<double2> vals(chain_row.size());
+  CTR_CUDA(cudaMemcpyAsync(vals.data(), dv, vals.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+  CTR_CUDA(cudaStreamSynchronize(stream));
+  std::vector<double2> patch(nflag);
+  std::vector<int> where(nflag);
+  size_t c = 0;
+  for (int i = 0; i < nflag; i++) {
+    const int o = flagged[i] % nout;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = off[o]; k < off[o + 1]; k++, c++) {
+      const int r = chain_row[c];
+      const double2 v = cmul(make_double2(coef[2 * r], coef[2 * r + 1]), vals[c]);
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    patch[i] = acc;
+    where[i] = flagged[i];
+  }
+  void *dw, *dp;
+  CTR_TRY(upload(WS_TASKS, where.data(), where.size() * sizeof(int), &dw, stream));
+  CTR_TRY(upload(WS_TASKS2, patch.data(), patch.size() * sizeof(double2), &dp, stream));
+  {
+    TimedLaunch tl(stream, "refine_scatter");
+    scatter_kernel<<<cdiv(nflag, 256), 256, 0, stream>>>((const int*)dw, (const double2*)dp, nflag, (double2*)out);
+    CTR_CUDA(cudaGetLastError());
+  }
+  g_refined_last = nflag;
   return CTR_OK;
 }
 
@@ -326,7 +450,136 @@ int split_levels(int N, const double* x, const double* y, float* levels, cudaStr
 
 }  // namespace ctr
 
+extern "C" int ctr_split_set_refine(double rel_tol) {
+  if (!(rel_tol >= 0.0)) return ctr::fail(CTR_ERR_ARG, "ctr_split_set_refine: rel_tol must be >= 0");
+  ctr::g_refine_tol = rel_tol;
+  return CTR_OK;
+}
+
+extern "C" long long ctr_split_refined(void) { return ctr::g_refined_last; }
+
 extern "C" int ctr_split_levels(int nev, const double* x, const double* y, float* levels, void* stream) {
   if (nev < 1 || !x || !y || !levels) return ctr::fail(CTR_ERR_ARG, "ctr_split_levels: bad arguments");
   return ctr::split_levels(nev, x, y, levels, (cudaStream_t)stream);
 }
+
+namespace ctr {
+
+// Split-engine execution of a stage of FP64-engine GEMM tasks.  Tasks with the
+// same left side (A pointers, transposes, weights) share one sliced left
+// operand and stack up to SPLIT_TASK_NB right sides along N, so each GEMM
+// instance is 128 x (nb N) x (nterm N); instances of equal shape form one
+// persistent launch, whose epilogue writes complex128 blocks in place.
+int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream) {
+  if (ntask == 0) return CTR_OK;
+  if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d (got %d)", SPLIT_MAXK, N);
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  struct LeftKey {
+    const double2* a[4];
+    float w[4];
+    int nterm, dag;
+    bool operator<(const LeftKey& o) const { return std::memcmp(this, &o, sizeof(LeftKey)) < 0; }
+  };
+  std::map<LeftKey, int> gid;
+  std::vector<std::vector<int>> groups;
+  std::vector<LeftKey> gkey;
+  for (int t = 0; t < ntask; t++) {
+    const ZTask& z = tasks[t];
+    if (z.nterm < 1 || z.nterm > 4 || z.nterm * N > 512)
+      return fail(CTR_ERR_ARG, "split task %d: %d terms of Nev %d", t, z.nterm, N);
+    LeftKey k;
+    std::memset(&k, 0, sizeof(k));
+    k.nterm = z.nterm;
+    for (int q = 0; q < z.nterm; q++) {
+      int ex;
+      if (z.wim[q] != 0.f || !(z.wre[q] != 0.f) || std::fabs(std::frexp(z.wre[q], &ex)) != 0.5f)
+        return fail(CTR_ERR_UNSUPPORTED, "split task %d: weight (%g, %g) is not a real power of two", t, z.wre[q],
+                    z.wim[q]);
+      k.a[q] = z.A[q];
+      k.w[q] = z.wre[q];
+      k.dag |= ((z.flags >> q) & 1) << q;
+    }
+    auto it = gid.find(k);
+    if (it == gid.end()) {
+      it = gid.emplace(k, (int)groups.size()).first;
+      groups.emplace_back();
+      gkey.push_back(k);
+    }
+    groups[it->second].push_back(t);
+  }
+  // instances (group, first task, count), bucketed by (nterm, nb)
+  struct Inst {
+    int g, t0, nb;
+  };
+  std::map<std::pair<int, int>, std::vector<Inst>> buckets;
+  for (int g = 0; g < (int)groups.size(); g++)
+    for (int t0 = 0; t0 < (int)groups[g].size(); t0 += SPLIT_TASK_NB) {
+      const int nb = std::min<int>(SPLIT_TASK_NB, (int)groups[g].size() - t0);
+      buckets[{gkey[g].nterm, nb}].push_back(Inst{g, t0, nb});
+    }
+  for (auto& bk : buckets) {
+    const int nterm = bk.first.first, nb = bk.first.second;
+    const int K = nterm * N, nchunk = cdiv(K, SPLIT_K), ntiles = cdiv(nb * N, SPLIT_N);
+    const int eplus = K > 128 ? 1 : 0;
+    const size_t l_b = align256((size_t)nchunk * SPLIT_A_STAGE), r_b = align256((size_t)ntiles * nchunk * SPLIT_B_STAGE);
+    const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)ntiles * SPLIT_N * 4);
+    const size_t per = l_b + r_b + le_b + re_b;
+    const std::vector<Inst>& all = bk.second;
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(all.size(), ((size_t)2 << 30) / per));
+    for (size_t i0 = 0; i0 < all.size(); i0 += batch) {
+      const int ni = (int)std::min<size_t>(batch, all.size() - i0);
+      void* mem;
+      CTR_TRY(workspace(WS_SPLITTASK).get((size_t)ni * per, &mem));
+      std::vector<SliceTaskLJob> lj(ni);
+      std::vector<SliceTaskRJob> rj(ni);
+      std::vector<SplitGemmInst> gi(ni);
+      std::vector<double2*> outs((size_t)ni * SPLIT_TASK_NB, nullptr);
+      for (int i = 0; i < ni; i++) {
+        const Inst& in = all[i0 + i];
+        const LeftKey& k = gkey[in.g];
+        uint8_t* p = (uint8_t*)mem + (size_t)i * per;
+        SliceTaskLJob& L = lj[i];
+        std::memset(&L, 0, sizeof(L));
+        for (int q = 0; q < nterm; q++) {
+          L.a[q] = k.a[q];
+          L.w[q] = k.w[q];
+        }
+        L.nterm = nterm;
+        L.dag = k.dag;
+        L.eplus = eplus;
+        L.out = p;
+        L.exps = (int*)(p + l_b + r_b);
+        SliceTaskRJob& R = rj[i];
+        std::memset(&R, 0, sizeof(R));
+        R.nb = in.nb;
+        R.nterm = nterm;
+        R.eplus = eplus;
+        R.out = p + l_b;
+        R.exps = (int*)(p + l_b + r_b + le_b);
+        for (int j = 0; j < in.nb; j++) {
+          const ZTask& z = tasks[groups[in.g][in.t0 + j]];
+          for (int q = 0; q < nterm; q++) {
+            R.b[j][q] = z.B[q];
+            R.dag |= ((z.flags >> (4 + q)) & 1) << (4 * j + q);
+          }
+          outs[(size_t)i * SPLIT_TASK_NB + j] = z.C;
+        }
+        gi[i] = SplitGemmInst{L.out, R.out, L.exps, R.exps, nullptr, nullptr};
+      }
+      void *d_lj, *d_rj, *d_gi, *d_outs;
+      CTR_TRY(upload(WS_SPLITJOBS, lj.data(), lj.size() * sizeof(SliceTaskLJob), &d_lj, stream));
+      CTR_TRY(upload(WS_SPLITJOBS2, rj.data(), rj.size() * sizeof(SliceTaskRJob), &d_rj, stream));
+      CTR_TRY(upload(WS_SPLITJOBS3, outs.data(), outs.size() * sizeof(double2*), &d_outs, stream));
+      for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d_outs + (size_t)i * SPLIT_TASK_NB;
+      CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
+      CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, ni, N, nchunk, stream));
+      CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, ni, N, nchunk, ntiles, stream));
+      SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N};
+      CTR_TRY(launch_split_gemm(G, ni, d_err, stream));
+    }
+  }
+  return CTR_OK;
+}
+
+}  // namespace ctr

@@ -197,6 +197,127 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
   }
 }
 
+// ------------------------------------------------------ task-form slicers
+__device__ __forceinline__ double2 task_left_elem(const SliceTaskLJob& J, int nev, int r, int k) {
+  const int q = k / nev, j = k - q * nev;
+  if (r >= nev || q >= J.nterm) return make_double2(0.0, 0.0);
+  double2 v;
+  if ((J.dag >> q) & 1) {
+    v = J.a[q][(size_t)j * nev + r];
+    v.y = -v.y;
+  } else {
+    v = J.a[q][(size_t)r * nev + j];
+  }
+  const double w = (double)J.w[q];
+  return make_double2(v.x * w, v.y * w);
+}
+
+__device__ __forceinline__ double2 task_right_elem(const SliceTaskRJob& J, int nev, int k, int n) {
+  const int q = k / nev, i = k - q * nev, jb = n / nev, c = n - jb * nev;
+  if (q >= J.nterm || jb >= J.nb) return make_double2(0.0, 0.0);
+  const double2* B = J.b[jb][q];
+  double2 v;
+  if ((J.dag >> (4 * jb + q)) & 1) {
+    v = B[(size_t)c * nev + i];
+    v.y = -v.y;
+  } else {
+    v = B[(size_t)i * nev + c];
+  }
+  return v;
+}
+
+// Left operand of a task instance (one M tile: rows < nev; K = nterm * nev).
+__global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJob* __restrict__ jobs, int nev,
+                                                              int nchunk) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  int* sexp = (int*)sm;
+  uint8_t* stage = sm + 512;
+  const SliceTaskLJob& J = jobs[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int K = J.nterm * nev;
+  for (int rr = warp; rr < SPLIT_M; rr += 8) {
+    int e = -30000;
+    if (rr < nev)
+      for (int k = lane; k < K; k += 32) {
+        const double2 v = task_left_elem(J, nev, rr, k);
+        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
+      }
+    for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if (lane == 0) {
+      const int E = (e < -1000 ? 0 : e) + J.eplus;
+      sexp[rr] = E;
+      J.exps[rr] = E;
+    }
+  }
+  __syncthreads();
+  for (int kc = 0; kc < nchunk; kc++) {
+    for (int e = threadIdx.x; e < SPLIT_M * SPLIT_K; e += 256) {
+      const int rr = e >> 4, kk = e & 15, k = kc * SPLIT_K + kk;
+      const double2 v = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
+      const int E = sexp[rr];
+      bool nr, ni;
+      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
+      const uint32_t off = core_offset(rr, kk);
+#pragma unroll
+      for (int s = 0; s < SPLIT_NSLICE; s++) {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_A_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_A_SUB + off) = slice_bf16(Ui, s, ni);
+      }
+    }
+    __syncthreads();
+    int4* d = (int4*)(J.out + (size_t)kc * SPLIT_A_STAGE);
+    const int4* src = (const int4*)stage;
+    for (int i = threadIdx.x; i < SPLIT_A_STAGE / 16; i += 256) d[i] = src[i];
+    __syncthreads();
+  }
+}
+
+// Right operand of a task instance: N tile nt of the nb stacked output blocks.
+__global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
+                                                               int nchunk, int ntiles) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  int* sexp = (int*)sm;
+  uint8_t* stage = sm + 512;
+  const SliceTaskRJob& J = jobs[blockIdx.x / ntiles];
+  const int nt = blockIdx.x % ntiles;
+  const int K = J.nterm * nev, ncols = J.nb * nev;
+  if (threadIdx.x < SPLIT_N) {
+    const int n = nt * SPLIT_N + threadIdx.x;
+    int e = -30000;
+    if (n < ncols)
+      for (int k = 0; k < K; k++) {
+        const double2 v = task_right_elem(J, nev, k, n);
+        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
+      }
+    const int E = (e < -1000 ? 0 : e) + J.eplus;
+    sexp[threadIdx.x] = E;
+    J.exps[n] = E;
+  }
+  __syncthreads();
+  uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE;
+  for (int kc = 0; kc < nchunk; kc++) {
+    for (int e = threadIdx.x; e < SPLIT_N * SPLIT_K; e += 256) {
+      const int nn = e % SPLIT_N, kk = e / SPLIT_N;
+      const int n = nt * SPLIT_N + nn, k = kc * SPLIT_K + kk;
+      const double2 v = (n < ncols && k < K) ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
+      const int E = sexp[nn];
+      bool nr, ni;
+      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
+      const uint32_t off = core_offset(nn, kk);
+#pragma unroll
+      for (int s = 0; s < SPLIT_NSLICE; s++) {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_B_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, ni);
+      }
+    }
+    __syncthreads();
+    int4* d = (int4*)(dst_tile + (size_t)kc * SPLIT_B_STAGE);
+    const int4* src = (const int4*)stage;
+    for (int i = threadIdx.x; i < SPLIT_B_STAGE / 16; i += 256) d[i] = src[i];
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ GEMM
 // Persistent kernel: each CTA walks output tiles t = blockIdx.x, +gridDim.x, ...
 // of 128 x SPLIT_N.  Warp 0: TMEM allocation and the bulk-copy producer, which
@@ -217,6 +338,11 @@ constexpr size_t gemm_smem_bytes() {
 __device__ __forceinline__ float pow2f(int e) {
   e = max(-126, min(127, e));
   return __int_as_float((127 + e) << 23);
+}
+
+__device__ __forceinline__ double pow2d(int e) {
+  e = max(-1022, min(1023, e));
+  return __longlong_as_double((long long)(1023 + e) << 52);
 }
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
@@ -401,6 +527,19 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           }
         }
         if (!rvalid || g.levels) continue;
+        if (g.out_mode == 1) {
+          const int erow = I->lexp[grow];
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const int gcol = nt * SPLIT_N + c0 + c;
+            if (gcol >= g.ncols) continue;
+            const double sc = pow2d(erow + sexp[c0 + c]);
+            const int j = gcol / g.blkn, cc = gcol - j * g.blkn;
+            I->outs[j][(size_t)grow * g.blkn + cc] =
+                make_double2(((double)hi[0][c] + (double)lo[0][c]) * sc, ((double)hi[1][c] + (double)lo[1][c]) * sc);
+          }
+          continue;
+        }
 #pragma unroll
         for (int c = 0; c < 16; c++) {
           const int gcol = nt * SPLIT_N + c0 + c;
@@ -426,12 +565,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 // ------------------------------------------------------------- ff traces
 // *out = coef * sum_{i<nev, j<nev} A(i,j) * conj(B(i,j)); A(i,j) = a[j*lda + i],
 // B(i,j) = b[j*ldb + i] (float-float complex).  One CTA of 128 threads per
-// task; thread i walks column elements i (and i+128) over all j.
+// task; thread i walks column elements i (and i+128) over all j.  The same
+// pass accumulates |coef| sum |A||B| (high words, FP32) into *absout.
 __global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __restrict__ tasks, int ntask, int nev) {
   const int t = blockIdx.x;
   if (t >= ntask) return;
   const TraceFFTask T = tasks[t];
-  float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+  float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f, sa = 0.f;
   for (int i = threadIdx.x; i < nev; i += 128) {
     for (int j = 0; j < nev; j++) {
       const float4 a = T.a[(size_t)j * T.lda + i];
@@ -440,24 +580,29 @@ __global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __rest
       ff_mac(sr, er, a.z, a.w, b.z, b.w);   // + ai bi
       ff_mac(si, ei, a.z, a.w, b.x, b.y);   // + ai br
       ff_mac(si, ei, -a.x, -a.y, b.z, b.w); // - ar bi
+      sa = fmaf(sqrtf(fmaf(a.x, a.x, a.z * a.z)), sqrtf(fmaf(b.x, b.x, b.z * b.z)), sa);
     }
   }
-  double re = (double)sr + (double)er, im = (double)si + (double)ei;
-  __shared__ double red[2][4];
+  double re = (double)sr + (double)er, im = (double)si + (double)ei, ab = (double)sa;
+  __shared__ double red[3][4];
   for (int o = 16; o; o >>= 1) {
     re += __shfl_down_sync(0xffffffffu, re, o);
     im += __shfl_down_sync(0xffffffffu, im, o);
+    ab += __shfl_down_sync(0xffffffffu, ab, o);
   }
   if ((threadIdx.x & 31) == 0) {
     red[0][threadIdx.x >> 5] = re;
     red[1][threadIdx.x >> 5] = im;
+    red[2][threadIdx.x >> 5] = ab;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     re = red[0][0] + red[0][1] + red[0][2] + red[0][3];
     im = red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    ab = red[2][0] + red[2][1] + red[2][2] + red[2][3];
     double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
     *T.out = cmul(c, make_double2(re, im));
+    if (T.absout) *T.absout = sqrt(c.x * c.x + c.y * c.y) * ab;
   }
 }
 
@@ -486,6 +631,34 @@ int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchu
   }
   TimedLaunch tl(s, "slice_right");
   slice_right_kernel<<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s) {
+  if (njobs == 0) return CTR_OK;
+  const size_t smem = 512 + SPLIT_A_STAGE;
+  static bool attr = false;
+  if (!attr) {
+    CTR_CUDA(cudaFuncSetAttribute(slice_task_left_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  TimedLaunch tl(s, "slice_task_left");
+  slice_task_left_kernel<<<njobs, 256, smem, s>>>(d_jobs, nev, nchunk);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
+  if (njobs == 0) return CTR_OK;
+  const size_t smem = 512 + SPLIT_B_STAGE;
+  static bool attr = false;
+  if (!attr) {
+    CTR_CUDA(cudaFuncSetAttribute(slice_task_right_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  TimedLaunch tl(s, "slice_task_right");
+  slice_task_right_kernel<<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

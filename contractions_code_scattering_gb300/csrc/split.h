@@ -44,7 +44,8 @@ struct SplitGemmInst {
   const uint8_t* right;  // sliced right operand (all N tiles)
   const int* lexp;       // row exponents
   const int* rexp;       // column exponents
-  float4* out;           // float-float complex, column-major: (r, c) at out[c * ldo + r]
+  float4* out;           // out_mode 0: float-float complex, column-major: (r, c) at out[c * ldo + r]
+  double2* const* outs;  // out_mode 1: complex128 row-major blocks; column c -> outs[c / blkn], (r, c % blkn)
 };
 
 struct SplitGemmBatch {
@@ -53,14 +54,40 @@ struct SplitGemmBatch {
   int mrows, ncols;  // valid rows / columns of every instance
   int ldo;           // column stride of the output (>= mtiles * SPLIT_M)
   float* levels;     // diagnostics only (NULL in production): raw accumulators
-                     // [6][ncols][ldo] of instance 0 instead of the ff output
+                     // [8][ncols][ldo] of instance 0 instead of the ff output
+  int out_mode;      // 0: float-float column-major, 1: complex128 row-major blocks
+  int blkn;          // out_mode 1: columns (and row stride) of one output block
 };
 
-// *out = coef * sum_{i,j<nev} A(i,j) conj(B(i,j)), A(i,j) = a[j*lda+i] (float-float complex)
+// Operands of the task form C = sum_q w_q op(A_q) op(B_q) (q < nterm <= 4),
+// concatenated along K (term q occupies k in [q N, (q+1) N)).  Left: rows of
+// the A side with the weights applied; right: up to SPLIT_TASK_NB output blocks
+// stacked along N.  dag bit q (left) / bit 4j+q (right): conjugate transpose.
+// eplus = 1 halves the leading digit (|d_0| <= 128) so that level 0 stays
+// exact for K <= 512.
+constexpr int SPLIT_TASK_NB = 8;
+struct SliceTaskLJob {
+  const double2* a[4];
+  float w[4];
+  int nterm, dag, eplus, pad;
+  uint8_t* out;  // [nchunk][SPLIT_A_STAGE]
+  int* exps;     // [SPLIT_M]
+};
+struct SliceTaskRJob {
+  const double2* b[SPLIT_TASK_NB][4];
+  int nb, nterm, dag, eplus;
+  uint8_t* out;  // [ntiles][nchunk][SPLIT_B_STAGE]
+  int* exps;     // [ntiles * SPLIT_N]
+};
+
+// *out = coef * sum_{i,j<nev} A(i,j) conj(B(i,j)), A(i,j) = a[j*lda+i] (float-float complex);
+// *absout = |coef| * sum |A(i,j)| |B(i,j)|, the scale the rounding errors of the
+// trace are proportional to (the entry's condition estimate).
 struct TraceFFTask {
   const float4* a;
   const float4* b;
   double2* out;
+  double* absout;
   int lda, ldb;
   float coef[2];
 };
@@ -93,5 +120,7 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
 int launch_trace_ff(const TraceFFTask* d_tasks, int ntask, int nev, cudaStream_t s);
+int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s);
+int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 
 }  // namespace ctr

@@ -86,10 +86,12 @@ int ctr_rho(int engine, int nev, int nt, int tf_begin, int tf_end, const double*
 int ctr_sigma(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
               const double* mom2, double* corr, void* stream);
 
-/* ---------------------------------------------------- chain diagrams (FP64)
+/* ------------------------------------------------------------ chain diagrams
  * prop_diag: tau(t,t) [Nt][4][4][N][N] (the reference's "extra" device buffer,
- * lib/contract.cpp:549-570).  Elementals [Nt][N][N] unless noted.  The split
- * engine returns CTR_ERR_UNSUPPORTED for these families. */
+ * lib/contract.cpp:549-570).  Elementals [Nt][N][N] unless noted.  With
+ * CTR_ENGINE_SPLIT every block product of the chains runs on the tensor-core
+ * split engine (Nev <= 128); the closing traces and the loop-unity traces are
+ * FP64 on both engines. */
 
 /* rho -> pi pi for gamma_idir (run_ContractRhoPi, lib/contract_kernels_rhopi.cu:64-137):
  * mom5_p1p2 [Nt][5][N][N]; corr [tf_end-tf_begin][Nt][4] (one entry per rho operator). */
@@ -147,6 +149,21 @@ int ctr_calculate_sigmapi(int nev, int nt, const void* prop, const double* p1, c
 int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, const double* const* y,
                       double* const* c, void* stream);
 
+/* Multi-term block products, the unit the chain diagrams are built from:
+ * c = sum_{q < nterm} w_q op(a_q) op(b_q), op = conjugate transpose where bit q
+ * (a_q) / bit 4+q (b_q) of flags is set; nev x nev row-major complex128 device
+ * blocks.  With CTR_ENGINE_SPLIT the weights must be real powers of two (the
+ * gamma_5 signs of the tables) and nterm * nev <= 512. */
+typedef struct {
+  const double* a[4];
+  const double* b[4];
+  double* c;
+  float wre[4], wim[4];
+  int nterm;
+  int flags;
+} ctr_ztask;
+int ctr_zgemm_tasks(int engine, int nev, int ntask, const ctr_ztask* tasks /* host */, void* stream);
+
 /* Diagnostics of the split engine: for one product x*y (nev x nev, device),
  * write the raw FP32 tensor-core accumulators before recombination, as
  * levels[8][nev][128] (Re levels 0, 1, 2, >=3, then Im; element (i,j) at
@@ -171,12 +188,70 @@ int ctr_rho_noalloc(int nev, int nt, int tf, const double* prop_row, const doubl
 /* Size in bytes of ctr_rho_noalloc's fixed device scratch array. */
 size_t ctr_rho_noalloc_scratch_bytes(void);
 
+/* ------------------------------------------------ distillation-profile adjoint
+ * The elementals enter the contractions as diag(f) Phi diag(f) for a real
+ * per-eigenvector profile f (no counterpart in the reference, whose
+ * elementals are fixed).  A chain is Tr[F_1 ... F_n], 2 <= n <= CTR_CHAIN_MAXF;
+ * a factor is a perambulator block tau(a, b)_{s1 s2} of the full perambulator
+ * prop [Nt][Nt][4][4][N][N], or a profiled elemental diag(f) phi[a][b] diag(f)
+ * of phi [Nt][nphi][N][N], conjugate-transposed when dag != 0.  All arrays are
+ * device complex128 except the host chain description (chain_off, factors, w).
+ * Gradients are vector-Jacobian products: grad[k] += Re sum_c w_c d value_c / d f_k,
+ * computed by reverse mode with recomputed prefix/suffix products; every f_k must
+ * be nonzero. */
+#define CTR_FACTOR_TAU 0
+#define CTR_FACTOR_PHI 1
+#define CTR_CHAIN_MAXF 12
+typedef struct {
+  int32_t kind; /* CTR_FACTOR_TAU or CTR_FACTOR_PHI */
+  int32_t dag;  /* conjugate transpose */
+  int32_t a, b; /* tau: (t1, t2); phi: (t, op) */
+  int32_t s1, s2; /* tau: spin block */
+} ctr_factor;
+
+/* dst[m] = diag(f) src[m] diag(f) for nmat matrices (device; dst may equal src). */
+int ctr_apply_profile(int nev, long long nmat, const double* f, const double* src, double* dst, void* stream);
+
+/* Generic chains: chain c has factors[chain_off[c] .. chain_off[c+1]) (host arrays), weight
+ * w[c] (host complex, may be NULL when grad is NULL).  values [nchain] complex (device, may be
+ * NULL); grad [N] real (device, accumulated into, may be NULL). */
+int ctr_chain_adjoint(int nev, int nt, int nphi, const double* prop, const double* phi, const double* f, int nchain,
+                      const int* chain_off, const ctr_factor* factors, const double* w, double* values, double* grad,
+                      void* stream);
+
+/* rho-rho (lib/calculate_rho_core.h): w [Nt][Nt][48] complex (device) weights the
+ * correlators corr[tf][ti][o] of ctr_rho; entries with zero weight are skipped.
+ * corr [Nt][Nt][48] (device, may be NULL): the forward correlators of the entries
+ * computed (zero elsewhere); grad [N] (device, may be NULL, accumulated into).
+ * prop: full perambulator; mom5 [Nt][5][N][N]; f [N] device. */
+int ctr_rho_profile_vjp(int nev, int nt, const double* prop, const double* mom5, const double* f, const double* w,
+                        double* corr, double* grad, void* stream);
+
+/* pi pi (lib/contract_kernels_pipi.cu:170-502): w [Nt][Nt][5] complex (device) weights the
+ * isospin-weighted slots (square, double triangle, star, fish, horizontal double triangle)
+ * of ctr_pipi; pairs whose weights are zero are skipped.  corr [Nt][Nt][5] (device, may be
+ * NULL): the forward correlators of the pairs computed (zero elsewhere); grad [N] (device,
+ * may be NULL, accumulated into). */
+int ctr_pipi_profile_vjp(int nev, int nt, int isospin, const double* prop, const double* p1, const double* p2,
+                         const double* p3, const double* p4, const double* f, const double* w, double* corr,
+                         double* grad, void* stream);
+
 /* On-device source-time average of the dumpData routines (lib/contract.cpp:616-643):
  * avg[dt][c] = scale/Nt * sum_ti corr[(ti+dt)%Nt][ti][c]; corr device [Nt][Nt][ncorr]. */
 int ctr_source_average(int nt, int ncorr, const double* corr, double scale, double* avg, void* stream);
 
 /* 1 when the split-precision tensor-core engine is compiled in. */
 int ctr_split_available(void);
+
+/* Per-entry accuracy control of the split engine's two-sided contractions
+ * (rho, sigma, ctr_twosided).  Each correlator entry carries an error estimate
+ * 2^-47 * sum_r |coef_r| sum_ij |A_r(i,j)||B_r(i,j)| (its spin rows' Hadamard
+ * traces in absolute value); entries whose estimate exceeds rel_tol * |entry|
+ * -- those with heavy cancellation -- are recomputed by FP64 chain products
+ * and patched in.  rel_tol = 0 disables the check.  Default 1e-9. */
+int ctr_split_set_refine(double rel_tol);
+/* Number of entries recomputed in FP64 by the last split two-sided call. */
+long long ctr_split_refined(void);
 
 /* Synchronise the stream and report the first device-side error flag. */
 int ctr_sync(void* stream);
