@@ -40,6 +40,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--nt", type=int, default=NT)
     ap.add_argument("--nev", type=int, default=NEV)
+    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint"],
+                    help="rho: the headline rho two-point (Nev=100, Lt=64); rho_small: Nev=32, Lt=16 FP64; "
+                         "pipi: pi pi I=0 diagram set, 19 momentum pairs; mixed: rho-pipi / sigma-pipi / "
+                         "sigma loops at Nev=128, Lt=48, 27 momenta; adjoint: profile objective and gradient")
     return ap.parse_args()
 
 
@@ -244,6 +248,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.workload != "rho":
+        WORKLOADS[args.workload](args)
+        return
     import numpy as np
     import torch
     from contractions_code_scattering_gb300 import _lib, api
@@ -335,6 +342,15 @@ def main():
         cs = torch.cuda.Stream()
         copied = [torch.cuda.Event() for _ in range(2)]
         freed = [torch.cuda.Event() for _ in range(2)]
+        # the copy alone, for reference (untimed by the e2e figure)
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        c0.record(cs)
+        with torch.cuda.stream(cs):
+            buf_tau[1].copy_(h_tau, non_blocking=True)
+        c1.record(cs)
+        torch.cuda.synchronize()
+        h2d_alone = c0.elapsed_time(c1) / 1e3
         torch.cuda.synchronize()
         barrier(ws)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -364,7 +380,8 @@ def main():
         e2e = {"value": ws * diagrams / te, "unit": "diagrams/s",
                "h2d_bytes_per_step": int(h_tau.numel() * 16 + h_phi.numel() * 16),
                "d2h_bytes_per_step": int(out.numel() * 16), "ms_per_step": 1e3 * te,
-               "pipelining": "inputs of step i+1 copied on a second stream while step i computes", "steps": K}
+               "pipelining": "inputs of step i+1 copied on a second stream while step i computes", "steps": K,
+               "h2d_tau_alone_ms": 1e3 * h2d_alone, "h2d_tau_alone_gbs": h_tau.numel() * 16 / h2d_alone / 1e9}
         del h_tau, h_phi, h_out, buf_tau, buf_phi
 
     # CPU baseline (the oracle, reference chain order) on a bounded sample; the
@@ -434,6 +451,246 @@ def roofline(engine, report, steps, nt, nev, nmom):
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
             "fp64_equivalent_tflops": achieved / 15 / 1.12,
             "algorithmic": "15 bf16 slice-pair products x 8*Nev^3 flops (K padded 100->112) per block product"}
+
+
+# ------------------------------------------------------- other workloads
+# The configurations other than the headline: each prints one JSON line with
+# its own metric; the plain FP64 engine is timed on a stated subset where a
+# full FP64 step would take minutes, and the per-entry errors of the split
+# engine are measured against it there.
+def _timed(fn, steps, warmup):
+    import torch
+    from contractions_code_scattering_gb300 import _lib
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    _lib.timing_enable(True)
+    n0 = _lib.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    launches = _lib.launch_count() - n0
+    rep = _lib.timing_report()
+    _lib.timing_enable(False)
+    return e0.elapsed_time(e1) / 1e3 / steps, launches, {k: {"launches": v[0], "ms": v[2]} for k, v in rep.items()}
+
+
+def _errs(a, b):
+    import numpy as np
+    rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+    return {"max": float(rel.max()), "median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
+            "max_over_maxabs": float(np.abs(a - b).max() / np.abs(b).max()), "entries": int(rel.size)}
+
+
+def _neg(p):
+    return tuple(-c for c in p)
+
+
+def run_rho_small(args):
+    """Nev=32, Lt=16 rho two-point at p=0 (gamma_i x Phi at both ends), FP64 engine,
+    against the oracle in full (16 x 16 x 3 = 768 diagrams)."""
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import api, synth
+    from oracle import pyoracle as O
+    api.device_init(0)
+    nt, nev = 16, 32
+    prop = synth.make_prop(nt, nev, seed=SEED, decay=0.35)
+    rng = np.random.default_rng(SEED + 1)
+    mom5 = np.ascontiguousarray(np.stack([synth.make_phi_hermitian(nt, nev, SEED + 2)] +
+                                         [synth.make_phi_random(nt, nev, rng) for _ in range(4)], axis=1))
+    dp, dm = torch.from_numpy(prop).cuda(), torch.from_numpy(mom5).cuda()
+    res = {}
+    for eng in ("fp64", "split"):
+        t, launches, kern = _timed(lambda: api.run_contract_rho(dp, dm, engine=eng), args.steps, args.warmup)
+        got = api.run_contract_rho(dp, dm, engine=eng).cpu().numpy()[:, :, 0, :]
+        res[eng] = {"value": nt * nt * 3 / t, "ms_per_step": 1e3 * t, "gpu_launches": launches}
+        res[eng]["out"] = got
+    t0 = time.perf_counter()
+    ref = O.rho(prop, mom5)[:, :, 0, :]
+    tcpu = time.perf_counter() - t0
+    line = {"workload": "rho_small", "metric": "diagrams/s @Nev=32,Lt=16 (rho, p=0, 3 polarisations)",
+            "unit": "diagrams/s", "diagrams_per_step": nt * nt * 3,
+            "fp64": {k: v for k, v in res["fp64"].items() if k != "out"},
+            "split": {k: v for k, v in res["split"].items() if k != "out"},
+            "fp64_vs_oracle": _errs(res["fp64"]["out"], ref), "split_vs_oracle": _errs(res["split"]["out"], ref),
+            "cpu_baseline": {"value": nt * nt * 768 / 16 / tcpu, "unit": "diagrams/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": "all 16 x 16 pairs, all 48 outputs (768 spin rows)"}}
+    print(json.dumps(line))
+
+
+def run_pipi(args):
+    """pi pi I=0 diagram set (square, double triangle, horizontal double triangle, star,
+    fish) for the 19 momentum pairs (p, -p), |p|^2 <= 2, all 64 x 64 pairs, Nev=100."""
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import _lib, api, synth
+    api.device_init(0)
+    nt, nev = 64, 100
+    moms = synth.momenta(2)
+    idx = {p: k for k, p in enumerate(moms)}
+    tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
+    diag = api.prop_diag(tau)
+    phis = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
+    P = {p: phis[:, idx[p]].contiguous() for p in moms}
+    del phis
+    pairs = [(p, _neg(p)) for p in moms]
+
+    refined = [0]
+
+    def step(engine, rows=None, plist=pairs):
+        tr = rows if rows is not None else (0, nt)
+        tb = tau[tr[0]:tr[1]]
+        out = []
+        refined[0] = 0
+        for a, b in plist:
+            out.append(api.run_contract_pipi(tb, diag, P[a], P[b], P[a], P[b], 0, engine=engine, tf_range=tr))
+            refined[0] += int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
+        return out
+
+    t, launches, kern = _timed(lambda: step("split"), args.steps, args.warmup)
+    refined_step = refined[0]
+    diagrams = nt * nt * len(pairs) * 5
+    sub_pairs, sub_rows = [((1, 0, 0), (-1, 0, 0))], (0, 4)
+    sub_diag = (sub_rows[1] - sub_rows[0]) * nt * len(sub_pairs) * 5
+    t64, _, k64 = _timed(lambda: step("fp64", sub_rows, sub_pairs), 1, 1)
+    ts, _, _ = _timed(lambda: step("split", sub_rows, sub_pairs), 1, 1)
+    a = step("split", sub_rows, sub_pairs)[0].cpu().numpy()
+    b = step("fp64", sub_rows, sub_pairs)[0].cpu().numpy()
+    line = {"workload": "pipi", "metric": "diagrams/s @Nev=100,Lt=64: pi pi I=0 set, 19 momentum pairs, split-TC",
+            "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t, "steps": args.steps,
+            "warmup": args.warmup, "diagrams_per_step": diagrams, "gpu_launches": launches, "kernels": kern,
+            "split_refined_entries_per_step": refined_step,
+            "fp64_subset": {"sample": "momentum pair (1,0,0)/(-1,0,0), t_sink 0..3, all t_src (%d diagrams)" % sub_diag,
+                            "fp64_diagrams_per_s": sub_diag / t64, "split_diagrams_per_s": sub_diag / ts,
+                            "split_speedup": t64 / ts, "split_vs_fp64_rel_err": _errs(a, b), "fp64_kernels": k64}}
+    print(json.dumps(line))
+
+
+def run_mixed(args):
+    """Mixed cross-correlator batch at Nev=128, Lt=48, decay 0.25: for each of the 27
+    momenta |p|^2 <= 3, rho -> pi pi (3 polarisations x 4 operators) and sigma -> pi pi
+    (triangle x 2 operators, horizontal fish) with the pion pair (p, -p), plus the
+    sigma one-fish loops; split engine."""
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import _lib, api, synth
+    api.device_init(0)
+    nt, nev = 48, 128
+    moms = synth.momenta(3)
+    idx = {p: k for k, p in enumerate(moms)}
+    tau = synth.make_prop(nt, nev, seed=SEED, decay=0.25, backend="torch")
+    diag = api.prop_diag(tau)
+    phis = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
+    P = {p: phis[:, idx[p]].contiguous() for p in moms}
+    del phis
+    g = torch.Generator(device="cuda")
+    g.manual_seed(SEED + 2)
+    sd = float(np.sqrt(0.5 / nev))
+    ops = torch.complex(torch.randn((nt, 5, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd,
+                        torch.randn((nt, 5, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd)
+    mom5 = ops.contiguous()
+    mom2 = ops[:, :2].contiguous()
+
+    refined = [0]
+
+    def count():
+        refined[0] += int(_lib.lib().ctr_split_refined())
+
+    def step(engine, plist=moms, rows=None):
+        tr = rows if rows is not None else (0, nt)
+        tb = tau[tr[0]:tr[1]]
+        out = []
+        refined[0] = 0
+        for p in plist:
+            for idir in range(3):
+                out.append(api.run_contract_rhopi(tb, diag, P[p], P[_neg(p)], mom5, idir, engine=engine, tf_range=tr))
+                count()
+            hf, tri = api.run_contract_sigmapi(tb, diag, P[p], P[_neg(p)], mom2, engine=engine, tf_range=tr)
+            count()
+            out += [tri, hf]
+        for k in range(2):
+            out.append(api.run_contract_loop_unity(diag, mom2[:, k].contiguous(), engine=engine))
+        return out
+
+    t, launches, kern = _timed(lambda: step("split"), args.steps, args.warmup)
+    refined_step = refined[0]
+    diagrams = nt * nt * len(moms) * (12 + 2) + nt * len(moms) + 2 * nt
+    sub = [(1, 1, 1)]
+    rows = (0, 4)
+    t64, _, _ = _timed(lambda: step("fp64", sub, rows), 1, 1)
+    ts, _, _ = _timed(lambda: step("split", sub, rows), 1, 1)
+    a = np.concatenate([x.cpu().numpy().ravel() for x in step("split", sub, rows)])
+    b = np.concatenate([x.cpu().numpy().ravel() for x in step("fp64", sub, rows)])
+    sub_diag = (rows[1] - rows[0]) * nt * 14 + nt + 2 * nt
+    line = {"workload": "mixed", "metric": "diagrams/s @Nev=128,Lt=48: rho-pipi + sigma-pipi + sigma loops, "
+            "27 momenta, split-TC", "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t,
+            "steps": args.steps, "warmup": args.warmup, "diagrams_per_step": diagrams, "gpu_launches": launches,
+            "kernels": kern, "split_refined_entries_per_step": refined_step,
+            "fp64_subset": {"sample": "momentum (1,1,1), t_sink 0..3, all t_src (%d diagrams)" % sub_diag,
+                            "fp64_diagrams_per_s": sub_diag / t64, "split_diagrams_per_s": sub_diag / ts,
+                            "split_speedup": t64 / ts, "split_vs_fp64_rel_err": _errs(a, b)}}
+    print(json.dumps(line))
+
+
+def run_adjoint(args):
+    """Distillation-profile objective and its gradient at Nev=100, Lt=64: rho (p=0) for
+    t = 2..9 and the pi pi I=0 set at dt = 4, f_k = exp(-lambda_k/0.3); forward plus
+    backward per evaluation, and FP64 central differences (h = 1e-6) on a few f_k."""
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import adjoint, api, synth
+    api.device_init(0)
+    nt, nev = 64, 100
+    tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
+    moms = [(0, 0, 0), (1, 0, 0), (-1, 0, 0)]
+    phis = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(SEED + 2)
+    sd = float(np.sqrt(0.5 / nev))
+    extra = torch.complex(torch.randn((nt, 4, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd,
+                          torch.randn((nt, 4, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd)
+    mom5 = torch.cat([phis[:, :1], extra], dim=1).contiguous()
+    p, m = phis[:, 1].contiguous(), phis[:, 2].contiguous()
+    pipi = (p, m, p, m)
+    f0 = adjoint.default_profile(nev)
+    kw = dict(rho_ts=(2, 8), pipi_dt=4, isospin=0, engine=args.engine if args.engine != "auto" else "split")
+
+    def evaluate():
+        f = torch.tensor(f0, device="cuda", requires_grad=True)
+        L = adjoint.objective(f, tau, mom5, pipi, **kw)
+        L.backward()
+        return L.item(), f.grad
+
+    t, launches, kern = _timed(evaluate, args.steps, args.warmup)
+    L, grad = evaluate()
+    grad = grad.cpu().numpy()
+    kw64 = dict(kw, engine="fp64")  # the differences are taken on the FP64 forward
+    h = 1e-6
+    fd = {}
+    for k in (0, 37, 99):
+        fp, fm = f0.copy(), f0.copy()
+        fp[k] += h
+        fm[k] -= h
+        with torch.no_grad():
+            lp = adjoint.objective(torch.tensor(fp, device="cuda"), tau, mom5, pipi, **kw64).item()
+            lm = adjoint.objective(torch.tensor(fm, device="cuda"), tau, mom5, pipi, **kw64).item()
+        fd[k] = (lp - lm) / (2 * h)
+    worst = max(abs(fd[k] - grad[k]) for k in fd) / np.abs(grad).max()
+    line = {"workload": "adjoint", "metric": "profile objective + gradient evaluations/s @Nev=100,Lt=64",
+            "value": 1.0 / t, "unit": "evaluations/s", "ms_per_evaluation": 1e3 * t, "steps": args.steps,
+            "engine": kw["engine"],
+            "warmup": args.warmup, "objective": L, "grad_norm": float(np.linalg.norm(grad)),
+            "fd_check": {"h": h, "forward": "fp64 engine", "components": {str(k): [fd[k], float(grad[k])] for k in fd},
+                         "max_abs_diff_over_max_grad": worst},
+            "gpu_launches": launches, "kernels": kern}
+    print(json.dumps(line))
+
+
+WORKLOADS = {"rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint}
 
 
 if __name__ == "__main__":

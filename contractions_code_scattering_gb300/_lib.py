@@ -64,9 +64,9 @@ def lib(build_if_missing=True):
     L.ctr_split_set_refine.argtypes = [d]
     L.ctr_split_refined.restype = ctypes.c_longlong
     L.ctr_apply_profile.argtypes = [i, ctypes.c_longlong, vp, vp, vp, vp]
-    L.ctr_chain_adjoint.argtypes = [i, i, i, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]
-    L.ctr_rho_profile_vjp.argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp]
-    L.ctr_pipi_profile_vjp.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.ctr_chain_adjoint.argtypes = [i, i, i, i, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]
+    L.ctr_rho_profile_vjp.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp, vp]
+    L.ctr_pipi_profile_vjp.argtypes = [i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     _LIB = L
     return L
 

@@ -275,7 +275,7 @@ def apply_profile(f, phi, out=None, stream=None):
     return out
 
 
-def chain_adjoint(prop, phi, f, chains, weights=None, values=True, grad=True, stream=None):
+def chain_adjoint(prop, phi, f, chains, weights=None, values=True, grad=True, engine="fp64", stream=None):
     """Generic chain traces and their profile gradient (include/ctr.h: ctr_chain_adjoint).
 
     chains: list of lists of (kind, dag, a, b, s1, s2); weights: complex per chain.
@@ -294,7 +294,7 @@ def chain_adjoint(prop, phi, f, chains, weights=None, values=True, grad=True, st
         w = np.ascontiguousarray(np.asarray(weights, np.complex128))
     vals = torch.zeros(len(chains), dtype=torch.complex128, device=prop.device) if values else None
     g = torch.zeros(nev, dtype=torch.float64, device=prop.device) if grad else None
-    check(lib().ctr_chain_adjoint(nev, nt, nphi, _dev(prop, "prop"), _dev(phi, "phi") if phi is not None else None,
+    check(lib().ctr_chain_adjoint(_engine(engine), nev, nt, nphi, _dev(prop, "prop"), _dev(phi, "phi") if phi is not None else None,
                                   _real(f, "f"), len(chains), _np_ptr(off), ctypes.cast(fac, ctypes.c_void_p),
                                   _np_ptr(w) if w is not None else None,
                                   _dev(vals, "values") if vals is not None else None,
@@ -302,20 +302,20 @@ def chain_adjoint(prop, phi, f, chains, weights=None, values=True, grad=True, st
     return vals, g
 
 
-def rho_profile_vjp(prop, mom5, f, w, corr=True, grad=True, stream=None):
+def rho_profile_vjp(prop, mom5, f, w, corr=True, grad=True, engine="fp64", stream=None):
     """rho-rho with profiled elementals: forward correlators [Nt, Nt, 48] of the entries
     with nonzero weight w [Nt, Nt, 48] (complex, device) and grad [N] = Re sum w dcorr/df."""
     import torch
     nt, nev = prop.shape[0], prop.shape[-1]
     c = torch.zeros((nt, nt, 48), dtype=torch.complex128, device=prop.device) if corr else None
     g = torch.zeros(nev, dtype=torch.float64, device=prop.device) if grad else None
-    check(lib().ctr_rho_profile_vjp(nev, nt, _dev(prop, "prop"), _dev(mom5, "mom5"), _real(f, "f"),
+    check(lib().ctr_rho_profile_vjp(_engine(engine), nev, nt, _dev(prop, "prop"), _dev(mom5, "mom5"), _real(f, "f"),
                                     _dev(w.contiguous(), "w"), _dev(c, "corr") if c is not None else None,
                                     _real(g, "grad") if g is not None else None, _stream(stream)))
     return c, g
 
 
-def pipi_profile_vjp(prop, p1, p2, p3, p4, f, w, isospin, corr=True, grad=True, stream=None):
+def pipi_profile_vjp(prop, p1, p2, p3, p4, f, w, isospin, corr=True, grad=True, engine="fp64", stream=None):
     """pi pi with profiled elementals: forward correlators [Nt, Nt, 5] (isospin-weighted
     square, double triangle, star, fish, horizontal double triangle) of the pairs with
     nonzero weight w [Nt, Nt, 5] and grad [N] = Re sum w dcorr/df."""
@@ -323,7 +323,7 @@ def pipi_profile_vjp(prop, p1, p2, p3, p4, f, w, isospin, corr=True, grad=True, 
     nt, nev = prop.shape[0], prop.shape[-1]
     c = torch.zeros((nt, nt, 5), dtype=torch.complex128, device=prop.device) if corr else None
     g = torch.zeros(nev, dtype=torch.float64, device=prop.device) if grad else None
-    check(lib().ctr_pipi_profile_vjp(nev, nt, isospin, _dev(prop, "prop"), _dev(p1, "p1"), _dev(p2, "p2"),
+    check(lib().ctr_pipi_profile_vjp(_engine(engine), nev, nt, isospin, _dev(prop, "prop"), _dev(p1, "p1"), _dev(p2, "p2"),
                                      _dev(p3, "p3"), _dev(p4, "p4"), _real(f, "f"), _dev(w.contiguous(), "w"),
                                      _dev(c, "corr") if c is not None else None,
                                      _real(g, "grad") if g is not None else None, _stream(stream)))

@@ -154,8 +154,8 @@ struct Opnd {
 
 class ChainProgram {
  public:
-  ChainProgram(int N, int Nt, int nphi, const double2* prop, const double2* phis)
-      : N_(N), Nt_(Nt), nphi_(nphi), prop_(prop), phis_(phis) {}
+  ChainProgram(int N, int Nt, int nphi, const double2* prop, const double2* phis, int engine)
+      : N_(N), Nt_(Nt), nphi_(nphi), engine_(engine), prop_(prop), phis_(phis) {}
 
   int check_factor(const ctr_factor& F) const {
     if (F.kind == CTR_FACTOR_TAU) {
@@ -256,7 +256,7 @@ class ChainProgram {
     return id;
   }
 
-  int N_, Nt_, nphi_;
+  int N_, Nt_, nphi_, engine_;
   const double2* prop_;
   const double2* phis_;
   std::vector<Node> nodes_;
@@ -295,7 +295,12 @@ int ChainProgram::run(const double* f, double2* values, double* grad, cudaStream
     }
   }
   level_off[maxd + 1] = tasks.size();
-  if (!tasks.empty()) {
+  if (!tasks.empty() && engine_ == CTR_ENGINE_SPLIT) {
+    for (int d = 2; d <= maxd; d++) {
+      const size_t n0 = level_off[d], n1 = level_off[d + 1];
+      if (n1 > n0) CTR_TRY(zgemm_split_tasks(N_, tasks.data() + n0, (int)(n1 - n0), s));
+    }
+  } else if (!tasks.empty()) {
     void* dt;
     CTR_TRY(upload(WS_GEMM_A, tasks.data(), tasks.size() * sizeof(ZTask), &dt, s));
     for (int d = 2; d <= maxd; d++) {
@@ -357,8 +362,8 @@ int ChainProgram::run(const double* f, double2* values, double* grad, cudaStream
 class ChainRunner {
  public:
   ChainRunner(int N, int Nt, int nphi, const double2* prop, const double2* phis, const double* f, double2* values,
-              double* grad, cudaStream_t s)
-      : prog_(N, Nt, nphi, prop, phis), f_(f), values_(values), grad_(grad), s_(s) {
+              double* grad, cudaStream_t s, int engine = CTR_ENGINE_FP64)
+      : prog_(N, Nt, nphi, prop, phis, engine), f_(f), values_(values), grad_(grad), s_(s) {
     const size_t budget = (size_t)3 << 30;
     max_nodes_ = std::max<size_t>(64, budget / ((size_t)N * N * sizeof(double2)));
   }
@@ -431,6 +436,11 @@ inline ctr_factor phi(int t, int op, int dag = 0) {
 
 inline double2 cw(double2 w, double re, double im) { return make_double2(w.x * re - w.y * im, w.x * im + w.y * re); }
 
+int check_engine(int engine, int nev) {
+  if (engine != CTR_ENGINE_FP64 && engine != CTR_ENGINE_SPLIT) return fail(CTR_ERR_ARG, "unknown engine %d", engine);
+  return CTR_OK;
+}
+
 }  // namespace
 
 int chain_values(int N, int Nt, int nphi, const double* prop, const double* phi, const std::vector<ctr_factor>& factors,
@@ -462,10 +472,11 @@ int ctr_apply_profile(int nev, long long nmat, const double* f, const double* sr
   return CTR_OK;
 }
 
-int ctr_chain_adjoint(int nev, int nt, int nphi, const double* prop, const double* phi, const double* f, int nchain,
-                      const int* chain_off, const ctr_factor* factors, const double* w, double* values, double* grad,
-                      void* stream) {
+int ctr_chain_adjoint(int engine, int nev, int nt, int nphi, const double* prop, const double* phi, const double* f,
+                      int nchain, const int* chain_off, const ctr_factor* factors, const double* w, double* values,
+                      double* grad, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  CTR_TRY(check_engine(engine, nev));
   if (nev < 1 || nt < 1 || nphi < 0 || nchain < 0 || !prop || !f || !chain_off || !factors || (!values && !grad))
     return fail(CTR_ERR_ARG, "ctr_chain_adjoint: bad arguments");
   if (grad && !w) return fail(CTR_ERR_ARG, "ctr_chain_adjoint: weights are needed for the gradient");
@@ -473,7 +484,7 @@ int ctr_chain_adjoint(int nev, int nt, int nphi, const double* prop, const doubl
   CTR_TRY(check_f(nev, f, s));
   double2* phis = nullptr;
   if (nphi > 0) CTR_TRY(profiled(nev, (long long)nt * nphi, phi, f, WS_PHI, &phis, s));
-  ChainRunner R(nev, nt, nphi, (const double2*)prop, phis, f, (double2*)values, grad, s);
+  ChainRunner R(nev, nt, nphi, (const double2*)prop, phis, f, (double2*)values, grad, s, engine);
   for (int c = 0; c < nchain; c++) {
     const int n = chain_off[c + 1] - chain_off[c];
     if (n < 2 || n > CTR_CHAIN_MAXF) return fail(CTR_ERR_ARG, "chain %d has %d factors (2..%d)", c, n, CTR_CHAIN_MAXF);
@@ -485,9 +496,10 @@ int ctr_chain_adjoint(int nev, int nt, int nphi, const double* prop, const doubl
   return R.flush();
 }
 
-int ctr_rho_profile_vjp(int nev, int nt, const double* prop, const double* mom5, const double* f, const double* w,
-                        double* corr, double* grad, void* stream) {
+int ctr_rho_profile_vjp(int engine, int nev, int nt, const double* prop, const double* mom5, const double* f,
+                        const double* w, double* corr, double* grad, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  CTR_TRY(check_engine(engine, nev));
   if (nev < 1 || nt < 1 || !prop || !mom5 || !f || !w || (!corr && !grad))
     return fail(CTR_ERR_ARG, "ctr_rho_profile_vjp: bad arguments");
   CTR_TRY(check_f(nev, f, s));
@@ -509,7 +521,7 @@ int ctr_rho_profile_vjp(int nev, int nt, const double* prop, const double* mom5,
     CTR_TRY(workspace(WS_TASKS2).get(nval * sizeof(double2), &dvals));
     CTR_CUDA(cudaMemsetAsync(dvals, 0, nval * sizeof(double2), s));
   }
-  ChainRunner R(nev, nt, 5, (const double2*)prop, phis, f, (double2*)dvals, grad, s);
+  ChainRunner R(nev, nt, 5, (const double2*)prop, phis, f, (double2*)dvals, grad, s, engine);
   // lib/calculate_rho_core.h: coef * Tr[tau_{s3s4} Phi_lp(ti) (Phi_rp(tf) tau_{s1s2})^dagger]
   for (size_t q = 0; q < pairs.size(); q++) {
     const int tf = pairs[q] / nt, ti = pairs[q] % nt;
@@ -550,10 +562,11 @@ int ctr_rho_profile_vjp(int nev, int nt, const double* prop, const double* mom5,
   return CTR_OK;
 }
 
-int ctr_pipi_profile_vjp(int nev, int nt, int isospin, const double* prop, const double* p1, const double* p2,
-                         const double* p3, const double* p4, const double* f, const double* w, double* corr,
-                         double* grad, void* stream) {
+int ctr_pipi_profile_vjp(int engine, int nev, int nt, int isospin, const double* prop, const double* p1,
+                         const double* p2, const double* p3, const double* p4, const double* f, const double* w,
+                         double* corr, double* grad, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  CTR_TRY(check_engine(engine, nev));
   if (nev < 1 || nt < 1 || !prop || !p1 || !p2 || !p3 || !p4 || !f || !w || (!corr && !grad))
     return fail(CTR_ERR_ARG, "ctr_pipi_profile_vjp: bad arguments");
   if (isospin != 0 && isospin != 1) return fail(CTR_ERR_ARG, "isospin must be 0 (I=0) or 1 (I=1)");
@@ -598,7 +611,7 @@ int ctr_pipi_profile_vjp(int nev, int nt, int isospin, const double* prop, const
   {
     void* dv;
     CTR_TRY(workspace(WS_TASKS2).get(std::max<size_t>(1, sfv.size()) * sizeof(double2), &dv));
-    ChainRunner R(nev, nt, 4, (const double2*)prop, phis, f, (double2*)dv, nullptr, s);
+    ChainRunner R(nev, nt, 4, (const double2*)prop, phis, f, (double2*)dv, nullptr, s, engine);
     for (size_t q = 0; q < pairs.size(); q++) {
       const int tf = pairs[q] / nt, ti = pairs[q] % nt;
       for (int k = 0; k < 4; k++)
@@ -622,7 +635,7 @@ int ctr_pipi_profile_vjp(int nev, int nt, int isospin, const double* prop, const
     CTR_CUDA(cudaMemsetAsync(dvals, 0, std::max<size_t>(1, pairs.size() * 768) * sizeof(double2), s));
   }
   const bool g = grad != nullptr;
-  ChainRunner R(nev, nt, 4, (const double2*)prop, phis, f, (double2*)dvals, grad, s);
+  ChainRunner R(nev, nt, 4, (const double2*)prop, phis, f, (double2*)dvals, grad, s, engine);
   for (size_t q = 0; q < pairs.size(); q++) {
     const int tf = pairs[q] / nt, ti = pairs[q] % nt;
     const double* wp = &hw[(size_t)pairs[q] * 10];

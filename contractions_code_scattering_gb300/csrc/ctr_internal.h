@@ -97,6 +97,11 @@ enum {
 // Perambulator file payload (complex128, file order) -> host buffer in the library layout.
 int reorder_prop_device(int N, int Nt, const double* file_payload, int single, void* host_out);
 
+// Per-entry accuracy control of the split engine (ctr_split_set_refine): relative
+// tolerance (0 = off) and the number of entries the last split call recomputed.
+extern double g_refine_tol;
+extern long long g_refined_last;
+
 // Reads (and clears) the device-side error flag of the split engine; syncs the stream.
 int split_error_check(cudaStream_t s);
 int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,

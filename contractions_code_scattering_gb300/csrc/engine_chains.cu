@@ -73,13 +73,13 @@ inline TraceTask tr(const double2* X, const double2* Y, double2* out, float cre,
   return t;
 }
 
-// R(t)_{ab} = Pa(t) taud(t)_{ab} Pb(t) for all t and the 16 spin blocks
-// -> out[t][16][N][N]; tmp holds the same amount.
+// R(t)_{ab} = Pa(t) taud(t)_{ab} Pb(t) for all t (or the t with tmask[t] set)
+// and the 16 spin blocks -> out[t][16][N][N]; tmp holds the same amount.
 int per_t_chain(const Ctx& c, const double2* diag, const double2* Pa, size_t pa_t, const double2* Pb, size_t pb_t,
-                double2* tmp, double2* out) {
+                double2* tmp, double2* out, const std::vector<char>* tmask = nullptr) {
   std::vector<ZTask> s1, s2;
   for (int t = 0; t < c.Nt; t++)
-    for (int b = 0; b < 16; b++) {
+    for (int b = 0; b < 16 && (!tmask || (*tmask)[t]); b++) {
       const size_t o = ((size_t)t * 16 + b) * c.N2;
       s1.push_back(zt(Pa + t * pa_t, diag + o, tmp + o));
       s2.push_back(zt(tmp + o, Pb + t * pb_t, out + o));
@@ -106,20 +106,24 @@ void block_gemm_g5(const Ctx& c, const double2* M1, const double2* M2, double2* 
 }
 
 __global__ void pipi_combine_kernel(const double2* __restrict__ tr, int ntr, int npair, int iso,
-                                    double2* __restrict__ out) {
+                                    double2* __restrict__ out, const double* __restrict__ trabs, double eps_over_tol,
+                                    int* __restrict__ count, int* __restrict__ list, int pair_base) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
   const double2* t = tr + (size_t)p * ntr;
   // layout per pair: [0,16) square, [16,32) dtri, [32,48) dtri_hor,
   // [48,64) Tr[U4 W1], [64,80) Tr[U3 W2], [80,96) Tr[U3 W1], [96,112) Tr[U4 W2]
   double2 sum[7];
+  double ab[7];
   for (int g = 0; g < 7; g++) {
-    double re = 0, im = 0;
+    double re = 0, im = 0, a = 0;
     for (int k = 0; k < 16; k++) {
       re += t[g * 16 + k].x;
       im += t[g * 16 + k].y;
+      if (trabs) a += trabs[(size_t)p * ntr + g * 16 + k];
     }
     sum[g] = make_double2(re, im);
+    ab[g] = a;
   }
   const double2 star = cmul(sum[3], sum[4]);
   const double2 fish = cmul(sum[5], sum[6]);
@@ -137,6 +141,75 @@ __global__ void pipi_combine_kernel(const double2* __restrict__ tr, int ntr, int
     o[3] = fish;
     o[4] = make_double2(-(5. / 3.) * sum[2].x, -(5. / 3.) * sum[2].y);
   }
+  if (trabs && eps_over_tol > 0.0) {
+    auto mag = [](double2 v) { return sqrt(v.x * v.x + v.y * v.y); };
+    const double w[3] = {iso == 1 ? 2.0 : 1.0 / 3.0, iso == 1 ? 2.0 : 1.0 / 3.0, iso == 1 ? 0.0 : 5.0 / 3.0};
+    const double scale[5] = {w[0] * ab[0], w[1] * ab[1], mag(sum[3]) * ab[4] + mag(sum[4]) * ab[3],
+                             mag(sum[5]) * ab[6] + mag(sum[6]) * ab[5], w[2] * ab[2]};
+    for (int k = 0; k < 5; k++)
+      if (scale[k] * eps_over_tol > mag(o[k])) {
+        list[atomicAdd(count, 1)] = (pair_base + p) * 5 + k;
+        break;
+      }
+  }
+}
+
+// ---- per-entry refinement of split-engine chains
+// A chain entry's rounding error is estimated as REFINE_EPS_CHAIN times the sum
+// of |coef| sum |Y|_1 |T|_1 over its closing traces (for products of traces,
+// the product rule of those scales): each of the up to four tensor-core
+// products of a chain keeps ~2^-45 of its row/column scales, and the errors of
+// the N^2 terms of a trace add with random signs.  Pairs (or time slices)
+// with an entry above g_refine_tol * |entry| are recomputed by the FP64 engine.
+constexpr double REFINE_EPS_CHAIN = 1.0 / 70368744177664.0;  // 2^-46
+
+struct Refine {
+  bool on = false;
+  double eps_over_tol = 0.0;
+  int* count = nullptr;
+  int* list = nullptr;
+};
+
+int refine_begin(const Ctx& c, size_t nentries, int slot, Refine& r) {
+  r.on = c.engine == CTR_ENGINE_SPLIT && g_refine_tol > 0.0;
+  if (!r.on) return CTR_OK;
+  r.eps_over_tol = REFINE_EPS_CHAIN / g_refine_tol;
+  void* p;
+  CTR_TRY(workspace(slot).get((nentries + 1) * sizeof(int), &p));
+  r.count = (int*)p;
+  r.list = r.count + 1;
+  CTR_CUDA(cudaMemsetAsync(r.count, 0, sizeof(int), c.s));
+  return CTR_OK;
+}
+
+// Flagged entries e -> units e / nout (pairs or time slices); rerun(units, out)
+// writes their FP64 values as [units][nout] into out (device); they are then
+// scattered over corr.  Returns the number of entries recomputed.
+template <typename Rerun>
+int refine_end(const Ctx& c, const Refine& r, int nout, int slot, double2* corr, long long* nref, Rerun&& rerun) {
+  if (!r.on) return CTR_OK;
+  int n = 0;
+  CTR_CUDA(cudaMemcpyAsync(&n, r.count, sizeof(int), cudaMemcpyDeviceToHost, c.s));
+  CTR_CUDA(cudaStreamSynchronize(c.s));
+  if (n == 0) return CTR_OK;
+  std::vector<int> list(n);
+  CTR_CUDA(cudaMemcpyAsync(list.data(), r.list, n * sizeof(int), cudaMemcpyDeviceToHost, c.s));
+  CTR_CUDA(cudaStreamSynchronize(c.s));
+  std::vector<int> units;
+  for (int e : list) units.push_back(e / nout);
+  std::sort(units.begin(), units.end());
+  units.erase(std::unique(units.begin(), units.end()), units.end());
+  void* tmp;
+  CTR_TRY(workspace(slot).get(units.size() * nout * sizeof(double2), &tmp));
+  CTR_TRY(rerun(units, (double2*)tmp));
+  std::vector<int> where(units.size() * nout);
+  for (size_t q = 0; q < units.size(); q++)
+    for (int o = 0; o < nout; o++) where[q * nout + o] = units[q] * nout + o;
+  void* dw;
+  CTR_TRY(upload(WS_TASKS, where.data(), where.size() * sizeof(int), &dw, c.s));
+  CTR_TRY(launch_scatter((const int*)dw, (const double2*)tmp, (int)where.size(), corr, c.s));
+  *nref += (long long)where.size();
+  return CTR_OK;
 }
 
 int batch_pairs(size_t per_pair, int npairs) {
@@ -149,37 +222,47 @@ int batch_pairs(size_t per_pair, int npairs) {
 // ------------------------------------------------------------------ pi pi
 int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* prop_rows, const double* prop_diag,
               const double* p1, const double* p2, const double* p3, const double* p4, double* corr, cudaStream_t s,
-              int engine) {
+              int engine, const std::vector<int>* plist) {
   Ctx c{N, Nt, (size_t)N * N, s, engine};
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)p1, *P2 = (const double2*)p2, *P3 = (const double2*)p3,
                 *P4 = (const double2*)p4;
-  // per time slice: L = P3 taud P4, Rsq = P2 taud P1, Rdt = P1 taud P2
+  const int npairs = plist ? (int)plist->size() : (tf_end - tf_begin) * Nt;
+  auto pair_of = [&](int i) { return plist ? (*plist)[i] : i; };
+  // per time slice: L = P3 taud P4 (sink times), Rsq = P2 taud P1, Rdt = P1 taud P2 (source times)
+  std::vector<char> need_tf(Nt, plist ? 0 : 1), need_ti(Nt, plist ? 0 : 1);
+  for (int i = 0; plist && i < npairs; i++) {
+    need_tf[tf_begin + pair_of(i) / Nt] = 1;
+    need_ti[pair_of(i) % Nt] = 1;
+  }
   void* pt;
   CTR_TRY(workspace(WS_PHI).get(4 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *L = (double2*)pt, *Rsq = L + Nt * blk16, *Rdt = Rsq + Nt * blk16, *tmp = Rdt + Nt * blk16;
-  CTR_TRY(per_t_chain(c, diag, P3, N2, P4, N2, tmp, L));
-  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, Rsq));
-  CTR_TRY(per_t_chain(c, diag, P1, N2, P2, N2, tmp, Rdt));
+  CTR_TRY(per_t_chain(c, diag, P3, N2, P4, N2, tmp, L, &need_tf));
+  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, Rsq, &need_ti));
+  CTR_TRY(per_t_chain(c, diag, P1, N2, P2, N2, tmp, Rdt, &need_ti));
 
   // per pair: X, Ysq, Ydt, V1, Pm, V2, Qm, F, G (16 blocks each), U3, U4, W1, W2
   const int nbuf = 13;
   const int ntr = 112;
   const size_t per_pair = (size_t)nbuf * blk16 * sizeof(double2) + ntr * sizeof(double2);
-  const int npairs = (tf_end - tf_begin) * Nt;
   const int batch = batch_pairs(per_pair, npairs);
+  Refine rf;
+  CTR_TRY(refine_begin(c, (size_t)npairs * 5, WS_REFINE, rf));
   for (int p0 = 0; p0 < npairs; p0 += batch) {
     const int np = std::min(batch, npairs - p0);
-    void *mem, *trm;
+    void *mem, *trm, *tra = nullptr;
     CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * nbuf * blk16 * sizeof(double2), &mem));
     CTR_TRY(workspace(WS_ROWS).get((size_t)np * ntr * sizeof(double2), &trm));
+    if (rf.on) CTR_TRY(workspace(WS_ROWABS).get((size_t)np * ntr * sizeof(double), &tra));
     double2* B = (double2*)mem;
     double2* TR = (double2*)trm;
+    double* TRA = (double*)tra;
     std::vector<ZTask> st1, st2, st3;
     std::vector<TraceTask> tt;
     for (int q = 0; q < np; q++) {
-      const int pr = p0 + q, tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
+      const int pr = pair_of(p0 + q), tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
       const double2* T = tau + ((size_t)tfl * Nt + ti) * blk16;
       double2* b0 = B + (size_t)q * nbuf * blk16;
       double2 *X = b0, *Ysq = b0 + blk16, *Ydt = b0 + 2 * blk16, *V1 = b0 + 3 * blk16, *Pm = b0 + 4 * blk16,
@@ -239,16 +322,25 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
         tt.push_back(tr(U4 + b * N2, W2 + b * N2, o + 96 + b, 1.f, 0.f, 1));
       }
     }
+    if (TRA)
+      for (size_t k = 0; k < tt.size(); k++) tt[k].absout = TRA + (tt[k].out - TR);
     CTR_TRY(run_stage(c, st1, WS_TASKS));
     CTR_TRY(run_stage(c, st2, WS_TASKS2));
     CTR_TRY(run_stage(c, st3, WS_GEMM_A));
     CTR_TRY(run_traces(c, tt));
     {
       TimedLaunch tl(s, "pipi_combine");
-      pipi_combine_kernel<<<(np + 127) / 128, 128, 0, s>>>(TR, ntr, np, iso, (double2*)corr + (size_t)p0 * 5);
+      pipi_combine_kernel<<<(np + 127) / 128, 128, 0, s>>>(TR, ntr, np, iso, (double2*)corr + (size_t)p0 * 5, TRA,
+                                                           rf.eps_over_tol, rf.count, rf.list, p0);
       CTR_CUDA(cudaGetLastError());
     }
   }
+  long long nref = 0;
+  CTR_TRY(refine_end(c, rf, 5, WS_REFINE, (double2*)corr, &nref, [&](const std::vector<int>& pairs, double2* out) {
+    return pipi_chain(N, Nt, tf_begin, tf_end, iso, prop_rows, prop_diag, p1, p2, p3, p4, (double*)out, s,
+                      CTR_ENGINE_FP64, &pairs);
+  }));
+  if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
   return CTR_OK;
 }
 
@@ -257,16 +349,21 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
 // Phi_P2(ti) taud(ti)_{s1s2} Phi_P1(ti) tau_{s3s2}^dag] with s6 = s1, s4 = s3;
 // coef = c(iop, s3, s5) * g5(s1), so the sum over s1 is (T G R)_{s5 s2}.
 int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double* prop_rows, const double* prop_diag,
-               const double* mp1, const double* mp2, const double* mom5, double* corr, cudaStream_t s, int engine) {
+                const double* mp1, const double* mp2, const double* mom5, double* corr, cudaStream_t s, int engine,
+                const std::vector<int>* plist) {
   if (idir < 0 || idir > 2) return fail(CTR_ERR_ARG, "idir %d not in {0,1,2}", idir);
   Ctx c{N, Nt, (size_t)N * N, s, engine};
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)mp1, *P2 = (const double2*)mp2, *P12 = (const double2*)mom5;
+  const int npairs = plist ? (int)plist->size() : (tf_end - tf_begin) * Nt;
+  auto pair_of = [&](int i) { return plist ? (*plist)[i] : i; };
+  std::vector<char> need_ti(Nt, plist ? 0 : 1);
+  for (int i = 0; plist && i < npairs; i++) need_ti[pair_of(i) % Nt] = 1;
   void* pt;
   CTR_TRY(workspace(WS_PHI).get(2 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *R = (double2*)pt, *tmp = R + Nt * blk16;
-  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R));  // R = Phi_P2 taud Phi_P1
+  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need_ti));  // R = Phi_P2 taud Phi_P1
 
   // groups (iop, s2, s3): s5 from the table, c = coef * g5(s1); the 4 rows s1=0..3 share a group
   const Tables& Tb = tables();
@@ -289,9 +386,10 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
   const int nprod = (int)pkeys.size(), ngrp = (int)grp.size();
   const int nbuf = 1 + (nprod + 15) / 16;
   const size_t per_pair = (size_t)(16 + nprod) * N2 * sizeof(double2) + ngrp * sizeof(double2);
-  const int npairs = (tf_end - tf_begin) * Nt;
   const int batch = batch_pairs(per_pair, npairs);
   (void)nbuf;
+  Refine rf;
+  CTR_TRY(refine_begin(c, (size_t)npairs * 4, WS_REFINE, rf));
   std::vector<int> off(5, 0), idx(ngrp);
   for (int g = 0; g < ngrp; g++) off[grp[g].iop + 1]++;
   for (int o = 0; o < 4; o++) off[o + 1] += off[o];
@@ -305,15 +403,17 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
   CTR_TRY(upload(WS_MISC, csr.data(), csr.size() * sizeof(int), &d_csr, s));
   for (int p0 = 0; p0 < npairs; p0 += batch) {
     const int np = std::min(batch, npairs - p0);
-    void *mem, *trm;
+    void *mem, *trm, *tra = nullptr;
     CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * (16 + nprod) * N2 * sizeof(double2), &mem));
     CTR_TRY(workspace(WS_ROWS).get((size_t)np * ngrp * sizeof(double2), &trm));
+    if (rf.on) CTR_TRY(workspace(WS_ROWABS).get((size_t)np * ngrp * sizeof(double), &tra));
     double2* Bm = (double2*)mem;
     double2* TR = (double2*)trm;
+    double* TRA = (double*)tra;
     std::vector<ZTask> st1, st2;
     std::vector<TraceTask> tt;
     for (int q = 0; q < np; q++) {
-      const int pr = p0 + q, tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
+      const int pr = pair_of(p0 + q), tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
       const double2* T = tau + ((size_t)tfl * Nt + ti) * blk16;
       double2* X = Bm + (size_t)q * (16 + nprod) * N2;
       double2* Y = X + blk16;
@@ -329,12 +429,24 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
                         grp[g].cim, 0));
       }
     }
+    if (TRA)
+      for (size_t k = 0; k < tt.size(); k++) tt[k].absout = TRA + (tt[k].out - TR);
     CTR_TRY(run_stage(c, st1, WS_TASKS));
     CTR_TRY(run_stage(c, st2, WS_TASKS2));
     CTR_TRY(run_traces(c, tt));
-    CTR_TRY(launch_rowsum(TR, ngrp, (const int*)d_csr, (const int*)d_csr + 5, 4, np, (double2*)corr + (size_t)p0 * 4,
-                          4, s));
+    if (rf.on)
+      CTR_TRY(launch_rowsum_refine(TR, TRA, ngrp, (const int*)d_csr, (const int*)d_csr + 5, 4, np,
+                                   (double2*)corr + (size_t)p0 * 4, rf.eps_over_tol, rf.count, rf.list, p0, s));
+    else
+      CTR_TRY(launch_rowsum(TR, ngrp, (const int*)d_csr, (const int*)d_csr + 5, 4, np,
+                            (double2*)corr + (size_t)p0 * 4, 4, s));
   }
+  long long nref = 0;
+  CTR_TRY(refine_end(c, rf, 4, WS_REFINE, (double2*)corr, &nref, [&](const std::vector<int>& pairs, double2* out) {
+    return rhopi_chain(N, Nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mp1, mp2, mom5, (double*)out, s,
+                       CTR_ENGINE_FP64, &pairs);
+  }));
+  if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
   return CTR_OK;
 }
 
@@ -344,39 +456,68 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
 // Triangle (lib/calculate_sigmapi_triangle_core.h): rows with s2 = s1, s4 = s3,
 // coef = g5(s1) g5(s3): sum_s3 g5(s3) tau_{s1s3} R_{s3s5} = (T G R)_{s1 s5}.
 int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* prop_diag,
-                 const double* mp1, const double* mp2, const double* mom2, double* hor_fish, double* tri,
-                 cudaStream_t s, int engine) {
+                  const double* mp1, const double* mp2, const double* mom2, double* hor_fish, double* tri,
+                  cudaStream_t s, int engine, const std::vector<int>* plist, const std::vector<int>* tlist) {
   Ctx c{N, Nt, (size_t)N * N, s, engine};
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)mp1, *P2 = (const double2*)mp2, *Px2 = (const double2*)mom2;
   const Tables& Tb = tables();
+  const int npairs = tri ? (plist ? (int)plist->size() : (tf_end - tf_begin) * Nt) : 0;
+  const int nts = hor_fish ? (tlist ? (int)tlist->size() : Nt) : 0;
+  auto pair_of = [&](int i) { return plist ? (*plist)[i] : i; };
+  auto t_of = [&](int i) { return tlist ? (*tlist)[i] : i; };
+  std::vector<char> need(Nt, 0);
+  for (int i = 0; i < nts; i++) need[t_of(i)] = 1;
+  for (int i = 0; i < npairs; i++) need[pair_of(i) % Nt] = 1;
   void* pt;
   CTR_TRY(workspace(WS_PHI).get(2 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *R = (double2*)pt, *tmp = R + Nt * blk16;
-  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R));
+  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need));
+  long long nref = 0;
   if (hor_fish) {
-    void* trm;
-    CTR_TRY(workspace(WS_ROWS).get((size_t)Nt * 16 * sizeof(double2), &trm));
+    // lib/calculate_sigmapi_hor_fish_core.h: sum_ab coef * sum R_ab (.) conj taud_ab, per time slice
+    Refine rf;
+    CTR_TRY(refine_begin(c, (size_t)nts, WS_REFINE, rf));
+    void *trm, *tra = nullptr;
+    CTR_TRY(workspace(WS_ROWS).get((size_t)nts * 16 * sizeof(double2), &trm));
+    if (rf.on) CTR_TRY(workspace(WS_ROWABS).get((size_t)nts * 16 * sizeof(double), &tra));
     std::vector<TraceTask> tt;
-    for (int t = 0; t < Nt; t++)
+    for (int i = 0; i < nts; i++) {
+      const int t = t_of(i);
       for (int b = 0; b < 16; b++) {
         const int ab = Tb.hf_spin[b][0] * 4 + Tb.hf_spin[b][1];
-        tt.push_back(tr(R + t * blk16 + ab * N2, diag + t * blk16 + ab * N2, (double2*)trm + t * 16 + b,
+        tt.push_back(tr(R + t * blk16 + ab * N2, diag + t * blk16 + ab * N2, (double2*)trm + i * 16 + b,
                         Tb.hf_coef[b][0], Tb.hf_coef[b][1], 0));
+        if (tra) tt.back().absout = (double*)tra + i * 16 + b;
       }
-    std::vector<int> csr(Nt + 1 + Nt * 16);
-    for (int t = 0; t <= Nt; t++) csr[t] = 16 * t;
-    for (int k = 0; k < Nt * 16; k++) csr[Nt + 1 + k] = k;
+    }
+    // one "pair" of nts outputs, 16 rows each
+    std::vector<int> csr(nts + 1 + nts * 16);
+    for (int i = 0; i <= nts; i++) csr[i] = 16 * i;
+    for (int k = 0; k < nts * 16; k++) csr[nts + 1 + k] = k;
     void* d_csr;
     CTR_TRY(upload(WS_MISC, csr.data(), csr.size() * sizeof(int), &d_csr, s));
     CTR_TRY(run_traces(c, tt));
-    CTR_TRY(launch_rowsum((double2*)trm, Nt * 16, (const int*)d_csr, (const int*)d_csr + Nt + 1, Nt, 1,
-                          (double2*)hor_fish, Nt, s));
+    if (rf.on)
+      CTR_TRY(launch_rowsum_refine((double2*)trm, (double*)tra, nts * 16, (const int*)d_csr, (const int*)d_csr + nts + 1,
+                                   nts, 1, (double2*)hor_fish, rf.eps_over_tol, rf.count, rf.list, 0, s));
+    else
+      CTR_TRY(launch_rowsum((double2*)trm, nts * 16, (const int*)d_csr, (const int*)d_csr + nts + 1, nts, 1,
+                            (double2*)hor_fish, nts, s));
+    CTR_TRY(refine_end(c, rf, 1, WS_REFINE, (double2*)hor_fish, &nref, [&](const std::vector<int>& ts, double2* out) {
+      return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2, (double*)out, nullptr, s,
+                           CTR_ENGINE_FP64, nullptr, &ts);
+    }));
+    // an FP64 recomputation above rebuilt R for its time slices in place
+    if (tri && nref > 0) CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need));
   }
-  if (!tri) return CTR_OK;
-  // triangle: X = T G R, Y_{ik, s1 s5} = Phix2_ik(tf) X_{s1 s5}, trace vs tau_{s1 s5}, weight g5(s1)
-  const int npairs = (tf_end - tf_begin) * Nt;
+  if (!tri) {
+    if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
+    return CTR_OK;
+  }
+  // triangle (lib/calculate_sigmapi_triangle_core.h): X = T G R, Y_{ik, s1 s5} = Phix2_ik(tf) X_{s1 s5},
+  // trace vs tau_{s1 s5}, weight g5(s1)
   const size_t per_pair = (size_t)(16 + 32) * N2 * sizeof(double2) + 32 * sizeof(double2);
   const int batch = batch_pairs(per_pair, npairs);
   std::vector<int> csr(3 + 32);
@@ -384,17 +525,21 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
   for (int k = 0; k < 32; k++) csr[3 + k] = k;
   void* d_csr;
   CTR_TRY(upload(WS_MISC, csr.data(), csr.size() * sizeof(int), &d_csr, s));
+  Refine rf;
+  CTR_TRY(refine_begin(c, (size_t)npairs * 2, WS_REFINE, rf));
   for (int p0 = 0; p0 < npairs; p0 += batch) {
     const int np = std::min(batch, npairs - p0);
-    void *mem, *trm;
+    void *mem, *trm, *tra = nullptr;
     CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * 48 * N2 * sizeof(double2), &mem));
     CTR_TRY(workspace(WS_ROWS).get((size_t)np * 32 * sizeof(double2), &trm));
+    if (rf.on) CTR_TRY(workspace(WS_ROWABS).get((size_t)np * 32 * sizeof(double), &tra));
     double2* Bm = (double2*)mem;
     double2* TR = (double2*)trm;
+    double* TRA = (double*)tra;
     std::vector<ZTask> st1, st2;
     std::vector<TraceTask> tt;
     for (int q = 0; q < np; q++) {
-      const int pr = p0 + q, tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
+      const int pr = pair_of(p0 + q), tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
       const double2* T = tau + ((size_t)tfl * Nt + ti) * blk16;
       double2* X = Bm + (size_t)q * 48 * N2;
       double2* Y = X + blk16;
@@ -404,14 +549,24 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
           st2.push_back(zt(Px2 + ((size_t)tf * 2 + ik) * N2, X + b * N2, Y + (ik * 16 + b) * N2));
           tt.push_back(tr(Y + (ik * 16 + b) * N2, T + b * N2, TR + (size_t)q * 32 + ik * 16 + b,
                           (float)G5[b / 4], 0.f, 0));
+          if (TRA) tt.back().absout = TRA + (size_t)q * 32 + ik * 16 + b;
         }
     }
     CTR_TRY(run_stage(c, st1, WS_TASKS));
     CTR_TRY(run_stage(c, st2, WS_TASKS2));
     CTR_TRY(run_traces(c, tt));
-    CTR_TRY(launch_rowsum(TR, 32, (const int*)d_csr, (const int*)d_csr + 3, 2, np, (double2*)tri + (size_t)p0 * 2, 2,
-                          s));
+    if (rf.on)
+      CTR_TRY(launch_rowsum_refine(TR, TRA, 32, (const int*)d_csr, (const int*)d_csr + 3, 2, np,
+                                   (double2*)tri + (size_t)p0 * 2, rf.eps_over_tol, rf.count, rf.list, p0, s));
+    else
+      CTR_TRY(launch_rowsum(TR, 32, (const int*)d_csr, (const int*)d_csr + 3, 2, np, (double2*)tri + (size_t)p0 * 2,
+                            2, s));
   }
+  CTR_TRY(refine_end(c, rf, 2, WS_REFINE, (double2*)tri, &nref, [&](const std::vector<int>& pairs, double2* out) {
+    return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2, nullptr, (double*)out, s,
+                         CTR_ENGINE_FP64, &pairs, nullptr);
+  }));
+  if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
   return CTR_OK;
 }
 
@@ -459,7 +614,7 @@ int ctr_rhopi(int engine, int nev, int nt, int tf_begin, int tf_end, int idir, c
       !aligned(corr))
     return ctr::fail(CTR_ERR_ARG, "ctr_rhopi: null or misaligned pointer");
   return ctr::rhopi_chain(nev, nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mom_p1, mom_p2, mom5_p1p2, corr,
-                         (cudaStream_t)stream, engine);
+                          (cudaStream_t)stream, engine, nullptr);
 }
 
 int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin, const double* prop_rows,
@@ -471,7 +626,7 @@ int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin,
       !aligned(corr))
     return ctr::fail(CTR_ERR_ARG, "ctr_pipi: null or misaligned pointer");
   return ctr::pipi_chain(nev, nt, tf_begin, tf_end, isospin, prop_rows, prop_diag, p1, p2, p3, p4, corr,
-                        (cudaStream_t)stream, engine);
+                         (cudaStream_t)stream, engine, nullptr);
 }
 
 int ctr_loop_unity(int engine, int nev, int nt, const double* prop_diag, const double* mom, double* loop,
@@ -489,7 +644,7 @@ int ctr_sigmapi(int engine, int nev, int nt, int tf_begin, int tf_end, const dou
       !aligned(mom2_p1p2) || !aligned(triangle))) || (hor_fish && !aligned(hor_fish)))
     return ctr::fail(CTR_ERR_ARG, "ctr_sigmapi: null or misaligned pointer");
   return ctr::sigmapi_chain(nev, nt, tf_begin, tf_end, prop_rows, prop_diag, mom_p1, mom_p2, mom2_p1p2, hor_fish,
-                           triangle, (cudaStream_t)stream, engine);
+                            triangle, (cudaStream_t)stream, engine, nullptr, nullptr);
 }
 
 }  // extern "C"

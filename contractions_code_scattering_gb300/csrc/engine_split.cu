@@ -43,37 +43,6 @@ __global__ void ff_to_f64_kernel(const float4* __restrict__ src, int ld, int nev
 // -- the few with heavy cancellation between their spin rows or inside their
 // traces -- are recomputed in FP64.
 constexpr double REFINE_EPS = 1.0 / 140737488355328.0;  // 2^-47
-double g_refine_tol = 1e-9;
-long long g_refined_last = 0;
-
-// out[p][o] = sum of the rows of output o; entries whose error estimate
-// exceeds tol * |out| are appended to list (as (pair_base + p) * nout + o).
-__global__ void rowsum_refine_kernel(const double2* __restrict__ rows, const double* __restrict__ rabs, int nrows,
-                                     const int* __restrict__ off, const int* __restrict__ idx, int nout, int npair,
-                                     double2* __restrict__ out, double eps_over_tol, int* __restrict__ count,
-                                     int* __restrict__ list, int pair_base) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= npair * nout) return;
-  const int p = g / nout, o = g % nout;
-  double re = 0.0, im = 0.0, sc = 0.0;
-  for (int k = off[o]; k < off[o + 1]; k++) {
-    const size_t r = (size_t)p * nrows + idx[k];
-    re += rows[r].x;
-    im += rows[r].y;
-    sc += rabs[r];
-  }
-  out[(size_t)p * nout + o] = make_double2(re, im);
-  if (eps_over_tol > 0.0 && sc * eps_over_tol > sqrt(re * re + im * im)) {
-    const int slot = atomicAdd(count, 1);
-    list[slot] = (pair_base + p) * nout + o;
-  }
-}
-
-__global__ void scatter_kernel(const int* __restrict__ where, const double2* __restrict__ vals, int n,
-                               double2* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[where[i]] = vals[i];
-}
 
 }  // namespace
 
@@ -284,14 +253,9 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
     CTR_TRY(upload(WS_ROWTASKS, tt.data(), tt.size() * sizeof(TraceFFTask), &d_tt, stream));
     CTR_TRY(launch_trace_ff((const TraceFFTask*)d_tt, (int)tt.size(), N, stream));
-    {
-      TimedLaunch tl(stream, "rowsum_refine");
-      const int n = np * nout;
-      rowsum_refine_kernel<<<cdiv(n, 256), 256, 0, stream>>>(
-          R, Rabs, nrows, (const int*)d_csr, (const int*)d_csr + (nout + 1), nout, np, (double2*)out + (size_t)p0 * nout,
-          g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0, d_count, d_list, p0);
-      CTR_CUDA(cudaGetLastError());
-    }
+    CTR_TRY(launch_rowsum_refine(R, Rabs, nrows, (const int*)d_csr, (const int*)d_csr + (nout + 1), nout, np,
+                                 (double2*)out + (size_t)p0 * nout, g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0,
+                                 d_count, d_list, p0, stream));
   }
   g_refined_last = 0;
   if (g_refine_tol <= 0.0) return CTR_OK;
@@ -355,11 +319,7 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   void *dw, *dp;
   CTR_TRY(upload(WS_TASKS, where.data(), where.size() * sizeof(int), &dw, stream));
   CTR_TRY(upload(WS_TASKS2, patch.data(), patch.size() * sizeof(double2), &dp, stream));
-  {
-    TimedLaunch tl(stream, "refine_scatter");
-    scatter_kernel<<<cdiv(nflag, 256), 256, 0, stream>>>((const int*)dw, (const double2*)dp, nflag, (double2*)out);
-    CTR_CUDA(cudaGetLastError());
-  }
+  CTR_TRY(launch_scatter((const int*)dw, (const double2*)dp, nflag, (double2*)out, stream));
   g_refined_last = nflag;
   return CTR_OK;
 }
@@ -458,6 +418,11 @@ extern "C" int ctr_split_set_refine(double rel_tol) {
 
 extern "C" long long ctr_split_refined(void) { return ctr::g_refined_last; }
 
+namespace ctr {
+double g_refine_tol = 1e-9;
+long long g_refined_last = 0;
+}  // namespace ctr
+
 extern "C" int ctr_split_levels(int nev, const double* x, const double* y, float* levels, void* stream) {
   if (nev < 1 || !x || !y || !levels) return ctr::fail(CTR_ERR_ARG, "ctr_split_levels: bad arguments");
   return ctr::split_levels(nev, x, y, levels, (cudaStream_t)stream);
@@ -524,21 +489,24 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
     const int eplus = K > 128 ? 1 : 0;
     const size_t l_b = align256((size_t)nchunk * SPLIT_A_STAGE), r_b = align256((size_t)ntiles * nchunk * SPLIT_B_STAGE);
     const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)ntiles * SPLIT_N * 4);
-    const size_t per = l_b + r_b + le_b + re_b;
+    const size_t per = l_b + r_b + le_b + re_b;  // one left and at most one distinct right per instance
     const std::vector<Inst>& all = bk.second;
     const int batch = (int)std::max<size_t>(1, std::min<size_t>(all.size(), ((size_t)2 << 30) / per));
     for (size_t i0 = 0; i0 < all.size(); i0 += batch) {
       const int ni = (int)std::min<size_t>(batch, all.size() - i0);
       void* mem;
       CTR_TRY(workspace(WS_SPLITTASK).get((size_t)ni * per, &mem));
+      uint8_t* lbase = (uint8_t*)mem;                       // ni x (left slices + row exponents)
+      uint8_t* rbase = lbase + (size_t)ni * (l_b + le_b);   // <= ni x (right slices + column exponents)
       std::vector<SliceTaskLJob> lj(ni);
-      std::vector<SliceTaskRJob> rj(ni);
+      std::vector<SliceTaskRJob> rj;
+      std::map<std::vector<uintptr_t>, int> rid;  // identical right sides are sliced once
       std::vector<SplitGemmInst> gi(ni);
       std::vector<double2*> outs((size_t)ni * SPLIT_TASK_NB, nullptr);
       for (int i = 0; i < ni; i++) {
         const Inst& in = all[i0 + i];
         const LeftKey& k = gkey[in.g];
-        uint8_t* p = (uint8_t*)mem + (size_t)i * per;
+        uint8_t* p = lbase + (size_t)i * (l_b + le_b);
         SliceTaskLJob& L = lj[i];
         std::memset(&L, 0, sizeof(L));
         for (int q = 0; q < nterm; q++) {
@@ -549,23 +517,33 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
         L.dag = k.dag;
         L.eplus = eplus;
         L.out = p;
-        L.exps = (int*)(p + l_b + r_b);
-        SliceTaskRJob& R = rj[i];
+        L.exps = (int*)(p + l_b);
+        SliceTaskRJob R;
         std::memset(&R, 0, sizeof(R));
         R.nb = in.nb;
         R.nterm = nterm;
         R.eplus = eplus;
-        R.out = p + l_b;
-        R.exps = (int*)(p + l_b + r_b + le_b);
+        std::vector<uintptr_t> key;
         for (int j = 0; j < in.nb; j++) {
           const ZTask& z = tasks[groups[in.g][in.t0 + j]];
           for (int q = 0; q < nterm; q++) {
             R.b[j][q] = z.B[q];
             R.dag |= ((z.flags >> (4 + q)) & 1) << (4 * j + q);
+            key.push_back((uintptr_t)z.B[q]);
           }
           outs[(size_t)i * SPLIT_TASK_NB + j] = z.C;
         }
-        gi[i] = SplitGemmInst{L.out, R.out, L.exps, R.exps, nullptr, nullptr};
+        key.push_back((uintptr_t)R.dag);
+        auto it = rid.find(key);
+        if (it == rid.end()) {
+          uint8_t* q = rbase + rj.size() * (r_b + re_b);
+          R.out = q;
+          R.exps = (int*)(q + r_b);
+          it = rid.emplace(key, (int)rj.size()).first;
+          rj.push_back(R);
+        }
+        const SliceTaskRJob& Ru = rj[it->second];
+        gi[i] = SplitGemmInst{L.out, Ru.out, L.exps, Ru.exps, nullptr, nullptr};
       }
       void *d_lj, *d_rj, *d_gi, *d_outs;
       CTR_TRY(upload(WS_SPLITJOBS, lj.data(), lj.size() * sizeof(SliceTaskLJob), &d_lj, stream));
@@ -574,7 +552,7 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
       for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d_outs + (size_t)i * SPLIT_TASK_NB;
       CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
       CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, ni, N, nchunk, stream));
-      CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, ni, N, nchunk, ntiles, stream));
+      CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, (int)rj.size(), N, nchunk, ntiles, stream));
       SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N};
       CTR_TRY(launch_split_gemm(G, ni, d_err, stream));
     }

@@ -19,10 +19,14 @@ struct ZTask {
 
 // One Hadamard trace: *out = coef * sum X (.) conj(Y)   (mode 0)
 //                      *out = coef * Tr[X Y]            (mode 1)
+// and, if absout is set, *absout = |coef| * sum |X_ij|_1 |Y_ij|_1 (mode 0) or
+// |coef| * sum |X_ij|_1 |Y_ji|_1 (mode 1), |z|_1 = |Re z| + |Im z| (within a factor
+// 2 of the product of moduli): the scale of the trace's rounding errors.
 struct TraceTask {
   const double2* X;
   const double2* Y;
   double2* out;
+  double* absout;
   float coef[2];
   int mode;
   int pad;
@@ -55,5 +59,12 @@ int launch_trace_f64(const TraceTask* d_tasks, int ntask, int N, cudaStream_t s)
 int launch_rowsum(const double2* rows, int nrows, const int* off, const int* idx, int nout, int npair,
                   double2* out, size_t out_pair_stride, cudaStream_t s);
 int launch_source_average(int Nt, int ncorr, const double2* corr, double scale, double2* avg, cudaStream_t s);
+// Row sums as launch_rowsum (out stride nout) plus per-entry refinement flags:
+// entries with eps_over_tol * sum(rabs) > |out| append (pair_base + p) * nout + o to list.
+int launch_rowsum_refine(const double2* rows, const double* rabs, int nrows, const int* off, const int* idx, int nout,
+                         int npair, double2* out, double eps_over_tol, int* count, int* list, int pair_base,
+                         cudaStream_t s);
+// Scatter: out[where[i]] = vals[i].
+int launch_scatter(const int* where, const double2* vals, int n, double2* out, cudaStream_t s);
 
 }  // namespace ctr

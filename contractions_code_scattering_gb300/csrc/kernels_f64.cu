@@ -102,12 +102,14 @@ __global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restr
   if (t >= ntask) return;
   const TraceTask& T = tasks[t];
   const int n2 = N * N;
-  double re = 0.0, im = 0.0;
+  const bool want_abs = T.absout != nullptr;
+  double re = 0.0, im = 0.0, ab = 0.0;
   if (T.mode == 0) {
     for (int e = threadIdx.x; e < n2; e += 256) {
       double2 x = T.X[e], y = T.Y[e];
       re += x.x * y.x + x.y * y.y;
       im += x.y * y.x - x.x * y.y;
+      if (want_abs) ab += (fabs(x.x) + fabs(x.y)) * (fabs(y.x) + fabs(y.y));
     }
   } else {
     for (int e = threadIdx.x; e < n2; e += 256) {
@@ -115,14 +117,17 @@ __global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restr
       double2 x = T.X[e], y = T.Y[(size_t)j * N + i];
       re += x.x * y.x - x.y * y.y;
       im += x.x * y.y + x.y * y.x;
+      if (want_abs) ab += (fabs(x.x) + fabs(x.y)) * (fabs(y.x) + fabs(y.y));
     }
   }
   re = block_sum_256(re);
   im = block_sum_256(im);
+  if (want_abs) ab = block_sum_256(ab);
   if (threadIdx.x == 0) {
     double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
     double2 s = make_double2(re, im);
     *T.out = cmul(c, s);
+    if (want_abs) *T.absout = sqrt(c.x * c.x + c.y * c.y) * ab;
   }
 }
 
@@ -141,6 +146,33 @@ __global__ void rowsum_kernel(const double2* __restrict__ rows, int nrows, const
     im += v.y;
   }
   out[(size_t)p * out_pair_stride + o] = make_double2(re, im);
+}
+
+__global__ void rowsum_refine_kernel(const double2* __restrict__ rows, const double* __restrict__ rabs, int nrows,
+                                     const int* __restrict__ off, const int* __restrict__ idx, int nout, int npair,
+                                     double2* __restrict__ out, double eps_over_tol, int* __restrict__ count,
+                                     int* __restrict__ list, int pair_base) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= npair * nout) return;
+  const int p = g / nout, o = g % nout;
+  double re = 0.0, im = 0.0, sc = 0.0;
+  for (int k = off[o]; k < off[o + 1]; k++) {
+    const size_t r = (size_t)p * nrows + idx[k];
+    re += rows[r].x;
+    im += rows[r].y;
+    sc += rabs[r];
+  }
+  out[(size_t)p * nout + o] = make_double2(re, im);
+  if (eps_over_tol > 0.0 && sc * eps_over_tol > sqrt(re * re + im * im)) {
+    const int slot = atomicAdd(count, 1);
+    list[slot] = (pair_base + p) * nout + o;
+  }
+}
+
+__global__ void scatter_kernel(const int* __restrict__ where, const double2* __restrict__ vals, int n,
+                               double2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[where[i]] = vals[i];
 }
 
 // -------------------------------------------------------- source average
@@ -194,6 +226,26 @@ int launch_source_average(int Nt, int ncorr, const double2* corr, double scale, 
   if (n == 0) return CTR_OK;
   TimedLaunch tl(s, "source_average");
   source_average_kernel<<<(n + 255) / 256, 256, 0, s>>>(Nt, ncorr, corr, scale, avg);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_rowsum_refine(const double2* rows, const double* rabs, int nrows, const int* off, const int* idx, int nout,
+                         int npair, double2* out, double eps_over_tol, int* count, int* list, int pair_base,
+                         cudaStream_t s) {
+  const int n = npair * nout;
+  if (n == 0) return CTR_OK;
+  TimedLaunch tl(s, "rowsum_refine");
+  rowsum_refine_kernel<<<(n + 255) / 256, 256, 0, s>>>(rows, rabs, nrows, off, idx, nout, npair, out, eps_over_tol,
+                                                        count, list, pair_base);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_scatter(const int* where, const double2* vals, int n, double2* out, cudaStream_t s) {
+  if (n == 0) return CTR_OK;
+  TimedLaunch tl(s, "refine_scatter");
+  scatter_kernel<<<(n + 255) / 256, 256, 0, s>>>(where, vals, n, out);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

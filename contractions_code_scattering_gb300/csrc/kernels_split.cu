@@ -276,22 +276,30 @@ __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJo
 __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
                                                                int nchunk, int ntiles) {
   extern __shared__ __align__(128) uint8_t sm[];
-  int* sexp = (int*)sm;
-  uint8_t* stage = sm + 512;
+  int* sexp = (int*)sm;  // [0, 64): exponents; [64, 320): per-thread partial maxima
+  uint8_t* stage = sm + 2048;
   const SliceTaskRJob& J = jobs[blockIdx.x / ntiles];
   const int nt = blockIdx.x % ntiles;
   const int K = J.nterm * nev, ncols = J.nb * nev;
-  if (threadIdx.x < SPLIT_N) {
-    const int n = nt * SPLIT_N + threadIdx.x;
+  // column exponents: 4 threads per column (k = kq, kq+4, ...), combined in shared memory
+  {
+    const int nn = threadIdx.x % SPLIT_N, kq = threadIdx.x / SPLIT_N;
+    const int n = nt * SPLIT_N + nn;
     int e = -30000;
     if (n < ncols)
-      for (int k = 0; k < K; k++) {
+      for (int k = kq; k < K; k += 4) {
         const double2 v = task_right_elem(J, nev, k, n);
         e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
       }
+    sexp[64 + threadIdx.x] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x < SPLIT_N) {
+    const int* q = sexp + 64 + threadIdx.x;
+    const int e = max(max(q[0], q[SPLIT_N]), max(q[2 * SPLIT_N], q[3 * SPLIT_N]));
     const int E = (e < -1000 ? 0 : e) + J.eplus;
     sexp[threadIdx.x] = E;
-    J.exps[n] = E;
+    J.exps[nt * SPLIT_N + threadIdx.x] = E;
   }
   __syncthreads();
   uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE;
@@ -566,7 +574,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 // *out = coef * sum_{i<nev, j<nev} A(i,j) * conj(B(i,j)); A(i,j) = a[j*lda + i],
 // B(i,j) = b[j*ldb + i] (float-float complex).  One CTA of 128 threads per
 // task; thread i walks column elements i (and i+128) over all j.  The same
-// pass accumulates |coef| sum |A||B| (high words, FP32) into *absout.
+// pass accumulates |coef| sum |A|_1 |B|_1 (high words, FP32; |z|_1 = |Re z| +
+// |Im z|, within a factor 2 of the product of moduli) into *absout.
 __global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __restrict__ tasks, int ntask, int nev) {
   const int t = blockIdx.x;
   if (t >= ntask) return;
@@ -580,7 +589,7 @@ __global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __rest
       ff_mac(sr, er, a.z, a.w, b.z, b.w);   // + ai bi
       ff_mac(si, ei, a.z, a.w, b.x, b.y);   // + ai br
       ff_mac(si, ei, -a.x, -a.y, b.z, b.w); // - ar bi
-      sa = fmaf(sqrtf(fmaf(a.x, a.x, a.z * a.z)), sqrtf(fmaf(b.x, b.x, b.z * b.z)), sa);
+      sa = fmaf(fabsf(a.x) + fabsf(a.z), fabsf(b.x) + fabsf(b.z), sa);
     }
   }
   double re = (double)sr + (double)er, im = (double)si + (double)ei, ab = (double)sa;
@@ -651,7 +660,7 @@ int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int 
 
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
-  const size_t smem = 512 + SPLIT_B_STAGE;
+  const size_t smem = 2048 + SPLIT_B_STAGE;
   static bool attr = false;
   if (!attr) {
     CTR_CUDA(cudaFuncSetAttribute(slice_task_right_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -81,8 +81,8 @@ struct SliceTaskRJob {
 };
 
 // *out = coef * sum_{i,j<nev} A(i,j) conj(B(i,j)), A(i,j) = a[j*lda+i] (float-float complex);
-// *absout = |coef| * sum |A(i,j)| |B(i,j)|, the scale the rounding errors of the
-// trace are proportional to (the entry's condition estimate).
+// *absout = |coef| * sum |A(i,j)|_1 |B(i,j)|_1 (|z|_1 = |Re z| + |Im z|), the scale
+// the rounding errors of the trace are proportional to (the entry's condition estimate).
 struct TraceFFTask {
   const float4* a;
   const float4* b;

@@ -198,7 +198,8 @@ size_t ctr_rho_noalloc_scratch_bytes(void);
  * device complex128 except the host chain description (chain_off, factors, w).
  * Gradients are vector-Jacobian products: grad[k] += Re sum_c w_c d value_c / d f_k,
  * computed by reverse mode with recomputed prefix/suffix products; every f_k must
- * be nonzero. */
+ * be nonzero.  engine selects where the chain products run (CTR_ENGINE_SPLIT: tensor
+ * cores, Nev <= 128); the diagonal reductions and traces are FP64. */
 #define CTR_FACTOR_TAU 0
 #define CTR_FACTOR_PHI 1
 #define CTR_CHAIN_MAXF 12
@@ -215,26 +216,26 @@ int ctr_apply_profile(int nev, long long nmat, const double* f, const double* sr
 /* Generic chains: chain c has factors[chain_off[c] .. chain_off[c+1]) (host arrays), weight
  * w[c] (host complex, may be NULL when grad is NULL).  values [nchain] complex (device, may be
  * NULL); grad [N] real (device, accumulated into, may be NULL). */
-int ctr_chain_adjoint(int nev, int nt, int nphi, const double* prop, const double* phi, const double* f, int nchain,
-                      const int* chain_off, const ctr_factor* factors, const double* w, double* values, double* grad,
-                      void* stream);
+int ctr_chain_adjoint(int engine, int nev, int nt, int nphi, const double* prop, const double* phi, const double* f,
+                      int nchain, const int* chain_off, const ctr_factor* factors, const double* w, double* values,
+                      double* grad, void* stream);
 
 /* rho-rho (lib/calculate_rho_core.h): w [Nt][Nt][48] complex (device) weights the
  * correlators corr[tf][ti][o] of ctr_rho; entries with zero weight are skipped.
  * corr [Nt][Nt][48] (device, may be NULL): the forward correlators of the entries
  * computed (zero elsewhere); grad [N] (device, may be NULL, accumulated into).
  * prop: full perambulator; mom5 [Nt][5][N][N]; f [N] device. */
-int ctr_rho_profile_vjp(int nev, int nt, const double* prop, const double* mom5, const double* f, const double* w,
-                        double* corr, double* grad, void* stream);
+int ctr_rho_profile_vjp(int engine, int nev, int nt, const double* prop, const double* mom5, const double* f,
+                        const double* w, double* corr, double* grad, void* stream);
 
 /* pi pi (lib/contract_kernels_pipi.cu:170-502): w [Nt][Nt][5] complex (device) weights the
  * isospin-weighted slots (square, double triangle, star, fish, horizontal double triangle)
  * of ctr_pipi; pairs whose weights are zero are skipped.  corr [Nt][Nt][5] (device, may be
  * NULL): the forward correlators of the pairs computed (zero elsewhere); grad [N] (device,
  * may be NULL, accumulated into). */
-int ctr_pipi_profile_vjp(int nev, int nt, int isospin, const double* prop, const double* p1, const double* p2,
-                         const double* p3, const double* p4, const double* f, const double* w, double* corr,
-                         double* grad, void* stream);
+int ctr_pipi_profile_vjp(int engine, int nev, int nt, int isospin, const double* prop, const double* p1,
+                         const double* p2, const double* p3, const double* p4, const double* f, const double* w,
+                         double* corr, double* grad, void* stream);
 
 /* On-device source-time average of the dumpData routines (lib/contract.cpp:616-643):
  * avg[dt][c] = scale/Nt * sum_ti corr[(ti+dt)%Nt][ti][c]; corr device [Nt][Nt][ncorr]. */

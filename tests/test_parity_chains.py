@@ -165,3 +165,41 @@ def test_block_product_tasks_split_vs_fp64(cuda):
         scale = np.abs(M1).reshape(4, 4, n, n).max(axis=(1, 3))[:, None, :, None] * np.abs(M2).max() * 4 * n
         err = (np.abs(got - ref).reshape(4, 4, n, n) / scale).max()
         assert err <= tol, (engine, err)
+
+
+def _refine(tol):
+    from contractions_code_scattering_gb300._lib import check, lib
+    check(lib().ctr_split_set_refine(tol))
+
+
+def test_split_chain_refinement(small):
+    """Per-entry accuracy of the split chain engine: with the tolerance below the
+    engine's error every pair is recomputed by the FP64 engine (results equal to
+    FP64 rounding); with 1e-9 every entry meets 1e-9 relative to itself."""
+    from contractions_code_scattering_gb300._lib import lib
+    d, t = small
+    nt = d["prop"].shape[0]
+    ref_pp = O.pipi(d["prop"], *d["ph"], 0)
+    ref_rp = O.rhopi(d["prop"], d["ph"][0], d["ph"][1], d["mom5"], 1)
+    ref_hf = O.sigmapi_hor_fish(d["prop"], d["ph"][0], d["ph"][1])
+    ref_tr = O.sigmapi_triangle(d["prop"], d["ph"][0], d["ph"][1], d["mom2"])
+
+    def rel(got, ref):
+        got = got.cpu().numpy()
+        return (np.abs(got - ref) / np.abs(ref)).max()
+    try:
+        _refine(1e-15)
+        assert rel(api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], 0, engine="split"), ref_pp) < 1e-12
+        assert lib().ctr_split_refined() == nt * nt * 5
+        assert rel(api.run_contract_rhopi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom5"], 1,
+                                          engine="split"), ref_rp) < 1e-12
+        assert lib().ctr_split_refined() == nt * nt * 4
+        hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"], engine="split")
+        assert rel(hf, ref_hf) < 1e-12 and rel(tri, ref_tr) < 1e-12
+        assert lib().ctr_split_refined() == nt + nt * nt * 2
+        _refine(1e-9)
+        assert rel(api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], 0, engine="split"), ref_pp) <= 1e-9
+        hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"], engine="split")
+        assert rel(hf, ref_hf) <= 1e-9 and rel(tri, ref_tr) <= 1e-9
+    finally:
+        _refine(1e-9)
