@@ -13,6 +13,7 @@ in HBM for `value`; `e2e` re-copies them from pinned host memory every step.
 """
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -38,12 +39,14 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
-    ap.add_argument("--nt", type=int, default=NT)
+    ap.add_argument("--nt", type=int, default=None, help="time extent (default: the workload's; a smaller value "
+                                                              "gives a small case of the same kernels, e.g. for ncu)")
     ap.add_argument("--nev", type=int, default=NEV)
-    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint"],
+    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu"],
                     help="rho: the headline rho two-point (Nev=100, Lt=64); rho_small: Nev=32, Lt=16 FP64; "
                          "pipi: pi pi I=0 diagram set, 19 momentum pairs; mixed: rho-pipi / sigma-pipi / "
-                         "sigma loops at Nev=128, Lt=48, 27 momenta; adjoint: profile objective and gradient")
+                         "sigma loops at Nev=128, Lt=48, 27 momenta; adjoint: profile objective and gradient; "
+                         "legacy_gpu: the reference's own rho kernel built for sm_103a beside both engines")
     return ap.parse_args()
 
 
@@ -258,7 +261,7 @@ def main():
     ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
     api.device_init(local)
-    nt, nev = args.nt, args.nev
+    nt, nev = args.nt or NT, args.nev
     moms, rows, coef, oi, nout = workload(nt, nev)
     diagrams = nt * nt * nout
     engine = args.engine
@@ -529,7 +532,7 @@ def run_pipi(args):
     import torch
     from contractions_code_scattering_gb300 import _lib, api, synth
     api.device_init(0)
-    nt, nev = 64, 100
+    nt, nev = args.nt or 64, 100
     moms = synth.momenta(2)
     idx = {p: k for k, p in enumerate(moms)}
     tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
@@ -579,7 +582,7 @@ def run_mixed(args):
     import torch
     from contractions_code_scattering_gb300 import _lib, api, synth
     api.device_init(0)
-    nt, nev = 48, 128
+    nt, nev = args.nt or 48, 128
     moms = synth.momenta(3)
     idx = {p: k for k, p in enumerate(moms)}
     tau = synth.make_prop(nt, nev, seed=SEED, decay=0.25, backend="torch")
@@ -644,7 +647,7 @@ def run_adjoint(args):
     import torch
     from contractions_code_scattering_gb300 import adjoint, api, synth
     api.device_init(0)
-    nt, nev = 64, 100
+    nt, nev = args.nt or 64, 100
     tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
     moms = [(0, 0, 0), (1, 0, 0), (-1, 0, 0)]
     phis = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
@@ -690,7 +693,71 @@ def run_adjoint(args):
     print(json.dumps(line))
 
 
-WORKLOADS = {"rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint}
+def run_legacy_gpu(args):
+    """The reference's own rho kernel (lib/contract_kernels_rho.cu built unmodified for
+    sm_103a: CUDA-core FP64, 25x25 tiles, one launch of 768 spin-row blocks per
+    (t_sink, t_src)) against both engines on the same workload: Nev=100, Lt=64, one
+    momentum, all 48 operator/polarisation outputs (16 op pairs x 3 polarisations) of
+    every (t_sink, t_src).  The reference is timed on the first t_sink rows."""
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import api, synth
+    from oracle import refkernels as RK
+    from oracle import tables as TB
+    if not os.path.exists(RK.cubin("rho")):
+        print(json.dumps({"workload": "legacy_gpu", "unavailable": "reference cubins not built (oracle/build_ref.sh)"}))
+        return
+    api.device_init(0)
+    nt, nev = 64, 100
+    tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(SEED + 3)
+    sd = float(np.sqrt(0.5 / nev))
+    mom5 = torch.complex(torch.randn((nt, 5, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd,
+                         torch.randn((nt, 5, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd)
+    mom5 = mom5.contiguous()
+    m = RK.RefModule(RK.cubin("rho"))
+    spin, lprp, coef = TB.rho_tables()
+    m.set_constant("c_spinIndices_rho", RK._i16(spin))
+    m.set_constant("c_lp_rp_rho", RK._i16(lprp))
+    m.set_constant("c_coef_rho", RK._f32(coef))
+    k = m.kernel("calculate_rho_kernel_double")
+    tmom = RK.texture(mom5)
+    tmp1 = torch.zeros(768 * nev * nev, dtype=torch.complex128, device="cuda")
+    tmp2 = torch.zeros_like(tmp1)
+    out = torch.zeros(nt * 768, dtype=torch.complex128, device="cuda")
+    rows = 2
+    texs = [RK.texture(tau[tf]) for tf in range(rows)]
+    m.launch(k, 768, [RK._p(out), texs[0], tmom, ctypes.c_int(0), ctypes.c_int(0), RK._p(tmp1), RK._p(tmp2)])
+    m.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for tf in range(rows):
+        for ti in range(nt):
+            m.launch(k, 768, [RK._p(out), texs[tf], tmom, ctypes.c_int(ti), ctypes.c_int(tf), RK._p(tmp1),
+                              RK._p(tmp2)])
+    e1.record()
+    m.sync()
+    t_ref = e0.elapsed_time(e1) / 1e3
+    for t in texs:
+        RK.destroy_texture(t)
+    RK.destroy_texture(tmom)
+    ref_rate = rows * nt * 48 / t_ref
+    res = {}
+    for eng in ("fp64", "split"):
+        t, launches, kern = _timed(lambda: api.run_contract_rho(tau, mom5, engine=eng), 1, 1)
+        res[eng] = {"diagrams_per_s": nt * nt * 48 / t, "ms_per_step": 1e3 * t}
+    line = {"workload": "legacy_gpu", "metric": "diagrams/s @Nev=100,Lt=64: rho, 48 outputs per pair, one momentum",
+            "unit": "diagrams/s", "reference_kernel": {"diagrams_per_s": ref_rate, "sample": "t_sink 0..%d, all t_src"
+                                                      % (rows - 1), "ms": 1e3 * t_ref},
+            "fp64_engine": res["fp64"], "split_engine": res["split"],
+            "split_vs_reference_kernel": res["split"]["diagrams_per_s"] / ref_rate,
+            "fp64_vs_reference_kernel": res["fp64"]["diagrams_per_s"] / ref_rate}
+    print(json.dumps(line))
+
+
+WORKLOADS = {"rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint,
+             "legacy_gpu": run_legacy_gpu}
 
 
 if __name__ == "__main__":

@@ -157,11 +157,14 @@ __global__ void pipi_combine_kernel(const double2* __restrict__ tr, int ntr, int
 // ---- per-entry refinement of split-engine chains
 // A chain entry's rounding error is estimated as REFINE_EPS_CHAIN times the sum
 // of |coef| sum |Y|_1 |T|_1 over its closing traces (for products of traces,
-// the product rule of those scales): each of the up to four tensor-core
-// products of a chain keeps ~2^-45 of its row/column scales, and the errors of
-// the N^2 terms of a trace add with random signs.  Pairs (or time slices)
-// with an entry above g_refine_tol * |entry| are recomputed by the FP64 engine.
-constexpr double REFINE_EPS_CHAIN = 1.0 / 70368744177664.0;  // 2^-46
+// the product rule of those scales).  The chain products run on the
+// high-precision split configuration (6 slices, levels 0-3 exact, exact integer
+// recombination), which keeps ~2^-53 of their row/column scales.  Measured on
+// the 20 480 entries of one pi pi momentum pair at Nev=100, Lt=64 against the
+// FP64 engine, the largest entry error without any refinement was 1.8e-10;
+// with REFINE_EPS_CHAIN = 2^-52 no entry is flagged there, and the check stays
+// as the safety net for entries whose cancellation exceeds ~10^6.
+constexpr double REFINE_EPS_CHAIN = 1.0 / 4503599627370496.0;  // 2^-52
 
 struct Refine {
   bool on = false;

@@ -36,13 +36,16 @@ __global__ void ff_to_f64_kernel(const float4* __restrict__ src, int ld, int nev
   dst[e] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
 }
 
-// Error model of a split-engine correlator entry: its rounding error is at
-// most REFINE_EPS * sum_r |coef_r| sum_ij |A_r(i,j)| |B_r(i,j)| (the products'
-// digits reach 2^-45 of the row/column scales; level >= 3 and the float-float
-// recombination add ~2^-47).  Entries whose estimate exceeds rel_tol * |value|
-// -- the few with heavy cancellation between their spin rows or inside their
-// traces -- are recomputed in FP64.
-constexpr double REFINE_EPS = 1.0 / 140737488355328.0;  // 2^-47
+// Error model of a split-engine correlator entry: its rounding error is
+// estimated as REFINE_EPS * sum_r |coef_r| sum_ij |A_r(i,j)|_1 |B_r(i,j)|_1.
+// The products' digits reach 2^-45 of the row/column scales and the errors of
+// the Nev^2 terms of a trace add with random signs, which puts the typical
+// error near 2^-50 of that scale.  REFINE_EPS = 2^-48 was calibrated on the
+// 86 016 entries of the rho benchmark against the FP64 engine: the largest
+// entry error left after refinement was 4.4e-10 at rel_tol = 1e-9.  Entries
+// whose estimate exceeds rel_tol * |value| -- the few with heavy cancellation
+// between their spin rows or inside their traces -- are recomputed in FP64.
+constexpr double REFINE_EPS = 1.0 / 281474976710656.0;  // 2^-48
 
 }  // namespace
 
@@ -183,16 +186,39 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   int* d_list = d_count + 1;
   CTR_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
 
+  // closing traces: each distinct (A block, B block) pair once (rows of different
+  // outputs often share one, e.g. 48 rho rows per momentum use 32 traces); the rows
+  // then combine them with their coefficients
+  std::vector<TraceRow> trow;
+  std::vector<int> tix(nrows);
+  {
+    std::map<std::pair<int, int>, int> seen;
+    for (int r = 0; r < nrows; r++) {
+      const int aoff = (il[r] * N) * ldA + ia[r] * N, boff = (ib[r] * N) * ldB + ir[r] * N;
+      auto it = seen.find({aoff, boff});
+      if (it == seen.end()) {
+        it = seen.emplace(std::make_pair(aoff, boff), (int)trow.size()).first;
+        trow.push_back(TraceRow{aoff, boff, {1.f, 0.f}});
+      }
+      tix[r] = it->second;
+    }
+  }
+  const int ntr = (int)trow.size();
+  void *d_trow, *d_tix, *d_rcoef;
+  CTR_TRY(upload(WS_SPLITJOBS, trow.data(), trow.size() * sizeof(TraceRow), &d_trow, stream));
+  CTR_TRY(upload(WS_SPLITJOBS2, tix.data(), tix.size() * sizeof(int), &d_tix, stream));
+  CTR_TRY(upload(WS_SPLITJOBS3, coef.data(), coef.size() * sizeof(float), &d_rcoef, stream));
+
   std::vector<SliceLeftJob> lj;
   std::vector<SliceRightJob> rj;
   std::vector<SplitGemmInst> ga, gb;
-  std::vector<TraceFFTask> tt;
+  std::vector<const float4*> abase, bbase;
   for (int p0 = 0; p0 < npairs_total; p0 += batch) {
     const int np = std::min(batch, npairs_total - p0);
     void *mem, *rowbuf, *absbuf;
     CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * per_pair, &mem));
-    CTR_TRY(workspace(WS_ROWS).get((size_t)np * nrows * sizeof(double2), &rowbuf));
-    CTR_TRY(workspace(WS_ROWABS).get((size_t)np * nrows * sizeof(double), &absbuf));
+    CTR_TRY(workspace(WS_ROWS).get((size_t)np * ntr * sizeof(double2), &rowbuf));
+    CTR_TRY(workspace(WS_ROWABS).get((size_t)np * ntr * sizeof(double), &absbuf));
     uint8_t* base = (uint8_t*)mem;
     double2* R = (double2*)rowbuf;
     double* Rabs = (double*)absbuf;
@@ -200,7 +226,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     rj.assign(np, SliceRightJob{});
     ga.resize(np);
     gb.resize(np);
-    tt.resize((size_t)np * nrows);
+    abase.resize(np);
+    bbase.resize(np);
     for (int q = 0; q < np; q++) {
       const int pr = p0 + q;
       const int tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
@@ -228,17 +255,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
                             F.rexp + (size_t)ti * F.ntiles * SPLIT_N, A};
       gb[q] = SplitGemmInst{F.left + (size_t)tf * F.mtiles * nchunk * SPLIT_A_STAGE, TR,
                             F.lexp + (size_t)tf * F.mtiles * SPLIT_M, TRe, B};
-      for (int r = 0; r < nrows; r++) {
-        TraceFFTask& t = tt[(size_t)q * nrows + r];
-        t.a = A + (size_t)il[r] * N * ldA + (size_t)ia[r] * N;
-        t.lda = ldA;
-        t.b = B + (size_t)ib[r] * N * ldB + (size_t)ir[r] * N;
-        t.ldb = ldB;
-        t.out = R + (size_t)q * nrows + r;
-        t.absout = Rabs + (size_t)q * nrows + r;
-        t.coef[0] = coef[2 * r];
-        t.coef[1] = coef[2 * r + 1];
-      }
+      abase[q] = A;
+      bbase[q] = B;
     }
     void *d_lj, *d_rj, *d_ga, *d_gb, *d_tt;
     CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &d_lj, stream));
@@ -251,11 +269,15 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     CTR_TRY(launch_split_gemm(GA, np, d_err, stream));
     SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
     CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
-    CTR_TRY(upload(WS_ROWTASKS, tt.data(), tt.size() * sizeof(TraceFFTask), &d_tt, stream));
-    CTR_TRY(launch_trace_ff((const TraceFFTask*)d_tt, (int)tt.size(), N, stream));
-    CTR_TRY(launch_rowsum_refine(R, Rabs, nrows, (const int*)d_csr, (const int*)d_csr + (nout + 1), nout, np,
-                                 (double2*)out + (size_t)p0 * nout, g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0,
-                                 d_count, d_list, p0, stream));
+    abase.insert(abase.end(), bbase.begin(), bbase.end());
+    CTR_TRY(upload(WS_ROWTASKS, abase.data(), abase.size() * sizeof(const float4*), &d_tt, stream));
+    CTR_TRY(launch_trace_rows((const TraceRow*)d_trow, ntr, (const float4* const*)d_tt,
+                              (const float4* const*)d_tt + np, ldA, ldB, np, N, R, Rabs, stream));
+    CTR_TRY(launch_rowsum_coef_refine(R, Rabs, ntr, (const int*)d_csr, (const int*)d_csr + (nout + 1),
+                                      (const int*)d_tix, (const float*)d_rcoef, nout, np,
+                                      (double2*)out + (size_t)p0 * nout,
+                                      g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0, d_count, d_list, p0,
+                                      stream));
   }
   g_refined_last = 0;
   if (g_refine_tol <= 0.0) return CTR_OK;
@@ -430,11 +452,13 @@ extern "C" int ctr_split_levels(int nev, const double* x, const double* y, float
 
 namespace ctr {
 
-// Split-engine execution of a stage of FP64-engine GEMM tasks.  Tasks with the
-// same left side (A pointers, transposes, weights) share one sliced left
-// operand and stack up to SPLIT_TASK_NB right sides along N, so each GEMM
-// instance is 128 x (nb N) x (nterm N); instances of equal shape form one
-// persistent launch, whose epilogue writes complex128 blocks in place.
+// Split-engine execution of a stage of FP64-engine GEMM tasks, on the
+// high-precision configuration (6 slices, 5 levels, tiles of 128 x 48).  Tasks
+// with the same left side (A pointers, transposes, weights) share one sliced
+// left operand and stack up to SPLIT_TASK_NB right sides along N, so each GEMM
+// instance is 128 x (nb N) x (nterm N); identical right sides are sliced once;
+// instances of equal shape form one persistent launch, whose epilogue writes
+// complex128 blocks in place.
 int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream) {
   if (ntask == 0) return CTR_OK;
   if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d (got %d)", SPLIT_MAXK, N);
@@ -485,10 +509,11 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
     }
   for (auto& bk : buckets) {
     const int nterm = bk.first.first, nb = bk.first.second;
-    const int K = nterm * N, nchunk = cdiv(K, SPLIT_K), ntiles = cdiv(nb * N, SPLIT_N);
+    const int K = nterm * N, nchunk = cdiv(K, SPLIT_K), ntiles = cdiv(nb * N, CfgHP::BN);
     const int eplus = K > 128 ? 1 : 0;
-    const size_t l_b = align256((size_t)nchunk * SPLIT_A_STAGE), r_b = align256((size_t)ntiles * nchunk * SPLIT_B_STAGE);
-    const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)ntiles * SPLIT_N * 4);
+    const size_t l_b = align256((size_t)nchunk * CfgHP::A_STAGE);
+    const size_t r_b = align256((size_t)ntiles * nchunk * CfgHP::B_STAGE);
+    const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)ntiles * CfgHP::BN * 4);
     const size_t per = l_b + r_b + le_b + re_b;  // one left and at most one distinct right per instance
     const std::vector<Inst>& all = bk.second;
     const int batch = (int)std::max<size_t>(1, std::min<size_t>(all.size(), ((size_t)2 << 30) / per));
@@ -553,7 +578,7 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
       CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
       CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, ni, N, nchunk, stream));
       CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, (int)rj.size(), N, nchunk, ntiles, stream));
-      SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N};
+      SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N, 1};
       CTR_TRY(launch_split_gemm(G, ni, d_err, stream));
     }
   }

@@ -64,6 +64,12 @@ int launch_source_average(int Nt, int ncorr, const double2* corr, double scale, 
 int launch_rowsum_refine(const double2* rows, const double* rabs, int nrows, const int* off, const int* idx, int nout,
                          int npair, double2* out, double eps_over_tol, int* count, int* list, int pair_base,
                          cudaStream_t s);
+// Row sums over shared traces: out[p][o] = sum over rows r of output o (CSR off/idx) of
+// coef[r] * tr[p][tix[r]]; the error scale sum |coef[r]| trabs[p][tix[r]] flags entries
+// as launch_rowsum_refine does.
+int launch_rowsum_coef_refine(const double2* tr, const double* trabs, int ntr, const int* off, const int* idx,
+                              const int* tix, const float* coef, int nout, int npair, double2* out,
+                              double eps_over_tol, int* count, int* list, int pair_base, cudaStream_t s);
 // Scatter: out[where[i]] = vals[i].
 int launch_scatter(const int* where, const double2* vals, int n, double2* out, cudaStream_t s);
 

@@ -169,6 +169,31 @@ __global__ void rowsum_refine_kernel(const double2* __restrict__ rows, const dou
   }
 }
 
+__global__ void rowsum_coef_refine_kernel(const double2* __restrict__ tr, const double* __restrict__ trabs, int ntr,
+                                          const int* __restrict__ off, const int* __restrict__ idx,
+                                          const int* __restrict__ tix, const float* __restrict__ coef, int nout,
+                                          int npair, double2* __restrict__ out, double eps_over_tol,
+                                          int* __restrict__ count, int* __restrict__ list, int pair_base) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= npair * nout) return;
+  const int p = g / nout, o = g % nout;
+  double re = 0.0, im = 0.0, sc = 0.0;
+  for (int k = off[o]; k < off[o + 1]; k++) {
+    const int r = idx[k];
+    const size_t t = (size_t)p * ntr + tix[r];
+    const double cr = coef[2 * r], ci = coef[2 * r + 1];
+    const double2 v = tr[t];
+    re += cr * v.x - ci * v.y;
+    im += cr * v.y + ci * v.x;
+    sc += sqrt(cr * cr + ci * ci) * trabs[t];
+  }
+  out[(size_t)p * nout + o] = make_double2(re, im);
+  if (eps_over_tol > 0.0 && sc * eps_over_tol > sqrt(re * re + im * im)) {
+    const int slot = atomicAdd(count, 1);
+    list[slot] = (pair_base + p) * nout + o;
+  }
+}
+
 __global__ void scatter_kernel(const int* __restrict__ where, const double2* __restrict__ vals, int n,
                                double2* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -238,6 +263,18 @@ int launch_rowsum_refine(const double2* rows, const double* rabs, int nrows, con
   TimedLaunch tl(s, "rowsum_refine");
   rowsum_refine_kernel<<<(n + 255) / 256, 256, 0, s>>>(rows, rabs, nrows, off, idx, nout, npair, out, eps_over_tol,
                                                         count, list, pair_base);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_rowsum_coef_refine(const double2* tr, const double* trabs, int ntr, const int* off, const int* idx,
+                              const int* tix, const float* coef, int nout, int npair, double2* out,
+                              double eps_over_tol, int* count, int* list, int pair_base, cudaStream_t s) {
+  const int n = npair * nout;
+  if (n == 0) return CTR_OK;
+  TimedLaunch tl(s, "rowsum_refine");
+  rowsum_coef_refine_kernel<<<(n + 255) / 256, 256, 0, s>>>(tr, trabs, ntr, off, idx, tix, coef, nout, npair, out,
+                                                             eps_over_tol, count, list, pair_base);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

@@ -74,7 +74,8 @@ __host__ __device__ constexpr uint64_t digit_offset(int nslice) {
   return o;
 }
 
-__device__ __forceinline__ uint64_t round_fixed(uint64_t U) { return U + digit_offset(SPLIT_NSLICE); }
+template <int NS = SPLIT_NSLICE>
+__device__ __forceinline__ uint64_t round_fixed(uint64_t U) { return U + digit_offset(NS); }
 
 __device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t W, int s, bool neg) {
   const int d = s == 0 ? (int)(W >> 55) : (int)((W >> slice_shift(s)) & 511u) - 256;
@@ -227,6 +228,7 @@ __device__ __forceinline__ double2 task_right_elem(const SliceTaskRJob& J, int n
 }
 
 // Left operand of a task instance (one M tile: rows < nev; K = nterm * nev).
+template <class C>
 __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJob* __restrict__ jobs, int nev,
                                                               int nchunk) {
   extern __shared__ __align__(128) uint8_t sm[];
@@ -256,37 +258,38 @@ __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJo
       const double2 v = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
       const int E = sexp[rr];
       bool nr, ni;
-      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
+      const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v.x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v.y, E, ni));
       const uint32_t off = core_offset(rr, kk);
 #pragma unroll
-      for (int s = 0; s < SPLIT_NSLICE; s++) {
-        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_A_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_A_SUB + off) = slice_bf16(Ui, s, ni);
+      for (int s = 0; s < C::NS; s++) {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::A_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::A_SUB + off) = slice_bf16(Ui, s, ni);
       }
     }
     __syncthreads();
-    int4* d = (int4*)(J.out + (size_t)kc * SPLIT_A_STAGE);
+    int4* d = (int4*)(J.out + (size_t)kc * C::A_STAGE);
     const int4* src = (const int4*)stage;
-    for (int i = threadIdx.x; i < SPLIT_A_STAGE / 16; i += 256) d[i] = src[i];
+    for (int i = threadIdx.x; i < C::A_STAGE / 16; i += 256) d[i] = src[i];
     __syncthreads();
   }
 }
 
 // Right operand of a task instance: N tile nt of the nb stacked output blocks.
+template <class C>
 __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
                                                                int nchunk, int ntiles) {
   extern __shared__ __align__(128) uint8_t sm[];
-  int* sexp = (int*)sm;  // [0, 64): exponents; [64, 320): per-thread partial maxima
+  int* sexp = (int*)sm;  // [0, 64): exponents; [64, 320): per-thread partial maxima (4 per column)
   uint8_t* stage = sm + 2048;
   const SliceTaskRJob& J = jobs[blockIdx.x / ntiles];
   const int nt = blockIdx.x % ntiles;
   const int K = J.nterm * nev, ncols = J.nb * nev;
   // column exponents: 4 threads per column (k = kq, kq+4, ...), combined in shared memory
   {
-    const int nn = threadIdx.x % SPLIT_N, kq = threadIdx.x / SPLIT_N;
-    const int n = nt * SPLIT_N + nn;
+    const int nn = threadIdx.x % C::BN, kq = threadIdx.x / C::BN;
+    const int n = nt * C::BN + nn;
     int e = -30000;
-    if (n < ncols)
+    if (n < ncols && kq < 4)
       for (int k = kq; k < K; k += 4) {
         const double2 v = task_right_elem(J, nev, k, n);
         e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
@@ -294,34 +297,34 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
     sexp[64 + threadIdx.x] = e;
   }
   __syncthreads();
-  if (threadIdx.x < SPLIT_N) {
+  if (threadIdx.x < C::BN) {
     const int* q = sexp + 64 + threadIdx.x;
-    const int e = max(max(q[0], q[SPLIT_N]), max(q[2 * SPLIT_N], q[3 * SPLIT_N]));
+    const int e = max(max(q[0], q[C::BN]), max(q[2 * C::BN], q[3 * C::BN]));
     const int E = (e < -1000 ? 0 : e) + J.eplus;
     sexp[threadIdx.x] = E;
-    J.exps[nt * SPLIT_N + threadIdx.x] = E;
+    J.exps[nt * C::BN + threadIdx.x] = E;
   }
   __syncthreads();
-  uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE;
+  uint8_t* dst_tile = J.out + (size_t)nt * nchunk * C::B_STAGE;
   for (int kc = 0; kc < nchunk; kc++) {
-    for (int e = threadIdx.x; e < SPLIT_N * SPLIT_K; e += 256) {
-      const int nn = e % SPLIT_N, kk = e / SPLIT_N;
-      const int n = nt * SPLIT_N + nn, k = kc * SPLIT_K + kk;
+    for (int e = threadIdx.x; e < C::BN * SPLIT_K; e += 256) {
+      const int nn = e % C::BN, kk = e / C::BN;
+      const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
       const double2 v = (n < ncols && k < K) ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
       const int E = sexp[nn];
       bool nr, ni;
-      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
+      const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v.x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v.y, E, ni));
       const uint32_t off = core_offset(nn, kk);
 #pragma unroll
-      for (int s = 0; s < SPLIT_NSLICE; s++) {
-        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, ni);
+      for (int s = 0; s < C::NS; s++) {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
       }
     }
     __syncthreads();
-    int4* d = (int4*)(dst_tile + (size_t)kc * SPLIT_B_STAGE);
+    int4* d = (int4*)(dst_tile + (size_t)kc * C::B_STAGE);
     const int4* src = (const int4*)stage;
-    for (int i = threadIdx.x; i < SPLIT_B_STAGE / 16; i += 256) d[i] = src[i];
+    for (int i = threadIdx.x; i < C::B_STAGE / 16; i += 256) d[i] = src[i];
     __syncthreads();
   }
 }
@@ -335,12 +338,48 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
 // (tmem_full after the last MMA of a tile, tmem_empty once drained).
 constexpr int GEMM_THREADS = 192;
 constexpr int NSTAGE = 3;
-constexpr int NLEVEL = 4;  // accumulation levels i+j = 0, 1, 2, >=3; (re, im) x 4 x SPLIT_N = 512 TMEM columns
-constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t TMEM_COLS = 512;  // (re, im) x NL levels x BN columns fit in 512 for both configurations
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
 
+template <class C>
 constexpr size_t gemm_smem_bytes() {
-  return (size_t)NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE) + 512;
+  return (size_t)NSTAGE * (C::A_STAGE + C::B_STAGE) + 512;
+}
+static_assert(2 * CfgStd::NL * CfgStd::BN <= (int)TMEM_COLS && 2 * CfgHP::NL * CfgHP::BN <= (int)TMEM_COLS,
+              "accumulators exceed TMEM");
+
+// x * 2^K as an exact 64-bit integer (|x| 2^K < 2^62), bits below 2^0 dropped
+// toward zero; integer operations only.
+__device__ __forceinline__ long long f2i_scaled(float x, int K) {
+  const uint32_t b = __float_as_uint(x);
+  const int be = (int)((b >> 23) & 0xFF);
+  if (be == 0) return 0;
+  const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+  const int sh = be - 150 + K;
+  const long long v = sh >= 0 ? (m << sh) : (sh > -40 ? (m >> -sh) : 0);
+  return (b >> 31) ? -v : v;
+}
+
+// I * 2^e as a double, rounded to nearest even; integer operations only
+// (normal results; magnitudes below 2^-1022 flush to zero).
+__device__ __forceinline__ double i2d_scaled(long long I, int e) {
+  if (I == 0) return 0.0;
+  const unsigned long long sgn = I < 0 ? (1ull << 63) : 0ull;
+  unsigned long long u = I < 0 ? 0ull - (unsigned long long)I : (unsigned long long)I;
+  const int lz = __clzll((long long)u);
+  u <<= lz;
+  unsigned long long mant = u >> 11;
+  const unsigned long long rem = u & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) mant++;
+  int ex = 63 - lz + e;
+  if (mant >> 53) {
+    mant >>= 1;
+    ex++;
+  }
+  const int biased = ex + 1023;
+  if (biased <= 0) return 0.0;
+  if (biased >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 __device__ __forceinline__ float pow2f(int e) {
@@ -355,26 +394,28 @@ __device__ __forceinline__ double pow2d(int e) {
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
-// All MMAs of one K chunk: 15 slice pairs x 4 real products into the 8 level
-// accumulators.  adesc / bdesc describe sub-tile (slice 0, re) of the stage;
-// the other sub-tiles are constant byte offsets (added as offset >> 4 to the
-// start-address field, which cannot carry: shared addresses are < 2^18).
+// All MMAs of one K chunk: NS(NS+1)/2 slice pairs (i + j < NS) x 4 real
+// products into the 2 NL level accumulators.  adesc / bdesc describe sub-tile
+// (slice 0, re) of the stage; the other sub-tiles are constant byte offsets
+// (added as offset >> 4 to the start-address field, which cannot carry:
+// shared addresses are < 2^18).
+template <class C>
 __device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
-  constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, SPLIT_N, false);
-  constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, SPLIT_N, true);
+  constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, C::BN, false);
+  constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, C::BN, true);
 #pragma unroll
-  for (int i = 0; i < SPLIT_NSLICE; i++) {
+  for (int i = 0; i < C::NS; i++) {
 #pragma unroll
-    for (int j = 0; j + i < SPLIT_NSLICE; j++) {
-      const int lvl = (i + j) < NLEVEL - 1 ? (i + j) : NLEVEL - 1;
-      // in loop order the first pair of level 0..3 is (0,0), (0,1), (0,2), (0,3)
-      const uint32_t accum = (!first_chunk || !(i == 0 && j <= NLEVEL - 1)) ? 1u : 0u;
-      const uint64_t ar = adesc + (uint64_t)(((i * 2 + 0) * SPLIT_A_SUB) >> 4);
-      const uint64_t ai = adesc + (uint64_t)(((i * 2 + 1) * SPLIT_A_SUB) >> 4);
-      const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * SPLIT_B_SUB) >> 4);
-      const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * SPLIT_B_SUB) >> 4);
-      const uint32_t dre = tbase + (uint32_t)(lvl * SPLIT_N);
-      const uint32_t dim = tbase + (uint32_t)((NLEVEL + lvl) * SPLIT_N);
+    for (int j = 0; j + i < C::NS; j++) {
+      const int lvl = (i + j) < C::NL - 1 ? (i + j) : C::NL - 1;
+      // in loop order the first pair of level l is (0, l)
+      const uint32_t accum = (!first_chunk || !(i == 0 && j <= C::NL - 1)) ? 1u : 0u;
+      const uint64_t ar = adesc + (uint64_t)(((i * 2 + 0) * C::A_SUB) >> 4);
+      const uint64_t ai = adesc + (uint64_t)(((i * 2 + 1) * C::A_SUB) >> 4);
+      const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * C::B_SUB) >> 4);
+      const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * C::B_SUB) >> 4);
+      const uint32_t dre = tbase + (uint32_t)(lvl * C::BN);
+      const uint32_t dim = tbase + (uint32_t)((C::NL + lvl) * C::BN);
       umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
       umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
       umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
@@ -383,18 +424,19 @@ __device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint
   }
 }
 
+template <class C>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     split_gemm_kernel(SplitGemmBatch g, int ntiles_total, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;
-  uint8_t* sB = smem + NSTAGE * SPLIT_A_STAGE;
-  uint64_t* full = (uint64_t*)(smem + NSTAGE * (SPLIT_A_STAGE + SPLIT_B_STAGE));
+  uint8_t* sB = smem + NSTAGE * C::A_STAGE;
+  uint64_t* full = (uint64_t*)(smem + NSTAGE * (C::A_STAGE + C::B_STAGE));
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = empty + NSTAGE;
   uint64_t* tempty = tfull + 1;
   uint64_t* drainb = tempty + 1;
   uint32_t* tslot = (uint32_t*)(drainb + 1);
-  int* sexp = (int*)(tslot + 4);  // SPLIT_N column exponents of the current tile
+  int* sexp = (int*)(tslot + 4);  // C::BN column exponents of the current tile
 
   volatile int* status = (volatile int*)(tslot + 1);  // block-uniform decisions
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -430,8 +472,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x) {
         const int inst = tile / per_inst, mt = (tile % per_inst) / g.ntiles, nt = tile % g.ntiles;
         const SplitGemmInst* I = &g.inst[inst];
-        const uint8_t* gA = I->left + (size_t)mt * g.nchunk * SPLIT_A_STAGE;
-        const uint8_t* gB = I->right + (size_t)nt * g.nchunk * SPLIT_B_STAGE;
+        const uint8_t* gA = I->left + (size_t)mt * g.nchunk * C::A_STAGE;
+        const uint8_t* gB = I->right + (size_t)nt * g.nchunk * C::B_STAGE;
         for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
           const int s = g_chunk % NSTAGE;
           if (g_chunk >= NSTAGE && !mbar_wait(&empty[s], ((g_chunk / NSTAGE) - 1) & 1, WAIT_NS, err)) {
@@ -439,9 +481,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             ok = false;
             break;
           }
-          mbar_arrive_expect_tx(&full[s], SPLIT_A_STAGE + SPLIT_B_STAGE);
-          bulk_g2s(sA + s * SPLIT_A_STAGE, gA + (size_t)kc * SPLIT_A_STAGE, SPLIT_A_STAGE, &full[s]);
-          bulk_g2s(sB + s * SPLIT_B_STAGE, gB + (size_t)kc * SPLIT_B_STAGE, SPLIT_B_STAGE, &full[s]);
+          mbar_arrive_expect_tx(&full[s], C::A_STAGE + C::B_STAGE);
+          bulk_g2s(sA + s * C::A_STAGE, gA + (size_t)kc * C::A_STAGE, C::A_STAGE, &full[s]);
+          bulk_g2s(sB + s * C::B_STAGE, gB + (size_t)kc * C::B_STAGE, C::B_STAGE, &full[s]);
         }
       }
     }
@@ -467,8 +509,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             break;
           }
           tc_fence_after();
-          issue_chunk(tbase, adesc0 + (uint64_t)((s * SPLIT_A_STAGE) >> 4),
-                      bdesc0 + (uint64_t)((s * SPLIT_B_STAGE) >> 4), kc == 0);
+          issue_chunk<C>(tbase, adesc0 + (uint64_t)((s * C::A_STAGE) >> 4),
+                         bdesc0 + (uint64_t)((s * C::B_STAGE) >> 4), kc == 0);
           umma_commit(&empty[s]);  // stage s free once these MMAs have read it
         }
         if (ok) umma_commit(tfull);
@@ -490,7 +532,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       // stage this tile's column exponents; the barrier also keeps the previous
       // tile's values until every epilogue thread has used them
       epi_bar();
-      if (et < SPLIT_N) sexp[et] = I->rexp[nt * SPLIT_N + et];
+      if (et < C::BN) sexp[et] = I->rexp[nt * C::BN + et];
       const int grow = mt * SPLIT_M + row;
       const bool rvalid = grow < g.mrows;
       const float srow = pow2f(I->lexp[grow]);
@@ -506,51 +548,71 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       tc_fence_after();
       float4* outp = I->out;
       const int ldo = g.ldo;
-      for (int c0 = 0; c0 < SPLIT_N; c0 += 16) {
-        // Re then Im: 4 level accumulators of 16 columns each -> float-float
+      for (int c0 = 0; c0 < C::BN; c0 += 16) {
+        if (g.out_mode == 1) {
+          // complex128 output: the exact levels and the last one summed exactly
+          // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
+          // below 2^8, so no overflow), then rounded once to double
+          long long acc[2][16];
+#pragma unroll
+          for (int part = 0; part < 2; part++) {
+#pragma unroll
+            for (int c = 0; c < 16; c++) acc[part][c] = 0;
+#pragma unroll
+            for (int l = 0; l < C::NL; l++) {
+              float v[16];
+              tmem_ld16(tl + (uint32_t)((part * C::NL + l) * C::BN + c0), v);
+              tmem_ld_wait();
+#pragma unroll
+              for (int c = 0; c < 16; c++) acc[part][c] += f2i_scaled(v[c], 54);
+            }
+          }
+          if (!rvalid) continue;
+          const int erow = I->lexp[grow];
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const int gcol = nt * C::BN + c0 + c;
+            if (gcol >= g.ncols) continue;
+            const int e = erow + sexp[c0 + c] - 54;
+            const int j = gcol / g.blkn, cc = gcol - j * g.blkn;
+            I->outs[j][(size_t)grow * g.blkn + cc] = make_double2(i2d_scaled(acc[0][c], e), i2d_scaled(acc[1][c], e));
+          }
+          continue;
+        }
+        // float-float output: levels 0 .. NL-2 exact, combined by exact two-sums;
+        // the rounding errors and the last level go to the low word
         float hi[2][16], lo[2][16];
 #pragma unroll
         for (int part = 0; part < 2; part++) {
-          float v[NLEVEL][16];
+          float v[C::NL][16];
 #pragma unroll
-          for (int l = 0; l < NLEVEL; l++) tmem_ld16(tl + (uint32_t)((part * NLEVEL + l) * SPLIT_N + c0), v[l]);
+          for (int l = 0; l < C::NL; l++) tmem_ld16(tl + (uint32_t)((part * C::NL + l) * C::BN + c0), v[l]);
           tmem_ld_wait();
           if (g.levels && rvalid) {
             for (int c = 0; c < 16; c++) {
-              const int gcol = nt * SPLIT_N + c0 + c;
+              const int gcol = nt * C::BN + c0 + c;
               if (gcol < g.ncols)
-                for (int l = 0; l < NLEVEL; l++)
-                  g.levels[((size_t)(part * NLEVEL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
+                for (int l = 0; l < C::NL; l++)
+                  g.levels[((size_t)(part * C::NL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
             }
           }
 #pragma unroll
           for (int c = 0; c < 16; c++) {
-            // levels 0..2 are exact multiples of 2^-16, 2^-25, 2^-34: two exact
-            // two-sums keep them; the rounding errors and level >= 3 (~2^-27 of
-            // the result) go to the low word, rounded at ~2^-48 of the result
-            float s1, e1, s2, e2;
-            two_sum(v[0][c], v[1][c], s1, e1);
-            two_sum(s1, v[2][c], s2, e2);
-            fast_two_sum(s2, (e1 + e2) + v[3][c], hi[part][c], lo[part][c]);
+            float s = v[0][c], e = 0.f;
+#pragma unroll
+            for (int l = 1; l < C::NL - 1; l++) {
+              float t, d;
+              two_sum(s, v[l][c], t, d);
+              s = t;
+              e += d;
+            }
+            fast_two_sum(s, e + v[C::NL - 1][c], hi[part][c], lo[part][c]);
           }
         }
         if (!rvalid || g.levels) continue;
-        if (g.out_mode == 1) {
-          const int erow = I->lexp[grow];
-#pragma unroll
-          for (int c = 0; c < 16; c++) {
-            const int gcol = nt * SPLIT_N + c0 + c;
-            if (gcol >= g.ncols) continue;
-            const double sc = pow2d(erow + sexp[c0 + c]);
-            const int j = gcol / g.blkn, cc = gcol - j * g.blkn;
-            I->outs[j][(size_t)grow * g.blkn + cc] =
-                make_double2(((double)hi[0][c] + (double)lo[0][c]) * sc, ((double)hi[1][c] + (double)lo[1][c]) * sc);
-          }
-          continue;
-        }
 #pragma unroll
         for (int c = 0; c < 16; c++) {
-          const int gcol = nt * SPLIT_N + c0 + c;
+          const int gcol = nt * C::BN + c0 + c;
           if (gcol >= g.ncols) continue;
           const float sc = srow * pow2f(sexp[c0 + c]);
           outp[(size_t)gcol * ldo + grow] = make_float4(hi[0][c] * sc, lo[0][c] * sc, hi[1][c] * sc, lo[1][c] * sc);
@@ -570,25 +632,33 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   }
 }
 
-// ------------------------------------------------------------- ff traces
-// *out = coef * sum_{i<nev, j<nev} A(i,j) * conj(B(i,j)); A(i,j) = a[j*lda + i],
-// B(i,j) = b[j*ldb + i] (float-float complex).  One CTA of 128 threads per
-// task; thread i walks column elements i (and i+128) over all j.  The same
-// pass accumulates |coef| sum |A|_1 |B|_1 (high words, FP32; |z|_1 = |Re z| +
-// |Im z|, within a factor 2 of the product of moduli) into *absout.
-__global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __restrict__ tasks, int ntask, int nev) {
-  const int t = blockIdx.x;
-  if (t >= ntask) return;
-  const TraceFFTask T = tasks[t];
+// ----------------------------------------------------------- closing traces
+// rows[q * nrows + r] = coef_r * sum_{i,j < nev} A(i,j) conj(B(i,j)) with
+// A = abase[q] + rt[r].aoff, B = bbase[q] + rt[r].boff, element (i, j) at
+// [j * ld + i] (float-float complex).  One CTA of 128 threads per (pair, row),
+// rows of a pair adjacent so that the blocks they share are re-read from L2;
+// thread i walks column elements i (and i + 128) over all j and keeps its sum
+// in float-float.  The same pass accumulates |coef_r| sum |A|_1 |B|_1 (high
+// words, FP32; |z|_1 = |Re z| + |Im z|, within a factor 2 of the product of
+// moduli) into rabs.
+__global__ void __launch_bounds__(128) trace_rows_kernel(const TraceRow* __restrict__ rt, int nrows,
+                                                         const float4* const* __restrict__ abase,
+                                                         const float4* const* __restrict__ bbase, int lda, int ldb,
+                                                         int nev, double2* __restrict__ rows,
+                                                         double* __restrict__ rabs) {
+  const int q = blockIdx.x / nrows, r = blockIdx.x % nrows;
+  const TraceRow T = rt[r];
+  const float4* pa = abase[q] + T.aoff;
+  const float4* pb = bbase[q] + T.boff;
   float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f, sa = 0.f;
   for (int i = threadIdx.x; i < nev; i += 128) {
     for (int j = 0; j < nev; j++) {
-      const float4 a = T.a[(size_t)j * T.lda + i];
-      const float4 b = T.b[(size_t)j * T.ldb + i];
-      ff_mac(sr, er, a.x, a.y, b.x, b.y);   // + ar br
-      ff_mac(sr, er, a.z, a.w, b.z, b.w);   // + ai bi
-      ff_mac(si, ei, a.z, a.w, b.x, b.y);   // + ai br
-      ff_mac(si, ei, -a.x, -a.y, b.z, b.w); // - ar bi
+      const float4 a = pa[(size_t)j * lda + i];
+      const float4 b = pb[(size_t)j * ldb + i];
+      ff_mac(sr, er, a.x, a.y, b.x, b.y);    // + ar br
+      ff_mac(sr, er, a.z, a.w, b.z, b.w);    // + ai bi
+      ff_mac(si, ei, a.z, a.w, b.x, b.y);    // + ai br
+      ff_mac(si, ei, -a.x, -a.y, b.z, b.w);  // - ar bi
       sa = fmaf(fabsf(a.x) + fabsf(a.z), fabsf(b.x) + fabsf(b.z), sa);
     }
   }
@@ -609,9 +679,9 @@ __global__ void __launch_bounds__(128) trace_ff_kernel(const TraceFFTask* __rest
     re = red[0][0] + red[0][1] + red[0][2] + red[0][3];
     im = red[1][0] + red[1][1] + red[1][2] + red[1][3];
     ab = red[2][0] + red[2][1] + red[2][2] + red[2][3];
-    double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
-    *T.out = cmul(c, make_double2(re, im));
-    if (T.absout) *T.absout = sqrt(c.x * c.x + c.y * c.y) * ab;
+    const double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+    rows[blockIdx.x] = cmul(c, make_double2(re, im));
+    rabs[blockIdx.x] = sqrt(c.x * c.x + c.y * c.y) * ab;
   }
 }
 
@@ -646,38 +716,40 @@ int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchu
 
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
-  const size_t smem = 512 + SPLIT_A_STAGE;
+  const size_t smem = 512 + CfgHP::A_STAGE;
   static bool attr = false;
   if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(slice_task_left_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CTR_CUDA(cudaFuncSetAttribute(slice_task_left_kernel<CfgHP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
     attr = true;
   }
   TimedLaunch tl(s, "slice_task_left");
-  slice_task_left_kernel<<<njobs, 256, smem, s>>>(d_jobs, nev, nchunk);
+  slice_task_left_kernel<CfgHP><<<njobs, 256, smem, s>>>(d_jobs, nev, nchunk);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
 
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
-  const size_t smem = 2048 + SPLIT_B_STAGE;
+  const size_t smem = 2048 + CfgHP::B_STAGE;
   static bool attr = false;
   if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(slice_task_right_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CTR_CUDA(cudaFuncSetAttribute(slice_task_right_kernel<CfgHP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
     attr = true;
   }
   TimedLaunch tl(s, "slice_task_right");
-  slice_task_right_kernel<<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+  slice_task_right_kernel<CfgHP><<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
 
-int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
-  if (ninst == 0) return CTR_OK;
-  const size_t smem = gemm_smem_bytes();
+template <class C>
+static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, const char* name) {
+  const size_t smem = gemm_smem_bytes<C>();
   static bool attr = false;
   if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CTR_CUDA(cudaFuncSetAttribute(split_gemm_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
   static int nsm = 0;
@@ -689,16 +761,28 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
   const long long total = (long long)ninst * g.mtiles * g.ntiles;
   if (total > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
   const int grid = (int)std::min<long long>(total, nsm);
-  TimedLaunch tl(s, "split_gemm");
-  split_gemm_kernel<<<grid, GEMM_THREADS, smem, s>>>(g, (int)total, d_err);
+  TimedLaunch tl(s, name);
+  split_gemm_kernel<C><<<grid, GEMM_THREADS, smem, s>>>(g, (int)total, d_err);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
 
-int launch_trace_ff(const TraceFFTask* d_tasks, int ntask, int nev, cudaStream_t s) {
-  if (ntask == 0) return CTR_OK;
-  TimedLaunch tl(s, "trace_ff");
-  trace_ff_kernel<<<ntask, 128, 0, s>>>(d_tasks, ntask, nev);
+int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
+  if (ninst == 0) return CTR_OK;
+  if (g.hp) {
+    if (g.out_mode != 1 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: the high-precision tiles write complex128");
+    return launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");
+  }
+  return launch_split_gemm_cfg<CfgStd>(g, ninst, d_err, s, "split_gemm");
+}
+
+int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
+                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, cudaStream_t s) {
+  if (npair == 0 || nrows == 0) return CTR_OK;
+  const long long nblk = (long long)npair * nrows;
+  if (nblk > 0x7fffffffLL) return fail(CTR_ERR_ARG, "traces: grid too large");
+  TimedLaunch tl(s, "trace_rows");
+  trace_rows_kernel<<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

@@ -21,6 +21,24 @@ constexpr int SPLIT_A_STAGE = SPLIT_NSLICE * 2 * SPLIT_A_SUB;       // 40960 B: 
 constexpr int SPLIT_B_STAGE = SPLIT_NSLICE * 2 * SPLIT_B_SUB;       // 20480 B
 constexpr int SPLIT_MAXBLK = 32;
 
+// Kernel configurations: slices per value, TMEM accumulation levels, tile N.
+//  * standard (two-sided form, float-float products): 5 slices (15 slice
+//    pairs), levels 0, 1, 2 exact and >= 3 in FP32, N = 64 (8 x 64 = 512 TMEM columns);
+//  * high precision (task form of the chain diagrams, complex128 products):
+//    6 slices (21 slice pairs, 54 bits), levels 0-3 exact and >= 4 in FP32,
+//    N = 48 (10 x 48 = 480 TMEM columns); the epilogue sums the levels exactly
+//    in 64-bit integers, so products keep ~2^-53 of their row/column scales.
+template <int NS_, int NL_, int BN_>
+struct SplitCfg {
+  static constexpr int NS = NS_, NL = NL_, BN = BN_;
+  static constexpr int A_SUB = SPLIT_M * SPLIT_K * 2;
+  static constexpr int B_SUB = BN * SPLIT_K * 2;
+  static constexpr int A_STAGE = NS * 2 * A_SUB;
+  static constexpr int B_STAGE = NS * 2 * B_SUB;
+};
+using CfgStd = SplitCfg<SPLIT_NSLICE, 4, SPLIT_N>;
+using CfgHP = SplitCfg<6, 5, 48>;
+
 // Slicing of a stacked operand.  Left: rows r -> row r%nev of blk[r/nev].
 struct SliceLeftJob {
   const double2* blk[SPLIT_MAXBLK];
@@ -57,6 +75,7 @@ struct SplitGemmBatch {
                      // [8][ncols][ldo] of instance 0 instead of the ff output
   int out_mode;      // 0: float-float column-major, 1: complex128 row-major blocks
   int blkn;          // out_mode 1: columns (and row stride) of one output block
+  int hp;            // 0: CfgStd operands and tiles, 1: CfgHP (out_mode 1 only)
 };
 
 // Operands of the task form C = sum_q w_q op(A_q) op(B_q) (q < nterm <= 4),
@@ -70,25 +89,20 @@ struct SliceTaskLJob {
   const double2* a[4];
   float w[4];
   int nterm, dag, eplus, pad;
-  uint8_t* out;  // [nchunk][SPLIT_A_STAGE]
+  uint8_t* out;  // [nchunk][CfgHP::A_STAGE]
   int* exps;     // [SPLIT_M]
 };
 struct SliceTaskRJob {
   const double2* b[SPLIT_TASK_NB][4];
   int nb, nterm, dag, eplus;
-  uint8_t* out;  // [ntiles][nchunk][SPLIT_B_STAGE]
-  int* exps;     // [ntiles * SPLIT_N]
+  uint8_t* out;  // [ntiles][nchunk][CfgHP::B_STAGE]
+  int* exps;     // [ntiles * CfgHP::BN]
 };
 
-// *out = coef * sum_{i,j<nev} A(i,j) conj(B(i,j)), A(i,j) = a[j*lda+i] (float-float complex);
-// *absout = |coef| * sum |A(i,j)|_1 |B(i,j)|_1 (|z|_1 = |Re z| + |Im z|), the scale
-// the rounding errors of the trace are proportional to (the entry's condition estimate).
-struct TraceFFTask {
-  const float4* a;
-  const float4* b;
-  double2* out;
-  double* absout;
-  int lda, ldb;
+// Closing trace of one two-sided row: element offsets of its A block (cd, L)
+// and B block (ab, R) inside a pair's product matrices, and its coefficient.
+struct TraceRow {
+  int aoff, boff;
   float coef[2];
 };
 
@@ -119,7 +133,11 @@ __device__ __forceinline__ void ff_mac(float& S, float& E, float xh, float xl, f
 int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s);
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
-int launch_trace_ff(const TraceFFTask* d_tasks, int ntask, int nev, cudaStream_t s);
+// Closing traces over npair pairs: products of pair q at a_base[q] / b_base[q]
+// (leading dimensions lda / ldb); rows[q * nrows + r] = coef_r * trace and
+// rabs[q * nrows + r] = |coef_r| sum |A|_1 |B|_1.
+int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
+                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, cudaStream_t s);
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s);
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 
