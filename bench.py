@@ -449,8 +449,15 @@ def roofline(engine, report, steps, nt, nev, nmom):
     peak = pk.get("bf16_tflops", 1924.8)
     mma_flops = steps * prods * 8.0 * n3 * 15 * (112.0 / 100.0)
     achieved = mma_flops / launches / (ms / launches / 1e3) / 1e12
+    # DRAM traffic per launch: the ncu capture of one launch at Nt=8 (64 pairs, 7 momenta, Nev=100)
+    # read 0.245 GB and wrote 1.089 GB, i.e. 20.8 MB per (t_sink, t_src) pair; scaled by the
+    # pairs one launch processes here (both GEMMs of a batch have the same output size)
+    pairs_per_launch = steps * nt * nt * 2.0 / launches
+    traffic = 20.84e6 * pairs_per_launch * (nmom / 7.0) if nev == 100 else None
     return {"kernel": "split_gemm", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at Nt=8, scaled "
+                              "by pairs per launch (profiles/split_gemm_rho_nt8.md)",
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
             "fp64_equivalent_tflops": achieved / 15 / 1.12,
             "algorithmic": "15 bf16 slice-pair products x 8*Nev^3 flops (K padded 100->112) per block product"}
