@@ -444,8 +444,8 @@ int check_engine(int engine, int nev) {
 }  // namespace
 
 int chain_values(int N, int Nt, int nphi, const double* prop, const double* phi, const std::vector<ctr_factor>& factors,
-                 const std::vector<int>& off, double* values, cudaStream_t s) {
-  ChainRunner R(N, Nt, nphi, (const double2*)prop, (const double2*)phi, nullptr, (double2*)values, nullptr, s);
+                 const std::vector<int>& off, double* values, cudaStream_t s, int engine) {
+  ChainRunner R(N, Nt, nphi, (const double2*)prop, (const double2*)phi, nullptr, (double2*)values, nullptr, s, engine);
   const int nchain = (int)off.size() - 1;
   for (int c = 0; c < nchain; c++) {
     const int n = off[c + 1] - off[c];

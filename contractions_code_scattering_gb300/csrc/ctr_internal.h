@@ -114,6 +114,8 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
 // Upload a host array into a workspace slot (async on stream, host buffer is
 // kept alive by a pinned staging copy owned by the slot).
 int upload(int slot, const void* host, size_t bytes, void** dev, cudaStream_t stream);
+// dst (device) <- src (device-accessible, e.g. mapped pinned host memory), by a kernel.
+int launch_stage_copy(void* dst, const void* src, size_t bytes, cudaStream_t stream);
 
 // ------------------------------------------------------- two-sided plan
 struct TwoSidedRow {
@@ -127,11 +129,12 @@ int twosided_split(int nev, int nt, int tf_begin, int tf_end, const double* prop
                    int nphi, const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
                    const std::vector<int32_t>& out_index, int nout, double* out, cudaStream_t stream);
 
-// Traces of chains of perambulator blocks and plain elementals in FP64
-// (the chain program of the profile adjoint, without a profile):
-// values[c] = Tr[F_1 ... F_n] for chain c = factors[off[c] .. off[c+1]);
-// perambulator factors index prop [rows][Nt][4][4][N][N] by (a = row, b = t2).
+// Traces of chains of perambulator blocks and plain elementals (the chain
+// program of the profile adjoint, without a profile): values[c] = Tr[F_1 ... F_n]
+// for chain c = factors[off[c] .. off[c+1]); perambulator factors index prop
+// [rows][Nt][4][4][N][N] by (a = row, b = t2).  engine: where the products run
+// (CTR_ENGINE_SPLIT: the high-precision split configuration); traces are FP64.
 int chain_values(int N, int Nt, int nphi, const double* prop, const double* phi, const std::vector<ctr_factor>& factors,
-                 const std::vector<int>& off, double* values, cudaStream_t s);
+                 const std::vector<int>& off, double* values, cudaStream_t s, int engine);
 
 }  // namespace ctr

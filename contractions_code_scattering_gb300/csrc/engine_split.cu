@@ -44,7 +44,8 @@ __global__ void ff_to_f64_kernel(const float4* __restrict__ src, int ld, int nev
 // 86 016 entries of the rho benchmark against the FP64 engine: the largest
 // entry error left after refinement was 4.4e-10 at rel_tol = 1e-9.  Entries
 // whose estimate exceeds rel_tol * |value| -- the few with heavy cancellation
-// between their spin rows or inside their traces -- are recomputed in FP64.
+// between their spin rows or inside their traces -- are recomputed with the
+// high-precision split configuration.
 constexpr double REFINE_EPS = 1.0 / 281474976710656.0;  // 2^-48
 
 }  // namespace
@@ -212,7 +213,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   std::vector<SliceLeftJob> lj;
   std::vector<SliceRightJob> rj;
   std::vector<SplitGemmInst> ga, gb;
-  std::vector<const float4*> abase, bbase;
+  std::vector<const float2*> abase, bbase;
+  const size_t aplane = (size_t)F.ntiles * SPLIT_N * ldA, bplane = (size_t)ntT * SPLIT_N * ldB;
   for (int p0 = 0; p0 < npairs_total; p0 += batch) {
     const int np = std::min(batch, npairs_total - p0);
     void *mem, *rowbuf, *absbuf;
@@ -255,8 +257,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
                             F.rexp + (size_t)ti * F.ntiles * SPLIT_N, A};
       gb[q] = SplitGemmInst{F.left + (size_t)tf * F.mtiles * nchunk * SPLIT_A_STAGE, TR,
                             F.lexp + (size_t)tf * F.mtiles * SPLIT_M, TRe, B};
-      abase[q] = A;
-      bbase[q] = B;
+      abase[q] = (const float2*)A;
+      bbase[q] = (const float2*)B;
     }
     void *d_lj, *d_rj, *d_ga, *d_gb, *d_tt;
     CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &d_lj, stream));
@@ -266,13 +268,17 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     CTR_TRY(upload(WS_GEMM_A, ga.data(), ga.size() * sizeof(SplitGemmInst), &d_ga, stream));
     CTR_TRY(upload(WS_GEMM_B, gb.data(), gb.size() * sizeof(SplitGemmInst), &d_gb, stream));
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
+    GA.parts = 1;
+    GA.plane = aplane;
     CTR_TRY(launch_split_gemm(GA, np, d_err, stream));
     SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
+    GB.parts = 1;
+    GB.plane = bplane;
     CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
     abase.insert(abase.end(), bbase.begin(), bbase.end());
     CTR_TRY(upload(WS_ROWTASKS, abase.data(), abase.size() * sizeof(const float4*), &d_tt, stream));
-    CTR_TRY(launch_trace_rows((const TraceRow*)d_trow, ntr, (const float4* const*)d_tt,
-                              (const float4* const*)d_tt + np, ldA, ldB, np, N, R, Rabs, stream));
+    CTR_TRY(launch_trace_rows((const TraceRow*)d_trow, ntr, (const float2* const*)d_tt,
+                              (const float2* const*)d_tt + np, ldA, ldB, aplane, bplane, np, N, R, Rabs, stream));
     CTR_TRY(launch_rowsum_coef_refine(R, Rabs, ntr, (const int*)d_csr, (const int*)d_csr + (nout + 1),
                                       (const int*)d_tix, (const float*)d_rcoef, nout, np,
                                       (double2*)out + (size_t)p0 * nout,
@@ -319,7 +325,9 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   }
   void* dv;
   CTR_TRY(workspace(WS_REFINE).get(chain_row.size() * sizeof(double2), &dv));
-  CTR_TRY(chain_values(N, Nt, nphi, prop_rows, phi, fac, foff, (double*)dv, stream));
+  // the flagged entries' chains on the high-precision configuration (~2^-53 of the
+  // row/column scales, ~2^9 below the standard one); traces in FP64
+  CTR_TRY(chain_values(N, Nt, nphi, prop_rows, phi, fac, foff, (double*)dv, stream, CTR_ENGINE_SPLIT));
   std::vector<double2> vals(chain_row.size());
   CTR_CUDA(cudaMemcpyAsync(vals.data(), dv, vals.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream));
   CTR_CUDA(cudaStreamSynchronize(stream));

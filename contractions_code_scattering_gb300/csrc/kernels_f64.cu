@@ -6,6 +6,8 @@
 // pipe busy with no padded work (threads whose outputs fall outside the Nev x
 // Nev block issue no DFMA) and to keep the summation order of the reference
 // (k ascending for every matrix element).
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace ctr {
@@ -275,6 +277,26 @@ int launch_rowsum_coef_refine(const double2* tr, const double* trabs, int ntr, c
   TimedLaunch tl(s, "rowsum_refine");
   rowsum_coef_refine_kernel<<<(n + 255) / 256, 256, 0, s>>>(tr, trabs, ntr, off, idx, tix, coef, nout, npair, out,
                                                              eps_over_tol, count, list, pair_base);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+__global__ void stage_copy_kernel(int4* __restrict__ dst, const int4* __restrict__ src, size_t n16,
+                                  uint8_t* __restrict__ dtail, const uint8_t* __restrict__ stail, int ntail) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+  if (blockIdx.x == 0 && threadIdx.x < ntail) dtail[threadIdx.x] = stail[threadIdx.x];
+}
+
+int launch_stage_copy(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return CTR_OK;
+  // both buffers are at least 16-byte aligned (cudaMalloc / cudaHostAlloc)
+  const size_t n16 = bytes / 16;
+  const int ntail = (int)(bytes % 16);
+  const int grid = (int)std::min<size_t>(1024, std::max<size_t>(1, (n16 + 255) / 256));
+  TimedLaunch tl(s, "stage_copy");
+  stage_copy_kernel<<<grid, 256, 0, s>>>((int4*)dst, (const int4*)src, n16, (uint8_t*)dst + n16 * 16,
+                                         (const uint8_t*)src + n16 * 16, ntail);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

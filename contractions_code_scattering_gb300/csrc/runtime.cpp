@@ -71,10 +71,14 @@ void Workspace::release() {
 
 Workspace& workspace(int slot) { return g_ws[slot]; }
 
-// Host-to-device upload through a pinned staging buffer per slot, so that the
-// copy is truly asynchronous and the caller's host array may be reused at once.
+// Host-to-device upload through a mapped pinned staging buffer per slot: a small
+// kernel reads the staging buffer over the host link and writes the device
+// workspace, so the tables of a call never queue behind large copy-engine
+// transfers that a caller runs on other streams (e.g. the next step's inputs),
+// and the caller's host array may be reused at once.
 struct Staging {
   void* host = nullptr;
+  void* host_dev = nullptr;  // device alias of the mapped staging buffer
   size_t bytes = 0;
   cudaEvent_t done = nullptr;
 };
@@ -82,17 +86,19 @@ static Staging g_stage[WS_COUNT];
 
 int upload(int slot, const void* host, size_t bytes, void** dev, cudaStream_t stream) {
   Staging& s = g_stage[slot];
-  if (s.done) CTR_CUDA(cudaEventSynchronize(s.done));  // previous upload from this buffer finished
+  if (s.done) CTR_CUDA(cudaEventSynchronize(s.done));  // the previous upload from this buffer was consumed
   if (bytes > s.bytes) {
     if (s.host) CTR_CUDA(cudaFreeHost(s.host));
+    s.host = nullptr;
     size_t nb = bytes < 4096 ? 4096 : bytes * 2;
-    CTR_CUDA(cudaMallocHost(&s.host, nb));
+    CTR_CUDA(cudaHostAlloc(&s.host, nb, cudaHostAllocMapped));
+    CTR_CUDA(cudaHostGetDevicePointer(&s.host_dev, s.host, 0));
     s.bytes = nb;
   }
   if (!s.done) CTR_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
   std::memcpy(s.host, host, bytes);
   CTR_TRY(g_ws[slot].get(bytes, dev));
-  CTR_CUDA(cudaMemcpyAsync(*dev, s.host, bytes, cudaMemcpyHostToDevice, stream));
+  CTR_TRY(launch_stage_copy(*dev, s.host_dev, bytes, stream));
   CTR_CUDA(cudaEventRecord(s.done, stream));
   return CTR_OK;
 }

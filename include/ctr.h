@@ -244,14 +244,15 @@ int ctr_source_average(int nt, int ncorr, const double* corr, double scale, doub
 /* 1 when the split-precision tensor-core engine is compiled in. */
 int ctr_split_available(void);
 
-/* Per-entry accuracy control of the split engine's two-sided contractions
- * (rho, sigma, ctr_twosided).  Each correlator entry carries an error estimate
- * 2^-47 * sum_r |coef_r| sum_ij |A_r(i,j)||B_r(i,j)| (its spin rows' Hadamard
- * traces in absolute value); entries whose estimate exceeds rel_tol * |entry|
- * -- those with heavy cancellation -- are recomputed by FP64 chain products
- * and patched in.  rel_tol = 0 disables the check.  Default 1e-9. */
+/* Per-entry accuracy control of the split engine (two-sided rho/sigma/ctr_twosided
+ * contractions and the chain families).  Each correlator entry carries an error
+ * estimate eps * sum_r |coef_r| sum_ij |A_r(i,j)|_1 |B_r(i,j)|_1 over its closing
+ * traces (|z|_1 = |Re z| + |Im z|); entries whose estimate exceeds rel_tol * |entry|
+ * -- those with heavy cancellation -- are recomputed (two-sided form: their spin rows
+ * on the high-precision split configuration; chains: their (t_sink, t_src) pairs on
+ * the FP64 engine) and patched in.  rel_tol = 0 disables the check.  Default 1e-9. */
 int ctr_split_set_refine(double rel_tol);
-/* Number of entries recomputed in FP64 by the last split two-sided call. */
+/* Number of entries the last split call recomputed. */
 long long ctr_split_refined(void);
 
 /* Synchronise the stream and report the first device-side error flag. */
