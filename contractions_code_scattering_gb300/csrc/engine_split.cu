@@ -213,8 +213,7 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   std::vector<SliceLeftJob> lj;
   std::vector<SliceRightJob> rj;
   std::vector<SplitGemmInst> ga, gb;
-  std::vector<const float2*> abase, bbase;
-  const size_t aplane = (size_t)F.ntiles * SPLIT_N * ldA, bplane = (size_t)ntT * SPLIT_N * ldB;
+  std::vector<const float4*> abase, bbase;
   for (int p0 = 0; p0 < npairs_total; p0 += batch) {
     const int np = std::min(batch, npairs_total - p0);
     void *mem, *rowbuf, *absbuf;
@@ -257,8 +256,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
                             F.rexp + (size_t)ti * F.ntiles * SPLIT_N, A};
       gb[q] = SplitGemmInst{F.left + (size_t)tf * F.mtiles * nchunk * SPLIT_A_STAGE, TR,
                             F.lexp + (size_t)tf * F.mtiles * SPLIT_M, TRe, B};
-      abase[q] = (const float2*)A;
-      bbase[q] = (const float2*)B;
+      abase[q] = A;
+      bbase[q] = B;
     }
     void *d_lj, *d_rj, *d_ga, *d_gb, *d_tt;
     CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &d_lj, stream));
@@ -268,17 +267,13 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     CTR_TRY(upload(WS_GEMM_A, ga.data(), ga.size() * sizeof(SplitGemmInst), &d_ga, stream));
     CTR_TRY(upload(WS_GEMM_B, gb.data(), gb.size() * sizeof(SplitGemmInst), &d_gb, stream));
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
-    GA.parts = 1;
-    GA.plane = aplane;
     CTR_TRY(launch_split_gemm(GA, np, d_err, stream));
     SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
-    GB.parts = 1;
-    GB.plane = bplane;
     CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
     abase.insert(abase.end(), bbase.begin(), bbase.end());
     CTR_TRY(upload(WS_ROWTASKS, abase.data(), abase.size() * sizeof(const float4*), &d_tt, stream));
-    CTR_TRY(launch_trace_rows((const TraceRow*)d_trow, ntr, (const float2* const*)d_tt,
-                              (const float2* const*)d_tt + np, ldA, ldB, aplane, bplane, np, N, R, Rabs, stream));
+    CTR_TRY(launch_trace_rows((const TraceRow*)d_trow, ntr, (const float4* const*)d_tt,
+                              (const float4* const*)d_tt + np, ldA, ldB, np, N, R, Rabs, stream));
     CTR_TRY(launch_rowsum_coef_refine(R, Rabs, ntr, (const int*)d_csr, (const int*)d_csr + (nout + 1),
                                       (const int*)d_tix, (const float*)d_rcoef, nout, np,
                                       (double2*)out + (size_t)p0 * nout,

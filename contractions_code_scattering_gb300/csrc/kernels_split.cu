@@ -632,226 +632,29 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   }
 }
 
-// ------------------------------------------------ split GEMM, part tiles
-// Standard configuration with the real and imaginary parts of every output tile
-// as two tiles: part 0 accumulates Re = Xr Yr - Xi Yi, part 1 Im = Xr Yi + Xi Yr,
-// each in NL level accumulators of BN columns.  One part needs 256 of the 512
-// TMEM columns, so the accumulators are double-buffered: the epilogue of one
-// tile overlaps the MMAs of the next, which the combined tiles (all 512 columns)
-// cannot do.  Each part re-streams its operand stages (from L2).
-template <class C>
-__device__ __forceinline__ void issue_chunk_part(uint32_t tbuf, uint64_t adesc, uint64_t bdesc, bool first_chunk,
-                                                 int part) {
-  constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, C::BN, false);
-  constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, C::BN, true);
-#pragma unroll
-  for (int i = 0; i < C::NS; i++) {
-#pragma unroll
-    for (int j = 0; j + i < C::NS; j++) {
-      const int lvl = (i + j) < C::NL - 1 ? (i + j) : C::NL - 1;
-      const uint32_t accum = (!first_chunk || !(i == 0 && j <= C::NL - 1)) ? 1u : 0u;
-      const uint64_t ar = adesc + (uint64_t)(((i * 2 + 0) * C::A_SUB) >> 4);
-      const uint64_t ai = adesc + (uint64_t)(((i * 2 + 1) * C::A_SUB) >> 4);
-      const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * C::B_SUB) >> 4);
-      const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * C::B_SUB) >> 4);
-      const uint32_t d = tbuf + (uint32_t)(lvl * C::BN);
-      if (part == 0) {
-        umma_f16(d, ar, br, id_pos, accum);  // Re += Xr Yr
-        umma_f16(d, ai, bi, id_neg, 1u);     // Re -= Xi Yi
-      } else {
-        umma_f16(d, ar, bi, id_pos, accum);  // Im += Xr Yi
-        umma_f16(d, ai, br, id_pos, 1u);     // Im += Xi Yr
-      }
-    }
-  }
-}
-
-template <class C>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
-    split_gemm_parts_kernel(SplitGemmBatch g, int ntiles_total, int* __restrict__ err) {
-  static_assert(2 * C::NL * C::BN <= (int)TMEM_COLS, "two accumulator buffers must fit");
-  constexpr uint32_t BUF_COLS = TMEM_COLS / 2;
-  extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + NSTAGE * C::A_STAGE;
-  uint64_t* full = (uint64_t*)(smem + NSTAGE * (C::A_STAGE + C::B_STAGE));
-  uint64_t* empty = full + NSTAGE;
-  uint64_t* tfull = empty + NSTAGE;  // [2]
-  uint64_t* tempty = tfull + 2;      // [2]
-  uint64_t* drainb = tempty + 2;
-  uint32_t* tslot = (uint32_t*)(drainb + 1);
-  volatile int* status = (volatile int*)(tslot + 1);  // block-uniform decisions
-  int* sexp = (int*)(tslot + 4);                      // C::BN column exponents of the current tile
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int per_inst = g.mtiles * g.ntiles;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < NSTAGE; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    for (int b = 0; b < 2; b++) {
-      mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
-    }
-    mbar_init(drainb, 1);
-    fence_mbar_init();
-    status[0] = *(volatile int*)err;
-  }
-  __syncthreads();
-  if (status[0]) return;
-  if (warp == 0) {
-    tmem_alloc(tslot, TMEM_COLS);
-    tmem_relinquish();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tbase = *tslot;
-
-  if (warp == 0) {
-    if (lane == 0) {
-      uint32_t g_chunk = 0;
-      bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x) {
-        const int base = tile >> 1;
-        const int inst = base / per_inst, mt = (base % per_inst) / g.ntiles, nt = base % g.ntiles;
-        const SplitGemmInst* I = &g.inst[inst];
-        const uint8_t* gA = I->left + (size_t)mt * g.nchunk * C::A_STAGE;
-        const uint8_t* gB = I->right + (size_t)nt * g.nchunk * C::B_STAGE;
-        for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
-          const int s = g_chunk % NSTAGE;
-          if (g_chunk >= NSTAGE && !mbar_wait(&empty[s], ((g_chunk / NSTAGE) - 1) & 1, WAIT_NS, err)) {
-            atomicExch(err, 1);
-            ok = false;
-            break;
-          }
-          mbar_arrive_expect_tx(&full[s], C::A_STAGE + C::B_STAGE);
-          bulk_g2s(sA + s * C::A_STAGE, gA + (size_t)kc * C::A_STAGE, C::A_STAGE, &full[s]);
-          bulk_g2s(sB + s * C::B_STAGE, gB + (size_t)kc * C::B_STAGE, C::B_STAGE, &full[s]);
-        }
-      }
-    }
-  } else if (warp == 1) {
-    if (lane == 0) {
-      uint32_t g_chunk = 0, local = 0;
-      bool ok = true;
-      const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
-      const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
-      for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x, local++) {
-        const int b = local & 1;
-        // buffer b was last used by tile local-2: wait until the epilogue drained it
-        if (local >= 2 && !mbar_wait(&tempty[b], ((local >> 1) - 1) & 1, 2 * WAIT_NS, err)) {
-          atomicExch(err, 4);
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t tbuf = tbase + (uint32_t)b * BUF_COLS;
-        for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
-          const int s = g_chunk % NSTAGE;
-          if (!mbar_wait(&full[s], (g_chunk / NSTAGE) & 1, WAIT_NS, err)) {
-            atomicExch(err, 2);
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          issue_chunk_part<C>(tbuf, adesc0 + (uint64_t)((s * C::A_STAGE) >> 4),
-                              bdesc0 + (uint64_t)((s * C::B_STAGE) >> 4), kc == 0, tile & 1);
-          umma_commit(&empty[s]);
-        }
-        if (ok) umma_commit(&tfull[b]);
-      }
-      umma_commit(drainb);
-      if (!mbar_wait(drainb, 0, WAIT_NS)) atomicExch(err, 5);
-    }
-  } else {
-    const int q = warp & 3;
-    const int et = threadIdx.x - 64;
-    const int row = q * 32 + lane;
-    uint32_t local = 0;
-    for (int tile = blockIdx.x; tile < ntiles_total; tile += gridDim.x, local++) {
-      const int b = local & 1, part = tile & 1, base = tile >> 1;
-      const int inst = base / per_inst, mt = (base % per_inst) / g.ntiles, nt = base % g.ntiles;
-      const SplitGemmInst* I = &g.inst[inst];
-      epi_bar();
-      if (et < C::BN) sexp[et] = I->rexp[nt * C::BN + et];
-      const int grow = mt * SPLIT_M + row;
-      const bool rvalid = grow < g.mrows;
-      const float srow = pow2f(I->lexp[grow]);
-      if (et == 0) {
-        const bool done = mbar_wait(&tfull[b], (local >> 1) & 1, 4 * WAIT_NS, err);
-        if (!done) atomicExch(err, 3);
-        status[1] = done ? 0 : 1;
-      }
-      epi_bar();
-      if (status[1]) break;
-      tc_fence_after();
-      const uint32_t tl = tbase + (uint32_t)b * BUF_COLS + ((uint32_t)(q * 32) << 16);
-      float2* outp = (float2*)I->out + (part ? g.plane : 0);
-      const int ldo = g.ldo;
-      for (int c0 = 0; c0 < C::BN; c0 += 16) {
-        float v[C::NL][16];
-#pragma unroll
-        for (int l = 0; l < C::NL; l++) tmem_ld16(tl + (uint32_t)(l * C::BN + c0), v[l]);
-        tmem_ld_wait();
-        if (!rvalid) continue;
-#pragma unroll
-        for (int c = 0; c < 16; c++) {
-          const int gcol = nt * C::BN + c0 + c;
-          if (gcol >= g.ncols) continue;
-          // levels 0 .. NL-2 exact: exact two-sums; the last level and the rounding errors to the low word
-          float s = v[0][c], e = 0.f;
-#pragma unroll
-          for (int l = 1; l < C::NL - 1; l++) {
-            float t, d;
-            two_sum(s, v[l][c], t, d);
-            s = t;
-            e += d;
-          }
-          float hi, lo;
-          fast_two_sum(s, e + v[C::NL - 1][c], hi, lo);
-          const float sc = srow * pow2f(sexp[c0 + c]);
-          outp[(size_t)gcol * ldo + grow] = make_float2(hi * sc, lo * sc);
-        }
-      }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty[b]);
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) {
-    tc_fence_after();
-    tmem_dealloc(tbase, TMEM_COLS);
-  }
-}
-
 // ----------------------------------------------------------- closing traces
 // rows[q * nrows + r] = coef_r * sum_{i,j < nev} A(i,j) conj(B(i,j)) with
 // A = abase[q] + rt[r].aoff, B = bbase[q] + rt[r].boff, element (i, j) at
-// [j * ld + i] of the Re plane and plane elements further for Im (float-float).  One CTA of 128 threads per (pair, row),
+// [j * ld + i] (float-float complex).  One CTA of 128 threads per (pair, row),
 // rows of a pair adjacent so that the blocks they share are re-read from L2;
 // thread i walks column elements i (and i + 128) over all j and keeps its sum
 // in float-float.  The same pass accumulates |coef_r| sum |A|_1 |B|_1 (high
 // words, FP32; |z|_1 = |Re z| + |Im z|, within a factor 2 of the product of
 // moduli) into rabs.
 __global__ void __launch_bounds__(128) trace_rows_kernel(const TraceRow* __restrict__ rt, int nrows,
-                                                         const float2* const* __restrict__ abase,
-                                                         const float2* const* __restrict__ bbase, int lda, int ldb,
-                                                         size_t aplane, size_t bplane, int nev,
-                                                         double2* __restrict__ rows, double* __restrict__ rabs) {
+                                                         const float4* const* __restrict__ abase,
+                                                         const float4* const* __restrict__ bbase, int lda, int ldb,
+                                                         int nev, double2* __restrict__ rows,
+                                                         double* __restrict__ rabs) {
   const int q = blockIdx.x / nrows, r = blockIdx.x % nrows;
   const TraceRow T = rt[r];
-  const float2* pa = abase[q] + T.aoff;
-  const float2* pb = bbase[q] + T.boff;
+  const float4* pa = abase[q] + T.aoff;
+  const float4* pb = bbase[q] + T.boff;
   float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f, sa = 0.f;
   for (int i = threadIdx.x; i < nev; i += 128) {
     for (int j = 0; j < nev; j++) {
-      const float2 ar = pa[(size_t)j * lda + i], ai = pa[aplane + (size_t)j * lda + i];
-      const float2 br = pb[(size_t)j * ldb + i], bi = pb[bplane + (size_t)j * ldb + i];
-      const float4 a = make_float4(ar.x, ar.y, ai.x, ai.y), b = make_float4(br.x, br.y, bi.x, bi.y);
+      const float4 a = pa[(size_t)j * lda + i];
+      const float4 b = pb[(size_t)j * ldb + i];
       ff_mac(sr, er, a.x, a.y, b.x, b.y);    // + ar br
       ff_mac(sr, er, a.z, a.w, b.z, b.w);    // + ai bi
       ff_mac(si, ei, a.z, a.w, b.x, b.y);    // + ai br
@@ -964,36 +767,8 @@ static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err,
   return CTR_OK;
 }
 
-template <class C>
-static int launch_split_gemm_parts(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
-  const size_t smem = gemm_smem_bytes<C>();
-  static bool attr = false;
-  if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(split_gemm_parts_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    attr = true;
-  }
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    CTR_CUDA(cudaGetDevice(&dev));
-    CTR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
-  const long long total = 2LL * ninst * g.mtiles * g.ntiles;
-  if (total > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
-  const int grid = (int)std::min<long long>(total, nsm);
-  TimedLaunch tl(s, "split_gemm");
-  split_gemm_parts_kernel<C><<<grid, GEMM_THREADS, smem, s>>>(g, (int)total, d_err);
-  CTR_CUDA(cudaGetLastError());
-  return CTR_OK;
-}
-
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
   if (ninst == 0) return CTR_OK;
-  if (g.parts) {
-    if (g.hp || g.out_mode != 0 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: part tiles write float-float planes");
-    return launch_split_gemm_parts<CfgStd>(g, ninst, d_err, s);
-  }
   if (g.hp) {
     if (g.out_mode != 1 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: the high-precision tiles write complex128");
     return launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");
@@ -1001,15 +776,13 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
   return launch_split_gemm_cfg<CfgStd>(g, ninst, d_err, s, "split_gemm");
 }
 
-int launch_trace_rows(const TraceRow* d_rows, int nrows, const float2* const* d_abase, const float2* const* d_bbase,
-                      int lda, int ldb, size_t aplane, size_t bplane, int npair, int nev, double2* rows, double* rabs,
-                      cudaStream_t s) {
+int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
+                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, cudaStream_t s) {
   if (npair == 0 || nrows == 0) return CTR_OK;
   const long long nblk = (long long)npair * nrows;
   if (nblk > 0x7fffffffLL) return fail(CTR_ERR_ARG, "traces: grid too large");
   TimedLaunch tl(s, "trace_rows");
-  trace_rows_kernel<<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, aplane, bplane, nev,
-                                                  rows, rabs);
+  trace_rows_kernel<<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

@@ -76,10 +76,6 @@ struct SplitGemmBatch {
   int out_mode;      // 0: float-float column-major, 1: complex128 row-major blocks
   int blkn;          // out_mode 1: columns (and row stride) of one output block
   int hp;            // 0: CfgStd operands and tiles, 1: CfgHP (out_mode 1 only)
-  int parts;         // 1: CfgStd with the real and imaginary parts as separate tiles and
-                     // double-buffered accumulators; output two float2 (hi, lo) planes,
-                     // Re at ((float2*)out)[c * ldo + r] and Im at plane elements further
-  size_t plane;      // parts: float2 elements between the Re and the Im plane
 };
 
 // Operands of the task form C = sum_q w_q op(A_q) op(B_q) (q < nterm <= 4),
@@ -138,12 +134,10 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
 // Closing traces over npair pairs: products of pair q at a_base[q] / b_base[q]
-// (float2 planes, leading dimensions lda / ldb, Im plane aplane / bplane
-// elements after Re); rows[q * nrows + r] = coef_r * trace and
+// (leading dimensions lda / ldb); rows[q * nrows + r] = coef_r * trace and
 // rabs[q * nrows + r] = |coef_r| sum |A|_1 |B|_1.
-int launch_trace_rows(const TraceRow* d_rows, int nrows, const float2* const* d_abase, const float2* const* d_bbase,
-                      int lda, int ldb, size_t aplane, size_t bplane, int npair, int nev, double2* rows, double* rabs,
-                      cudaStream_t s);
+int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
+                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, cudaStream_t s);
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s);
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 
