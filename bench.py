@@ -38,6 +38,9 @@ def parse():
     ap.add_argument("--engine", default="auto", choices=["auto", "split", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine (0 = skip)")
     ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--graph", type=int, default=1, help="time replays of the step recorded as a CUDA graph "
+                    "(the eager calls are timed beside them); 0 = eager calls only")
+    ap.add_argument("--tune", type=int, default=1, help="autotune the knobs on the first warm-up step")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--nt", type=int, default=None, help="time extent (default: the workload's; a smaller value "
                                                               "gives a small case of the same kernels, e.g. for ncu)")
@@ -270,37 +273,62 @@ def main():
 
     tau, phi = make_inputs(nt, nev, moms)
     out = torch.empty((nt, nt, nout), dtype=torch.complex128, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a created stream (graphs cannot be recorded on the legacy default stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
 
     def step(eng, o=out):
         api.twosided(tau, phi, rows, coef, oi, nout, engine=eng, out=o)
 
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
+        if w == 0 and args.tune:
+            api.tune_set_mode(1)  # the autotuner measures its knobs on this step's live data
         step(engine)
+        if w == 0 and args.tune:
+            torch.cuda.synchronize()
+            api.tune_set_mode(0)
     torch.cuda.synchronize()
     barrier(ws)
 
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = _lib.launch_count()
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+        return allmax(ws, e0.elapsed_time(e1) / 1e3), _lib.launch_count() - n0
+
     clocks = ClockSampler(local)
     clocks.start()
+    # eager calls, with per-kernel CUDA-event timing (the roofline's source)
     _lib.timing_enable(True)
-    n0 = _lib.launch_count()
-    torch.cuda.synchronize()
-    barrier(ws)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        step(engine)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier(ws)
-    launches = _lib.launch_count() - n0
-    refined = int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
+    t_eager, launches_eager = timed(lambda: step(engine), args.steps)
     report = _lib.timing_report()
+    _lib.timing_enable(False)
+    eager = {"ms_per_step": 1e3 * t_eager / args.steps, "value": ws * diagrams * args.steps / t_eager,
+             "gpu_launches": int(launches_eager)}
+    graph_info = None
+    if args.graph:
+        # the same step recorded once as a CUDA graph and replayed
+        with api.Graph(stream) as g:
+            step(engine)
+        g.launch(stream)
+        nseg, nker, nbytes = g.info()
+        elapsed, launches = timed(lambda: g.launch(stream), args.steps)
+        graph_info = {"segments": nseg, "kernels_per_replay": nker, "device_bytes": nbytes,
+                      "speedup_vs_eager": t_eager / elapsed}
+    else:
+        elapsed, launches = t_eager, launches_eager
+    refined = int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
     clk = clocks.stop()
-    elapsed = allmax(ws, ev0.elapsed_time(ev1) / 1e3)
     ms_per_step = 1e3 * elapsed / args.steps
     value = ws * diagrams * args.steps / elapsed
-    _lib.timing_enable(False)
+    tuned = api.tune_report()
 
     res_main = out.cpu().numpy()
 
@@ -365,6 +393,17 @@ def main():
                 buf_phi[b].copy_(h_phi, non_blocking=True)
                 copied[b].record(cs)
 
+        graphs = None
+        if args.graph:
+            # one recorded step per input buffer (recorded before the timed region)
+            graphs = []
+            for b in range(2):
+                with api.Graph(stream) as gb:
+                    api.twosided(buf_tau[b], buf_phi[b], rows, coef, oi, nout, engine=engine, out=out)
+                graphs.append(gb)
+            torch.cuda.synchronize()
+            barrier(ws)
+            e0.record(stream)
         cs.wait_event(e0)
         load(0)
         for i in range(K):
@@ -374,7 +413,10 @@ def main():
                     cs.wait_event(freed[1 - b])
                 load(1 - b)
             stream.wait_event(copied[b])
-            api.twosided(buf_tau[b], buf_phi[b], rows, coef, oi, nout, engine=engine, out=out)
+            if graphs:
+                graphs[b].launch(stream)
+            else:
+                api.twosided(buf_tau[b], buf_phi[b], rows, coef, oi, nout, engine=engine, out=out)
             freed[b].record(stream)
             h_out[i].copy_(out, non_blocking=True)
         e1.record(stream)
@@ -384,7 +426,11 @@ def main():
                "h2d_bytes_per_step": int(h_tau.numel() * 16 + h_phi.numel() * 16),
                "d2h_bytes_per_step": int(out.numel() * 16), "ms_per_step": 1e3 * te,
                "pipelining": "inputs of step i+1 copied on a second stream while step i computes", "steps": K,
+               "graph": bool(args.graph),
                "h2d_tau_alone_ms": 1e3 * h2d_alone, "h2d_tau_alone_gbs": h_tau.numel() * 16 / h2d_alone / 1e9}
+        if graphs:
+            for gb in graphs:
+                gb.close()
         del h_tau, h_phi, h_out, buf_tau, buf_phi
 
     # CPU baseline (the oracle, reference chain order) on a bounded sample; the
@@ -411,6 +457,7 @@ def main():
                    "diagrams_per_step": diagrams, "l2": "inputs larger than L2 (tau 10.5 GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
+        "graph": graph_info, "eager": eager, "autotune": tuned,
         "kernels": {k: {"launches": v[0], "ms": v[2]} for k, v in report.items()},
         "fp64_engine": fp64, "parity_vs_oracle_sample": parity,
         "split_refined_entries_per_step": refined,
@@ -513,12 +560,28 @@ def run_rho_small(args):
     mom5 = np.ascontiguousarray(np.stack([synth.make_phi_hermitian(nt, nev, SEED + 2)] +
                                          [synth.make_phi_random(nt, nev, rng) for _ in range(4)], axis=1))
     dp, dm = torch.from_numpy(prop).cuda(), torch.from_numpy(mom5).cuda()
+    stream = torch.cuda.Stream()  # a created stream, so that the step can be recorded as a graph
+    torch.cuda.set_stream(stream)
     res = {}
     for eng in ("fp64", "split"):
-        t, launches, kern = _timed(lambda: api.run_contract_rho(dp, dm, engine=eng), args.steps, args.warmup)
-        got = api.run_contract_rho(dp, dm, engine=eng).cpu().numpy()[:, :, 0, :]
+        out = torch.empty((nt, nt, 16, 3), dtype=torch.complex128, device="cuda")
+        if args.tune:
+            api.tune_set_mode(1)
+            api.run_contract_rho(dp, dm, engine=eng, out=out)
+            torch.cuda.synchronize()
+            api.tune_set_mode(0)
+        t, launches, kern = _timed(lambda: api.run_contract_rho(dp, dm, engine=eng, out=out), args.steps, args.warmup)
+        got = out.cpu().numpy()
         res[eng] = {"value": nt * nt * 3 / t, "ms_per_step": 1e3 * t, "gpu_launches": launches}
-        res[eng]["out"] = got
+        if args.graph:
+            with api.Graph(stream) as g:
+                api.run_contract_rho(dp, dm, engine=eng, out=out)
+            tg, lg, _ = _timed(lambda: g.launch(stream), args.steps, args.warmup)
+            same = bool(np.array_equal(out.cpu().numpy(), got))
+            res[eng]["graph"] = {"value": nt * nt * 3 / tg, "ms_per_step": 1e3 * tg, "gpu_launches": lg,
+                                 "speedup_vs_eager": t / tg, "segments": g.info()[0], "bitwise_equal_to_eager": same}
+            g.close()
+        res[eng]["out"] = got[:, :, 0, :]
     t0 = time.perf_counter()
     ref = O.rho(prop, mom5)[:, :, 0, :]
     tcpu = time.perf_counter() - t0
@@ -528,7 +591,8 @@ def run_rho_small(args):
             "split": {k: v for k, v in res["split"].items() if k != "out"},
             "fp64_vs_oracle": _errs(res["fp64"]["out"], ref), "split_vs_oracle": _errs(res["split"]["out"], ref),
             "cpu_baseline": {"value": nt * nt * 768 / 16 / tcpu, "unit": "diagrams/s", "cores": os.cpu_count(),
-                             "kind": "port", "sample": "all 16 x 16 pairs, all 48 outputs (768 spin rows)"}}
+                             "kind": "port", "sample": "all 16 x 16 pairs, all 48 outputs (768 spin rows)"},
+            "autotune": api.tune_report()}
     print(json.dumps(line))
 
 

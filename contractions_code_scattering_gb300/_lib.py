@@ -67,6 +67,19 @@ def lib(build_if_missing=True):
     L.ctr_chain_adjoint.argtypes = [i, i, i, i, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]
     L.ctr_rho_profile_vjp.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp, vp]
     L.ctr_pipi_profile_vjp.argtypes = [i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.ctr_graph_begin.argtypes = [vp]
+    L.ctr_graph_end.argtypes = [vp, ctypes.POINTER(vp)]
+    L.ctr_graph_launch.argtypes = [vp, vp]
+    L.ctr_graph_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_longlong),
+                                 ctypes.POINTER(ctypes.c_longlong)]
+    L.ctr_graph_destroy.argtypes = [vp]
+    L.ctr_graph_destroy.restype = None
+    L.ctr_tune_set_mode.argtypes = [i]
+    L.ctr_tune_force.argtypes = [ctypes.c_char_p, i]
+    L.ctr_tune_report.argtypes = [ctypes.c_char_p, i]
+    L.ctr_tune_clear.restype = None
+    L.ctr_tune_save.argtypes = [ctypes.c_char_p]
+    L.ctr_tune_load.argtypes = [ctypes.c_char_p]
     _LIB = L
     return L
 

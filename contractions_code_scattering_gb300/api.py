@@ -136,47 +136,54 @@ def _rows(tf_range, nt):
     return tf_range if tf_range is not None else (0, nt)
 
 
-def run_contract_rhopi(prop_rows, diag, p1, p2, mom5_p1p2, idir, engine="fp64", tf_range=None, stream=None):
+def run_contract_rhopi(prop_rows, diag, p1, p2, mom5_p1p2, idir, engine="fp64", tf_range=None, out=None,
+                       stream=None):
     """rho -> pi pi (run_ContractRhoPi): corr [rows, Nt, 4]."""
     import torch
     nt, nev = p1.shape[0], p1.shape[-1]
     tf0, tf1 = _rows(tf_range, nt)
-    out = torch.empty((tf1 - tf0, nt, 4), dtype=torch.complex128, device=p1.device)
+    if out is None:
+        out = torch.empty((tf1 - tf0, nt, 4), dtype=torch.complex128, device=p1.device)
     check(lib().ctr_rhopi(_engine(engine), nev, nt, tf0, tf1, idir, _dev(prop_rows, "prop_rows"), _dev(diag, "diag"),
                           _dev(p1, "p1"), _dev(p2, "p2"), _dev(mom5_p1p2, "mom5_p1p2"), _dev(out, "out"),
                           _stream(stream)))
     return out
 
 
-def run_contract_pipi(prop_rows, diag, p1, p2, p3, p4, isospin, engine="fp64", tf_range=None, stream=None):
+def run_contract_pipi(prop_rows, diag, p1, p2, p3, p4, isospin, engine="fp64", tf_range=None, out=None,
+                      stream=None):
     """pi pi -> pi pi (run_ContractPiPi / run_ContractPiPi_I0; isospin 1 or 0): corr [rows, Nt, 5]."""
     import torch
     nt, nev = p1.shape[0], p1.shape[-1]
     tf0, tf1 = _rows(tf_range, nt)
-    out = torch.empty((tf1 - tf0, nt, 5), dtype=torch.complex128, device=p1.device)
+    if out is None:
+        out = torch.empty((tf1 - tf0, nt, 5), dtype=torch.complex128, device=p1.device)
     check(lib().ctr_pipi(_engine(engine), nev, nt, tf0, tf1, isospin, _dev(prop_rows, "prop_rows"), _dev(diag, "diag"),
                          _dev(p1, "p1"), _dev(p2, "p2"), _dev(p3, "p3"), _dev(p4, "p4"), _dev(out, "out"),
                          _stream(stream)))
     return out
 
 
-def run_contract_loop_unity(diag, mom, engine="fp64", stream=None):
+def run_contract_loop_unity(diag, mom, engine="fp64", out=None, stream=None):
     """Loop-unity (run_ContractLoopUnity): loop [Nt]."""
     import torch
     nt, nev = mom.shape[0], mom.shape[-1]
-    out = torch.empty((nt,), dtype=torch.complex128, device=mom.device)
+    if out is None:
+        out = torch.empty((nt,), dtype=torch.complex128, device=mom.device)
     check(lib().ctr_loop_unity(_engine(engine), nev, nt, _dev(diag, "diag"), _dev(mom, "mom"), _dev(out, "out"),
                                _stream(stream)))
     return out
 
 
-def run_contract_sigmapi(prop_rows, diag, p1, p2, mom2_p1p2, engine="fp64", tf_range=None, stream=None):
-    """sigma -> pi pi (hor fish + triangle): (hor_fish [Nt], triangle [rows, Nt, 2])."""
+def run_contract_sigmapi(prop_rows, diag, p1, p2, mom2_p1p2, engine="fp64", tf_range=None, out=None, stream=None):
+    """sigma -> pi pi (hor fish + triangle): (hor_fish [Nt], triangle [rows, Nt, 2]); out = (hf, tri) or None."""
     import torch
     nt, nev = p1.shape[0], p1.shape[-1]
     tf0, tf1 = _rows(tf_range, nt)
-    hf = torch.empty((nt,), dtype=torch.complex128, device=p1.device)
-    tri = torch.empty((tf1 - tf0, nt, 2), dtype=torch.complex128, device=p1.device)
+    if out is None:
+        out = (torch.empty((nt,), dtype=torch.complex128, device=p1.device),
+               torch.empty((tf1 - tf0, nt, 2), dtype=torch.complex128, device=p1.device))
+    hf, tri = out
     check(lib().ctr_sigmapi(_engine(engine), nev, nt, tf0, tf1, _dev(prop_rows, "prop_rows"), _dev(diag, "diag"),
                             _dev(p1, "p1"), _dev(p2, "p2"), _dev(mom2_p1p2, "mom2_p1p2"), _dev(hf, "hor_fish"),
                             _dev(tri, "triangle"), _stream(stream)))
@@ -197,6 +204,89 @@ def zgemm_batched(x, y, engine="fp64", out=None, stream=None):
     pc = (ctypes.c_void_p * nb)(*[out.data_ptr() + b * stride for b in range(nb)])
     check(lib().ctr_zgemm_batched(_engine(engine), n, nb, px, py, pc, _stream(stream)))
     return out
+
+
+class Graph:
+    """Library calls recorded once on a stream and replayed (include/ctr.h: ctr_graph_*).
+
+        corr = torch.empty(...)           # outputs allocated before recording
+        with api.Graph(stream) as g:      # records; nothing executes
+            api.run_contract_rho(prop_rows, mom5, engine="split", out=corr, stream=stream)
+        g.launch(stream)                  # replays; any number of times
+
+    A replay reads the device tensors passed while recording (with the contents
+    they hold at replay time) and writes the same outputs, so keep them alive
+    and refill them in place.  Allocate every tensor before recording (pass
+    out=): the stream is capturing while the block runs.  The split engine's recomputation of
+    ill-conditioned entries runs between graph segments at every launch."""
+
+    def __init__(self, stream=None):
+        self._stream = stream
+        self._g = None
+
+    def __enter__(self):
+        check(lib().ctr_graph_begin(_stream(self._stream)))
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        g = ctypes.c_void_p()
+        rc = lib().ctr_graph_end(_stream(self._stream), ctypes.byref(g))
+        if exc_type is None:
+            check(rc)
+            self._g = g
+        return False
+
+    def launch(self, stream=None):
+        if self._g is None:
+            raise CtrError(-1, "graph was not recorded")
+        check(lib().ctr_graph_launch(self._g, _stream(stream if stream is not None else self._stream)))
+
+    def info(self):
+        """(segments, kernel nodes per replay, device bytes owned)."""
+        ns, nk, nb = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().ctr_graph_info(self._g, ctypes.byref(ns), ctypes.byref(nk), ctypes.byref(nb)))
+        return ns.value, nk.value, nb.value
+
+    def close(self):
+        if self._g is not None:
+            lib().ctr_graph_destroy(self._g)
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tune_set_mode(mode):
+    """0: cached choices or defaults; 1: measure keys met for the first time; 2: re-measure."""
+    check(lib().ctr_tune_set_mode(int(mode)))
+
+
+def tune_force(knob, value):
+    """Pin a knob ("twosided.batch", "trace_rows", "split_gemm.order") to a value; -1 releases it."""
+    check(lib().ctr_tune_force(knob.encode(), int(value)))
+
+
+def tune_report():
+    """{"knob|shape": {"choice": c, "ms": [...]}} of the autotuner's table."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(lib().ctr_tune_report(buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
+def tune_clear():
+    lib().ctr_tune_clear()
+
+
+def tune_save(path):
+    check(lib().ctr_tune_save(str(path).encode()))
+
+
+def tune_load(path):
+    check(lib().ctr_tune_load(str(path).encode()))
 
 
 def sync(stream=None):

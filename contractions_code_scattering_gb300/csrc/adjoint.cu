@@ -475,6 +475,7 @@ int ctr_apply_profile(int nev, long long nmat, const double* f, const double* sr
 int ctr_chain_adjoint(int engine, int nev, int nt, int nphi, const double* prop, const double* phi, const double* f,
                       int nchain, const int* chain_off, const ctr_factor* factors, const double* w, double* values,
                       double* grad, void* stream) {
+  CTR_NO_CAPTURE("ctr_chain_adjoint");
   cudaStream_t s = (cudaStream_t)stream;
   CTR_TRY(check_engine(engine, nev));
   if (nev < 1 || nt < 1 || nphi < 0 || nchain < 0 || !prop || !f || !chain_off || !factors || (!values && !grad))
@@ -498,6 +499,7 @@ int ctr_chain_adjoint(int engine, int nev, int nt, int nphi, const double* prop,
 
 int ctr_rho_profile_vjp(int engine, int nev, int nt, const double* prop, const double* mom5, const double* f,
                         const double* w, double* corr, double* grad, void* stream) {
+  CTR_NO_CAPTURE("ctr_rho_profile_vjp");
   cudaStream_t s = (cudaStream_t)stream;
   CTR_TRY(check_engine(engine, nev));
   if (nev < 1 || nt < 1 || !prop || !mom5 || !f || !w || (!corr && !grad))
@@ -565,6 +567,7 @@ int ctr_rho_profile_vjp(int engine, int nev, int nt, const double* prop, const d
 int ctr_pipi_profile_vjp(int engine, int nev, int nt, int isospin, const double* prop, const double* p1,
                          const double* p2, const double* p3, const double* p4, const double* f, const double* w,
                          double* corr, double* grad, void* stream) {
+  CTR_NO_CAPTURE("ctr_pipi_profile_vjp");
   cudaStream_t s = (cudaStream_t)stream;
   CTR_TRY(check_engine(engine, nev));
   if (nev < 1 || nt < 1 || !prop || !p1 || !p2 || !p3 || !p4 || !f || !w || (!corr && !grad))

@@ -215,6 +215,7 @@ using namespace ctr;
 extern "C" {
 
 int ctr_contract_init(int nev, int nt, int dev) {
+  CTR_NO_CAPTURE("ctr_contract_init");
   if (g_on) return fail(CTR_ERR_ARG, "initContract can be called once only");
   if (nev < 1 || nt < 1) return fail(CTR_ERR_ARG, "Nev=%d, Nt=%d invalid", nev, nt);
   CTR_TRY(ctr_device_init(dev));
@@ -226,6 +227,7 @@ int ctr_contract_init(int nev, int nt, int dev) {
 }
 
 int ctr_contract_destroy(void) {
+  CTR_NO_CAPTURE("ctr_contract_destroy");
   if (!g_on) return fail(CTR_ERR_ARG, "cannot destroy contract library because is not on");
   ctr_release_workspace();
   g_on = false;
@@ -234,6 +236,7 @@ int ctr_contract_destroy(void) {
 
 // Perambulator file -> host buffer [t1][t2][s1][s2][v1][v2] complex (lib/contract.cpp:91-160).
 int ctr_read_prop(const char* path, int nev, int nt, int single, void* host_out) {
+  CTR_NO_CAPTURE("ctr_read_prop");
   if (!path || !host_out || nev < 1 || nt < 1) return fail(CTR_ERR_ARG, "ctr_read_prop: bad arguments");
   FILE* f = std::fopen(path, "rb");
   if (!f) return fail(CTR_ERR_IO, "cannot find file %s for reading the perambulator", path);
@@ -303,6 +306,7 @@ int ctr_read_momenta(const char* path, int nmom, int momcomb, int* p) {
 }
 
 int ctr_calculate_rho(int nev, int nt, const void* prop, const double* mom, int single, const char* outfile) {
+  CTR_NO_CAPTURE("ctr_calculate_rho");
   CTR_TRY(check_on(nev, nt));
   File F;
   CTR_TRY(open_out(outfile, F));
@@ -330,6 +334,7 @@ int ctr_calculate_rho(int nev, int nt, const void* prop, const double* mom, int 
 
 int ctr_calculate_rhopi(int idir, int nev, int nt, const void* prop, const double* p1, const double* p2,
                         const double* p1p2, int single, const char* outfile) {
+  CTR_NO_CAPTURE("ctr_calculate_rhopi");
   CTR_TRY(check_on(nev, nt));
   File F;
   CTR_TRY(open_out(outfile, F));
@@ -358,6 +363,7 @@ int ctr_calculate_rhopi(int idir, int nev, int nt, const void* prop, const doubl
 
 int ctr_calculate_pipi(int nev, int nt, const void* prop, const double* p1, const double* p2, const double* p3,
                        const double* p4, int single, const char* outfile, int isospin) {
+  CTR_NO_CAPTURE("ctr_calculate_pipi");
   CTR_TRY(check_on(nev, nt));
   if (isospin != 0 && isospin != 1) return fail(CTR_ERR_ARG, "This Isospin is not implemeted");
   File F;
@@ -389,6 +395,7 @@ int ctr_calculate_pipi(int nev, int nt, const void* prop, const double* p1, cons
 }
 
 int ctr_calculate_sigma(int nev, int nt, const void* prop, const double* mom, int single, const char* outfile) {
+  CTR_NO_CAPTURE("ctr_calculate_sigma");
   CTR_TRY(check_on(nev, nt));
   File F;
   CTR_TRY(open_out(outfile, F));
@@ -428,6 +435,7 @@ int ctr_calculate_sigma(int nev, int nt, const void* prop, const double* mom, in
 
 int ctr_calculate_sigmapi(int nev, int nt, const void* prop, const double* p1, const double* p2,
                           const double* p1p2, int single, const char* outfile) {
+  CTR_NO_CAPTURE("ctr_calculate_sigmapi");
   CTR_TRY(check_on(nev, nt));
   File F;
   CTR_TRY(open_out(outfile, F));

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -91,6 +92,7 @@ enum {
   WS_SPLITJOBS,     // their job / instance / pointer tables
   WS_SPLITJOBS2,
   WS_SPLITJOBS3,
+  WS_RPHI,          // per-time-slice products of a recomputation call
   WS_COUNT
 };
 
@@ -111,11 +113,46 @@ int zgemm_split_batched(int N, int nb, const double* const* x, const double* con
 struct ZTask;
 int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream);
 
+// ------------------------------------------------------------ graph capture
+// A host step that reads device results (e.g. the split engine's refinement
+// list).  Run at once by eager calls; while the thread records a graph, it ends
+// the current graph segment and runs after that segment at every launch, on the
+// launch stream.  Steps capture what they need by value.
+using HostStep = std::function<int(cudaStream_t)>;
+int host_step(cudaStream_t s, HostStep fn);
+bool capturing();
+#define CTR_NO_CAPTURE(name)                                                                         \
+  do {                                                                                               \
+    if (::ctr::capturing())                                                                          \
+      return ::ctr::fail(CTR_ERR_UNSUPPORTED, "%s reads device data on the host to plan its work and " \
+                         "cannot be recorded into a graph", name);                                   \
+  } while (0)
+// One-time device state needed before a capture (error flag, kernel attributes).
+int prepare_for_capture();
+
+// ---------------------------------------------------------------- autotuner
+// Knob choices keyed by "knob|shape" (tune.cpp).  tune_mode() is 0 while the
+// thread records a graph.  tune_resolve returns the forced value, the cached
+// choice, a fresh measurement of run(c) for c < ncand (mode >= 1), or dflt.
+int tune_mode();
+std::string tune_key(const char* knob, const std::string& shape);
+int tune_forced(const char* knob);
+bool tune_lookup(const std::string& key, int* choice);
+void tune_store(const std::string& key, int choice, const std::vector<double>& ms);
+int tune_resolve(const char* knob, const std::string& shape, int ncand, int dflt, cudaStream_t s,
+                 const std::function<int(int)>& run, int* choice);
+
 // Upload a host array into a workspace slot (async on stream, host buffer is
 // kept alive by a pinned staging copy owned by the slot).
 int upload(int slot, const void* host, size_t bytes, void** dev, cudaStream_t stream);
 // dst (device) <- src (device-accessible, e.g. mapped pinned host memory), by a kernel.
 int launch_stage_copy(void* dst, const void* src, size_t bytes, cudaStream_t stream);
+// dst <- src for any alignment (a kernel; dst may be mapped pinned host memory).
+int launch_readback(void* dst, const void* src, size_t bytes, cudaStream_t stream);
+// Reads a small device result into host memory through a mapped pinned buffer
+// written by a kernel (never queued behind copy-engine transfers that a caller
+// runs on other streams); synchronises the stream.  Not usable while recording.
+int download(void* host, const void* dev, size_t bytes, cudaStream_t stream);
 
 // ------------------------------------------------------- two-sided plan
 struct TwoSidedRow {

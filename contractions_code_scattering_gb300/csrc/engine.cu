@@ -243,6 +243,7 @@ int ctr_source_average(int nt, int ncorr, const double* corr, double scale, doub
 }
 
 int ctr_sync(void* stream) {
+  CTR_NO_CAPTURE("ctr_sync");
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return ctr::cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
   return ctr::split_error_check((cudaStream_t)stream);

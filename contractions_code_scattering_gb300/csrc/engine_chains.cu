@@ -185,34 +185,38 @@ int refine_begin(const Ctx& c, size_t nentries, int slot, Refine& r) {
   return CTR_OK;
 }
 
-// Flagged entries e -> units e / nout (pairs or time slices); rerun(units, out)
-// writes their FP64 values as [units][nout] into out (device); they are then
-// scattered over corr.  Returns the number of entries recomputed.
+// Flagged entries e -> units e / nout (pairs or time slices); rerun(units, out,
+// stream) writes their FP64 values as [units][nout] into out (device); they are
+// then scattered over corr, and their number is added to g_refined_last.  The
+// list is read on the host, so under graph recording this runs after the
+// recorded kernels at every launch (the closure holds copies of what it needs).
 template <typename Rerun>
-int refine_end(const Ctx& c, const Refine& r, int nout, int slot, double2* corr, long long* nref, Rerun&& rerun) {
+int refine_end(const Ctx& c, const Refine& r, int nout, int slot, double2* corr, Rerun rerun) {
   if (!r.on) return CTR_OK;
-  int n = 0;
-  CTR_CUDA(cudaMemcpyAsync(&n, r.count, sizeof(int), cudaMemcpyDeviceToHost, c.s));
-  CTR_CUDA(cudaStreamSynchronize(c.s));
-  if (n == 0) return CTR_OK;
-  std::vector<int> list(n);
-  CTR_CUDA(cudaMemcpyAsync(list.data(), r.list, n * sizeof(int), cudaMemcpyDeviceToHost, c.s));
-  CTR_CUDA(cudaStreamSynchronize(c.s));
-  std::vector<int> units;
-  for (int e : list) units.push_back(e / nout);
-  std::sort(units.begin(), units.end());
-  units.erase(std::unique(units.begin(), units.end()), units.end());
-  void* tmp;
-  CTR_TRY(workspace(slot).get(units.size() * nout * sizeof(double2), &tmp));
-  CTR_TRY(rerun(units, (double2*)tmp));
-  std::vector<int> where(units.size() * nout);
-  for (size_t q = 0; q < units.size(); q++)
-    for (int o = 0; o < nout; o++) where[q * nout + o] = units[q] * nout + o;
-  void* dw;
-  CTR_TRY(upload(WS_TASKS, where.data(), where.size() * sizeof(int), &dw, c.s));
-  CTR_TRY(launch_scatter((const int*)dw, (const double2*)tmp, (int)where.size(), corr, c.s));
-  *nref += (long long)where.size();
-  return CTR_OK;
+  const int* count = r.count;
+  const int* flagged = r.list;
+  return host_step(c.s, [=](cudaStream_t s) -> int {
+    int n = 0;
+    CTR_TRY(download(&n, count, sizeof(int), s));
+    if (n == 0) return CTR_OK;
+    std::vector<int> list(n);
+    CTR_TRY(download(list.data(), flagged, n * sizeof(int), s));
+    std::vector<int> units;
+    for (int e : list) units.push_back(e / nout);
+    std::sort(units.begin(), units.end());
+    units.erase(std::unique(units.begin(), units.end()), units.end());
+    void* tmp;
+    CTR_TRY(workspace(slot).get(units.size() * nout * sizeof(double2), &tmp));
+    CTR_TRY(rerun(units, (double2*)tmp, s));
+    std::vector<int> where(units.size() * nout);
+    for (size_t q = 0; q < units.size(); q++)
+      for (int o = 0; o < nout; o++) where[q * nout + o] = units[q] * nout + o;
+    void* dw;
+    CTR_TRY(upload(WS_TASKS, where.data(), where.size() * sizeof(int), &dw, s));
+    CTR_TRY(launch_scatter((const int*)dw, (const double2*)tmp, (int)where.size(), corr, s));
+    g_refined_last += (long long)where.size();
+    return CTR_OK;
+  });
 }
 
 int batch_pairs(size_t per_pair, int npairs) {
@@ -227,6 +231,7 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
               const double* p1, const double* p2, const double* p3, const double* p4, double* corr, cudaStream_t s,
               int engine, const std::vector<int>* plist) {
   Ctx c{N, Nt, (size_t)N * N, s, engine};
+  if (engine == CTR_ENGINE_SPLIT && !plist) g_refined_last = 0;
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)p1, *P2 = (const double2*)p2, *P3 = (const double2*)p3,
@@ -338,13 +343,11 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
       CTR_CUDA(cudaGetLastError());
     }
   }
-  long long nref = 0;
-  CTR_TRY(refine_end(c, rf, 5, WS_REFINE, (double2*)corr, &nref, [&](const std::vector<int>& pairs, double2* out) {
-    return pipi_chain(N, Nt, tf_begin, tf_end, iso, prop_rows, prop_diag, p1, p2, p3, p4, (double*)out, s,
-                      CTR_ENGINE_FP64, &pairs);
-  }));
-  if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
-  return CTR_OK;
+  return refine_end(c, rf, 5, WS_REFINE, (double2*)corr,
+                    [=](const std::vector<int>& pairs, double2* out, cudaStream_t ls) {
+                      return pipi_chain(N, Nt, tf_begin, tf_end, iso, prop_rows, prop_diag, p1, p2, p3, p4,
+                                        (double*)out, ls, CTR_ENGINE_FP64, &pairs);
+                    });
 }
 
 // ---------------------------------------------------------------- rho pipi
@@ -356,6 +359,7 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
                 const std::vector<int>* plist) {
   if (idir < 0 || idir > 2) return fail(CTR_ERR_ARG, "idir %d not in {0,1,2}", idir);
   Ctx c{N, Nt, (size_t)N * N, s, engine};
+  if (engine == CTR_ENGINE_SPLIT && !plist) g_refined_last = 0;
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)mp1, *P2 = (const double2*)mp2, *P12 = (const double2*)mom5;
@@ -444,13 +448,11 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
       CTR_TRY(launch_rowsum(TR, ngrp, (const int*)d_csr, (const int*)d_csr + 5, 4, np,
                             (double2*)corr + (size_t)p0 * 4, 4, s));
   }
-  long long nref = 0;
-  CTR_TRY(refine_end(c, rf, 4, WS_REFINE, (double2*)corr, &nref, [&](const std::vector<int>& pairs, double2* out) {
-    return rhopi_chain(N, Nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mp1, mp2, mom5, (double*)out, s,
-                       CTR_ENGINE_FP64, &pairs);
-  }));
-  if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
-  return CTR_OK;
+  return refine_end(c, rf, 4, WS_REFINE, (double2*)corr,
+                    [=](const std::vector<int>& pairs, double2* out, cudaStream_t ls) {
+                      return rhopi_chain(N, Nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mp1, mp2, mom5,
+                                         (double*)out, ls, CTR_ENGINE_FP64, &pairs);
+                    });
 }
 
 // -------------------------------------------------------------- sigma pipi
@@ -462,6 +464,7 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
                   const double* mp1, const double* mp2, const double* mom2, double* hor_fish, double* tri,
                   cudaStream_t s, int engine, const std::vector<int>* plist, const std::vector<int>* tlist) {
   Ctx c{N, Nt, (size_t)N * N, s, engine};
+  if (engine == CTR_ENGINE_SPLIT && !plist && !tlist) g_refined_last = 0;
   const size_t N2 = c.N2, blk16 = 16 * N2;
   const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag;
   const double2 *P1 = (const double2*)mp1, *P2 = (const double2*)mp2, *Px2 = (const double2*)mom2;
@@ -474,10 +477,10 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
   for (int i = 0; i < nts; i++) need[t_of(i)] = 1;
   for (int i = 0; i < npairs; i++) need[pair_of(i) % Nt] = 1;
   void* pt;
-  CTR_TRY(workspace(WS_PHI).get(2 * (size_t)Nt * blk16 * sizeof(double2), &pt));
+  // a recomputation (plist / tlist) keeps its own R, so that the caller's stays valid
+  CTR_TRY(workspace((plist || tlist) ? WS_RPHI : WS_PHI).get(2 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *R = (double2*)pt, *tmp = R + Nt * blk16;
   CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need));
-  long long nref = 0;
   if (hor_fish) {
     // lib/calculate_sigmapi_hor_fish_core.h: sum_ab coef * sum R_ab (.) conj taud_ab, per time slice
     Refine rf;
@@ -508,17 +511,14 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
     else
       CTR_TRY(launch_rowsum((double2*)trm, nts * 16, (const int*)d_csr, (const int*)d_csr + nts + 1, nts, 1,
                             (double2*)hor_fish, nts, s));
-    CTR_TRY(refine_end(c, rf, 1, WS_REFINE, (double2*)hor_fish, &nref, [&](const std::vector<int>& ts, double2* out) {
-      return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2, (double*)out, nullptr, s,
-                           CTR_ENGINE_FP64, nullptr, &ts);
-    }));
-    // an FP64 recomputation above rebuilt R for its time slices in place
-    if (tri && nref > 0) CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need));
+    // (the recomputation keeps its own R, so R above stays valid for the triangle)
+    CTR_TRY(refine_end(c, rf, 1, WS_REFINE, (double2*)hor_fish,
+                       [=](const std::vector<int>& ts, double2* out, cudaStream_t ls) {
+                         return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2,
+                                              (double*)out, nullptr, ls, CTR_ENGINE_FP64, nullptr, &ts);
+                       }));
   }
-  if (!tri) {
-    if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
-    return CTR_OK;
-  }
+  if (!tri) return CTR_OK;
   // triangle (lib/calculate_sigmapi_triangle_core.h): X = T G R, Y_{ik, s1 s5} = Phix2_ik(tf) X_{s1 s5},
   // trace vs tau_{s1 s5}, weight g5(s1)
   const size_t per_pair = (size_t)(16 + 32) * N2 * sizeof(double2) + 32 * sizeof(double2);
@@ -565,12 +565,11 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
       CTR_TRY(launch_rowsum(TR, 32, (const int*)d_csr, (const int*)d_csr + 3, 2, np, (double2*)tri + (size_t)p0 * 2,
                             2, s));
   }
-  CTR_TRY(refine_end(c, rf, 2, WS_REFINE, (double2*)tri, &nref, [&](const std::vector<int>& pairs, double2* out) {
-    return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2, nullptr, (double*)out, s,
-                         CTR_ENGINE_FP64, &pairs, nullptr);
-  }));
-  if (engine == CTR_ENGINE_SPLIT) g_refined_last = nref;
-  return CTR_OK;
+  return refine_end(c, rf, 2, WS_REFINE, (double2*)tri,
+                    [=](const std::vector<int>& pairs, double2* out, cudaStream_t ls) {
+                      return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2, nullptr,
+                                           (double*)out, ls, CTR_ENGINE_FP64, &pairs, nullptr);
+                    });
 }
 
 // -------------------------------------------------------------- loop unity

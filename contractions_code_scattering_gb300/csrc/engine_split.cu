@@ -50,11 +50,16 @@ constexpr double REFINE_EPS = 1.0 / 281474976710656.0;  // 2^-48
 
 }  // namespace
 
+int prepare_for_capture() {
+  int* d;
+  CTR_TRY(err_flag(&d));
+  return split_kernels_prepare();
+}
+
 int split_error_check(cudaStream_t s) {
   if (!g_err_dev) return CTR_OK;
   int h = 0;
-  CTR_CUDA(cudaMemcpyAsync(&h, g_err_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CTR_CUDA(cudaStreamSynchronize(s));
+  CTR_TRY(download(&h, g_err_dev, sizeof(int), s));
   if (h != 0) {
     CTR_CUDA(cudaMemsetAsync(g_err_dev, 0, sizeof(int), s));
     return fail(CTR_ERR_TIMEOUT, "split GEMM pipeline wait timed out (stage %d)", h);
@@ -77,6 +82,11 @@ static size_t phi_bytes(int N, int Nt, int nL, int nR, int nchunk) {
   return align256((size_t)Nt * mt * nchunk * SPLIT_A_STAGE) + align256((size_t)Nt * nt * nchunk * SPLIT_B_STAGE) +
          align256((size_t)Nt * mt * SPLIT_M * 4) + align256((size_t)Nt * nt * SPLIT_N * 4);
 }
+
+static int refine_twosided(int N, int Nt, int tf_begin, int nphi, const double* prop_rows, const double* phi,
+                           const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
+                           const std::vector<int>& off, const std::vector<int>& ord, int nout, double* out,
+                           const int* d_count, const int* d_list, cudaStream_t stream);
 
 int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* phi, int nphi,
                    const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
@@ -214,8 +224,10 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   std::vector<SliceRightJob> rj;
   std::vector<SplitGemmInst> ga, gb;
   std::vector<const float4*> abase, bbase;
-  for (int p0 = 0; p0 < npairs_total; p0 += batch) {
-    const int np = std::min(batch, npairs_total - p0);
+  char shape[160];
+  snprintf(shape, sizeof(shape), "nev=%d,ncd=%d,nab=%d,nL=%d,nR=%d,ntr=%d", N, ncd, nab, nL, nR, ntr);
+  // one batch of pairs [p0, p0 + np): slice tau, both GEMMs, traces, per-entry sums
+  auto run_batch = [&](int p0, int np) -> int {
     void *mem, *rowbuf, *absbuf;
     CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * per_pair, &mem));
     CTR_TRY(workspace(WS_ROWS).get((size_t)np * ntr * sizeof(double2), &rowbuf));
@@ -266,31 +278,113 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     CTR_TRY(launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream));
     CTR_TRY(upload(WS_GEMM_A, ga.data(), ga.size() * sizeof(SplitGemmInst), &d_ga, stream));
     CTR_TRY(upload(WS_GEMM_B, gb.data(), gb.size() * sizeof(SplitGemmInst), &d_gb, stream));
+    // tile walk of each GEMM (autotuned; idempotent, so candidates re-run on the same data)
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
-    CTR_TRY(launch_split_gemm(GA, np, d_err, stream));
     SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
-    CTR_TRY(launch_split_gemm(GB, np, d_err, stream));
+    for (SplitGemmBatch* G : {&GA, &GB}) {
+      char gshape[96];
+      snprintf(gshape, sizeof(gshape), "std,m=%d,n=%d,k=%d", G->mtiles, G->ntiles, G->nchunk);
+      int order = 0;
+      CTR_TRY(tune_resolve("split_gemm.order", gshape, 2, 0, stream,
+                           [&](int c) {
+                             SplitGemmBatch t = *G;
+                             t.order = c;
+                             return launch_split_gemm(t, np, d_err, stream);
+                           },
+                           &order));
+      G->order = order;
+      CTR_TRY(launch_split_gemm(*G, np, d_err, stream));
+    }
     abase.insert(abase.end(), bbase.begin(), bbase.end());
     CTR_TRY(upload(WS_ROWTASKS, abase.data(), abase.size() * sizeof(const float4*), &d_tt, stream));
-    CTR_TRY(launch_trace_rows((const TraceRow*)d_trow, ntr, (const float4* const*)d_tt,
-                              (const float4* const*)d_tt + np, ldA, ldB, np, N, R, Rabs, stream));
-    CTR_TRY(launch_rowsum_coef_refine(R, Rabs, ntr, (const int*)d_csr, (const int*)d_csr + (nout + 1),
-                                      (const int*)d_tix, (const float*)d_rcoef, nout, np,
-                                      (double2*)out + (size_t)p0 * nout,
-                                      g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0, d_count, d_list, p0,
-                                      stream));
+    auto traces = [&](int variant) {
+      return launch_trace_rows((const TraceRow*)d_trow, ntr, (const float4* const*)d_tt,
+                               (const float4* const*)d_tt + np, ldA, ldB, np, N, R, Rabs, variant, stream);
+    };
+    int variant = 0;
+    CTR_TRY(tune_resolve("trace_rows", shape, TRACE_VARIANTS, 0, stream, traces, &variant));
+    CTR_TRY(traces(variant));
+    return launch_rowsum_coef_refine(R, Rabs, ntr, (const int*)d_csr, (const int*)d_csr + (nout + 1),
+                                     (const int*)d_tix, (const float*)d_rcoef, nout, np,
+                                     (double2*)out + (size_t)p0 * nout,
+                                     g_refine_tol > 0.0 ? REFINE_EPS / g_refine_tol : 0.0, d_count, d_list, p0,
+                                     stream);
+  };
+
+  // pairs per batch: forced, cached, measured on this call's first batches, or
+  // the largest that fits the scratch budget
+  int p0 = 0;
+  {
+    const std::string bkey = tune_key("twosided.batch", shape);
+    int v = tune_forced("twosided.batch");
+    if (v > 0) {
+      batch = std::min(v, batch);
+    } else if (tune_lookup(bkey, &v) && v > 0) {
+      batch = std::min(v, batch);
+    } else if (tune_mode() > 0) {
+      // candidates, largest first (the scratch then grows once), each run twice:
+      // the first pass warms up (and resolves the kernel knobs), the second is timed
+      std::vector<int> cand;
+      for (int c = std::min(batch, 512); c >= 2; c /= 2) cand.push_back(c);
+      int sum = 0;
+      for (int c : cand) sum += c;
+      while (cand.size() > 1 && 2 * sum > npairs_total) {
+        sum -= cand.front();
+        cand.erase(cand.begin());
+      }
+      if (cand.size() > 1) {
+        cudaEvent_t e0, e1;
+        CTR_CUDA(cudaEventCreate(&e0));
+        CTR_CUDA(cudaEventCreate(&e1));
+        std::vector<double> per(cand.size(), 0.0);
+        int rc = CTR_OK;
+        for (int rep = 0; rep < 2 && rc == CTR_OK; rep++)
+          for (size_t k = 0; k < cand.size() && rc == CTR_OK; k++) {
+            cudaEventRecord(e0, stream);
+            rc = run_batch(p0, cand[k]);
+            cudaEventRecord(e1, stream);
+            p0 += cand[k];
+            float ms = 0.f;
+            if (rc == CTR_OK) {
+              cudaError_t e = cudaEventSynchronize(e1);
+              if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+              if (e != cudaSuccess) rc = cuda_fail(e, "tuning events", __FILE__, __LINE__);
+            }
+            if (rep == 1) per[k] = ms / cand[k];
+          }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        CTR_TRY(rc);
+        size_t best = 0;
+        for (size_t k = 1; k < cand.size(); k++)
+          if (per[k] < per[best]) best = k;
+        batch = cand[best];
+        tune_store(bkey, batch, per);  // ms per pair of each candidate
+      }
+    }
   }
+  for (; p0 < npairs_total; p0 += batch) CTR_TRY(run_batch(p0, std::min(batch, npairs_total - p0)));
   g_refined_last = 0;
   if (g_refine_tol <= 0.0) return CTR_OK;
+  // ---- recomputation of the flagged entries: the list is read on the host, so
+  // under graph recording this runs after the recorded kernels at every launch
+  return host_step(stream, [=](cudaStream_t ls) {
+    return refine_twosided(N, Nt, tf_begin, nphi, prop_rows, phi, rows, coef, off, ord, nout, out, d_count, d_list,
+                           ls);
+  });
+}
 
-  // ---- FP64 recomputation of the flagged entries
+// Recomputes the entries listed in d_list[0 .. *d_count) (indices pair * nout + o
+// of the call's output) with the high-precision configuration and patches them.
+static int refine_twosided(int N, int Nt, int tf_begin, int nphi, const double* prop_rows, const double* phi,
+                           const std::vector<TwoSidedRow>& rows, const std::vector<float>& coef,
+                           const std::vector<int>& off, const std::vector<int>& ord, int nout, double* out,
+                           const int* d_count, const int* d_list, cudaStream_t stream) {
   int nflag = 0;
-  CTR_CUDA(cudaMemcpyAsync(&nflag, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
-  CTR_CUDA(cudaStreamSynchronize(stream));
+  CTR_TRY(download(&nflag, d_count, sizeof(int), stream));
   if (nflag == 0) return CTR_OK;
   std::vector<int> flagged(nflag);
-  CTR_CUDA(cudaMemcpyAsync(flagged.data(), d_list, nflag * sizeof(int), cudaMemcpyDeviceToHost, stream));
-  CTR_CUDA(cudaStreamSynchronize(stream));
+  CTR_TRY(download(flagged.data(), d_list, nflag * sizeof(int), stream));
   std::sort(flagged.begin(), flagged.end());
   std::vector<ctr_factor> fac;
   std::vector<int> foff(1, 0), chain_row;
@@ -324,8 +418,7 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   // row/column scales, ~2^9 below the standard one); traces in FP64
   CTR_TRY(chain_values(N, Nt, nphi, prop_rows, phi, fac, foff, (double*)dv, stream, CTR_ENGINE_SPLIT));
   std::vector<double2> vals(chain_row.size());
-  CTR_CUDA(cudaMemcpyAsync(vals.data(), dv, vals.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream));
-  CTR_CUDA(cudaStreamSynchronize(stream));
+  CTR_TRY(download(vals.data(), dv, vals.size() * sizeof(double2), stream));
   std::vector<double2> patch(nflag);
   std::vector<int> where(nflag);
   size_t c = 0;
@@ -345,7 +438,7 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   CTR_TRY(upload(WS_TASKS, where.data(), where.size() * sizeof(int), &dw, stream));
   CTR_TRY(upload(WS_TASKS2, patch.data(), patch.size() * sizeof(double2), &dp, stream));
   CTR_TRY(launch_scatter((const int*)dw, (const double2*)dp, nflag, (double2*)out, stream));
-  g_refined_last = nflag;
+  g_refined_last += nflag;
   return CTR_OK;
 }
 

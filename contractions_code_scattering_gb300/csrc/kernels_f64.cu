@@ -301,6 +301,27 @@ int launch_stage_copy(void* dst, const void* src, size_t bytes, cudaStream_t s) 
   return CTR_OK;
 }
 
+__global__ void readback_kernel(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src, size_t bytes, int words) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if (words) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < bytes / 4; i += stride)
+      ((uint32_t*)dst)[i] = ((const uint32_t*)src)[i];
+  } else {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < bytes; i += stride) dst[i] = src[i];
+  }
+}
+
+int launch_readback(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return CTR_OK;
+  const int words = (((uintptr_t)dst | (uintptr_t)src | bytes) & 3) == 0;
+  const size_t n = words ? bytes / 4 : bytes;
+  const int grid = (int)std::min<size_t>(256, std::max<size_t>(1, (n + 255) / 256));
+  TimedLaunch tl(s, "readback");
+  readback_kernel<<<grid, 256, 0, s>>>((uint8_t*)dst, (const uint8_t*)src, bytes, words);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
 int launch_scatter(const int* where, const double2* vals, int n, double2* out, cudaStream_t s) {
   if (n == 0) return CTR_OK;
   TimedLaunch tl(s, "refine_scatter");

@@ -424,6 +424,22 @@ __device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint
   }
 }
 
+// Output tile -> (instance, M tile, N tile).  order 0 walks the N tiles of one
+// M tile first (consecutive CTAs share the left operand tile), order 1 the M
+// tiles of one N tile first (they share the right operand tile).
+__device__ __forceinline__ void tile_coords(const SplitGemmBatch& g, int tile, int& inst, int& mt, int& nt) {
+  const int per_inst = g.mtiles * g.ntiles;
+  inst = tile / per_inst;
+  const int r = tile - inst * per_inst;
+  if (g.order == 0) {
+    mt = r / g.ntiles;
+    nt = r - mt * g.ntiles;
+  } else {
+    nt = r / g.mtiles;
+    mt = r - nt * g.mtiles;
+  }
+}
+
 template <class C>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     split_gemm_kernel(SplitGemmBatch g, int ntiles_total, int* __restrict__ err) {
@@ -440,7 +456,6 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
   volatile int* status = (volatile int*)(tslot + 1);  // block-uniform decisions
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int per_inst = g.mtiles * g.ntiles;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; s++) {
@@ -470,7 +485,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       uint32_t g_chunk = 0;
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x) {
-        const int inst = tile / per_inst, mt = (tile % per_inst) / g.ntiles, nt = tile % g.ntiles;
+        int inst, mt, nt;
+        tile_coords(g, tile, inst, mt, nt);
         const SplitGemmInst* I = &g.inst[inst];
         const uint8_t* gA = I->left + (size_t)mt * g.nchunk * C::A_STAGE;
         const uint8_t* gB = I->right + (size_t)nt * g.nchunk * C::B_STAGE;
@@ -527,7 +543,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
     uint32_t local = 0;
     for (int tile = blockIdx.x; tile < ntiles_total; tile += gridDim.x, local++) {
-      const int inst = tile / per_inst, mt = (tile % per_inst) / g.ntiles, nt = tile % g.ntiles;
+      int inst, mt, nt;
+      tile_coords(g, tile, inst, mt, nt);
       const SplitGemmInst* I = &g.inst[inst];
       // stage this tile's column exponents; the barrier also keeps the previous
       // tile's values until every epilogue thread has used them
@@ -685,15 +702,114 @@ __global__ void __launch_bounds__(128) trace_rows_kernel(const TraceRow* __restr
   }
 }
 
+// Flattened form of the same traces: the TPB threads of a CTA walk the nev*nev
+// elements in column order (element e -> i = e % nev, j = e / nev), so every
+// thread is busy whatever nev is, and each thread sums fewer terms.
+template <int TPB>
+__global__ void __launch_bounds__(TPB) trace_rows_flat_kernel(const TraceRow* __restrict__ rt, int nrows,
+                                                              const float4* const* __restrict__ abase,
+                                                              const float4* const* __restrict__ bbase, int lda,
+                                                              int ldb, int nev, double2* __restrict__ rows,
+                                                              double* __restrict__ rabs) {
+  constexpr int NW = TPB / 32;
+  const int q = blockIdx.x / nrows, r = blockIdx.x % nrows;
+  const TraceRow T = rt[r];
+  const float4* pa = abase[q] + T.aoff;
+  const float4* pb = bbase[q] + T.boff;
+  float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f, sa = 0.f;
+  const int total = nev * nev, di = TPB % nev, dj = TPB / nev;
+  int i = threadIdx.x % nev, j = threadIdx.x / nev;
+  for (int e = threadIdx.x; e < total; e += TPB) {
+    const float4 a = pa[(size_t)j * lda + i];
+    const float4 b = pb[(size_t)j * ldb + i];
+    ff_mac(sr, er, a.x, a.y, b.x, b.y);    // + ar br
+    ff_mac(sr, er, a.z, a.w, b.z, b.w);    // + ai bi
+    ff_mac(si, ei, a.z, a.w, b.x, b.y);    // + ai br
+    ff_mac(si, ei, -a.x, -a.y, b.z, b.w);  // - ar bi
+    sa = fmaf(fabsf(a.x) + fabsf(a.z), fabsf(b.x) + fabsf(b.z), sa);
+    i += di;
+    j += dj;
+    if (i >= nev) {
+      i -= nev;
+      j++;
+    }
+  }
+  double re = (double)sr + (double)er, im = (double)si + (double)ei, ab = (double)sa;
+  __shared__ double red[3][NW];
+  for (int o = 16; o; o >>= 1) {
+    re += __shfl_down_sync(0xffffffffu, re, o);
+    im += __shfl_down_sync(0xffffffffu, im, o);
+    ab += __shfl_down_sync(0xffffffffu, ab, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = re;
+    red[1][threadIdx.x >> 5] = im;
+    red[2][threadIdx.x >> 5] = ab;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    re = 0.0;
+    im = 0.0;
+    ab = 0.0;
+    for (int w = 0; w < NW; w++) {
+      re += red[0][w];
+      im += red[1][w];
+      ab += red[2][w];
+    }
+    const double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+    rows[blockIdx.x] = cmul(c, make_double2(re, im));
+    rabs[blockIdx.x] = sqrt(c.x * c.x + c.y * c.y) * ab;
+  }
+}
+
 // --------------------------------------------------------------- launchers
+// Dynamic shared-memory limits are raised once per kernel (before any graph
+// capture, through split_kernels_prepare, or at the first launch).
+template <typename K>
+static int ensure_smem(K kernel, size_t smem, bool& done) {
+  if (!done) {
+    CTR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    done = true;
+  }
+  return CTR_OK;
+}
+static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr = false, g_attr_std = false,
+            g_attr_hp = false;
+static int g_nsm = 0;
+
+template <class C>
+static bool& gemm_attr_flag();
+template <>
+bool& gemm_attr_flag<CfgStd>() { return g_attr_std; }
+template <>
+bool& gemm_attr_flag<CfgHP>() { return g_attr_hp; }
+
+static int sm_count(int* out) {
+  if (!g_nsm) {
+    int dev = 0;
+    CTR_CUDA(cudaGetDevice(&dev));
+    CTR_CUDA(cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  *out = g_nsm;
+  return CTR_OK;
+}
+
+int split_kernels_prepare() {
+  int nsm;
+  CTR_TRY(sm_count(&nsm));
+  CTR_TRY(ensure_smem(slice_left_kernel, 512 + SPLIT_A_STAGE, g_attr_sl));
+  CTR_TRY(ensure_smem(slice_right_kernel, 512 + SPLIT_B_STAGE, g_attr_sr));
+  CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
+  CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 2048 + CfgHP::B_STAGE, g_attr_tr));
+  CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
+  CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
+  return CTR_OK;
+}
+
 int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
   const size_t smem = 512 + SPLIT_A_STAGE;
-  static bool attr = false;
-  if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(slice_left_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  CTR_TRY(ensure_smem(slice_left_kernel, smem, g_attr_sl));
   TimedLaunch tl(s, "slice_left");
   slice_left_kernel<<<njobs * mtiles, 256, smem, s>>>(d_jobs, nev, nchunk, mtiles);
   CTR_CUDA(cudaGetLastError());
@@ -703,11 +819,7 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
   const size_t smem = 512 + SPLIT_B_STAGE;
-  static bool attr = false;
-  if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(slice_right_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  CTR_TRY(ensure_smem(slice_right_kernel, smem, g_attr_sr));
   TimedLaunch tl(s, "slice_right");
   slice_right_kernel<<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
   CTR_CUDA(cudaGetLastError());
@@ -717,12 +829,7 @@ int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchu
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
   const size_t smem = 512 + CfgHP::A_STAGE;
-  static bool attr = false;
-  if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(slice_task_left_kernel<CfgHP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    attr = true;
-  }
+  CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, smem, g_attr_tl));
   TimedLaunch tl(s, "slice_task_left");
   slice_task_left_kernel<CfgHP><<<njobs, 256, smem, s>>>(d_jobs, nev, nchunk);
   CTR_CUDA(cudaGetLastError());
@@ -732,12 +839,7 @@ int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int 
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
   const size_t smem = 2048 + CfgHP::B_STAGE;
-  static bool attr = false;
-  if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(slice_task_right_kernel<CfgHP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    attr = true;
-  }
+  CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, smem, g_attr_tr));
   TimedLaunch tl(s, "slice_task_right");
   slice_task_right_kernel<CfgHP><<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
   CTR_CUDA(cudaGetLastError());
@@ -747,17 +849,9 @@ int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int
 template <class C>
 static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, const char* name) {
   const size_t smem = gemm_smem_bytes<C>();
-  static bool attr = false;
-  if (!attr) {
-    CTR_CUDA(cudaFuncSetAttribute(split_gemm_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    CTR_CUDA(cudaGetDevice(&dev));
-    CTR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
+  CTR_TRY(ensure_smem(split_gemm_kernel<C>, smem, gemm_attr_flag<C>()));
+  int nsm;
+  CTR_TRY(sm_count(&nsm));
   const long long total = (long long)ninst * g.mtiles * g.ntiles;
   if (total > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
   const int grid = (int)std::min<long long>(total, nsm);
@@ -777,12 +871,30 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
 }
 
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
-                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, cudaStream_t s) {
+                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, int variant,
+                      cudaStream_t s) {
   if (npair == 0 || nrows == 0) return CTR_OK;
   const long long nblk = (long long)npair * nrows;
   if (nblk > 0x7fffffffLL) return fail(CTR_ERR_ARG, "traces: grid too large");
   TimedLaunch tl(s, "trace_rows");
-  trace_rows_kernel<<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+  switch (variant) {
+    case 0:
+      trace_rows_kernel<<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 1:
+      trace_rows_flat_kernel<128>
+          <<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 2:
+      trace_rows_flat_kernel<256>
+          <<<(unsigned)nblk, 256, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 3:
+      trace_rows_flat_kernel<512>
+          <<<(unsigned)nblk, 512, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    default: return fail(CTR_ERR_ARG, "traces: unknown variant %d", variant);
+  }
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

@@ -180,6 +180,7 @@ int rho_noalloc(int N, int Nt, int tf, const double* prop_row, const double* mom
 
 extern "C" int ctr_rho_noalloc(int nev, int nt, int tf, const double* prop_row, const double* mom5, double* corr,
                                void* stream) {
+  CTR_NO_CAPTURE("ctr_rho_noalloc");
   if (nev < 1 || nt < 1 || tf < 0 || tf >= nt || !prop_row || !mom5 || !corr)
     return ctr::fail(CTR_ERR_ARG, "ctr_rho_noalloc: bad arguments");
   if (((uintptr_t)prop_row | (uintptr_t)mom5 | (uintptr_t)corr) & 15)

@@ -76,6 +76,7 @@ struct SplitGemmBatch {
   int out_mode;      // 0: float-float column-major, 1: complex128 row-major blocks
   int blkn;          // out_mode 1: columns (and row stride) of one output block
   int hp;            // 0: CfgStd operands and tiles, 1: CfgHP (out_mode 1 only)
+  int order;         // persistent tile walk: 0 N tiles innermost, 1 M tiles innermost
 };
 
 // Operands of the task form C = sum_q w_q op(A_q) op(B_q) (q < nterm <= 4),
@@ -133,11 +134,17 @@ __device__ __forceinline__ void ff_mac(float& S, float& E, float xh, float xl, f
 int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s);
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
+// Raises the shared-memory limits of the split kernels and caches the SM count.
+int split_kernels_prepare();
 // Closing traces over npair pairs: products of pair q at a_base[q] / b_base[q]
 // (leading dimensions lda / ldb); rows[q * nrows + r] = coef_r * trace and
 // rabs[q * nrows + r] = |coef_r| sum |A|_1 |B|_1.
+// variant: 0 one thread per row i walking the columns (128 threads), 1/2/3 the
+// flattened element walk with 128/256/512 threads (TRACE_VARIANTS candidates).
+constexpr int TRACE_VARIANTS = 4;
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
-                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, cudaStream_t s);
+                      int lda, int ldb, int npair, int nev, double2* rows, double* rabs, int variant,
+                      cudaStream_t s);
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s);
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 

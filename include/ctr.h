@@ -270,6 +270,51 @@ void ctr_timing_enable(int on);
 long long ctr_launch_count(void);
 int ctr_timing_report(char* buf, int buflen);
 
+/* ------------------------------------------------------------ CUDA graphs
+ * Record the library calls a thread issues on one stream and replay them.
+ *   ctr_graph_begin(s);  ctr_rho(..., s);  ...;  ctr_graph_end(s, &g);
+ *   ctr_graph_launch(g, s);  (any number of times)  ctr_graph_destroy(g);
+ * While recording, nothing executes: the kernels of the calls are captured into
+ * CUDA graphs, their task tables are copied once into device memory owned by
+ * the graph, and their scratch comes from buffers owned by the graph (so a
+ * recorded graph never shares scratch with eager calls or with other graphs).
+ * A replay reads the device buffers that were passed while recording, with the
+ * contents they hold at replay time.  Steps that need host decisions on device
+ * results -- the split engine's recomputation of ill-conditioned entries --
+ * end a graph segment; ctr_graph_launch replays the segments in order and runs
+ * those steps between them, synchronising the stream there (as the eager call
+ * does).  Recording needs a created stream (not the legacy default stream),
+ * uses the autotuner's cached choices (it measures nothing), and rejects the
+ * calls that read device data on the host to plan their work: the profile
+ * adjoint entry points, ctr_rho_noalloc, the ctr_calculate_* host API and
+ * ctr_sync.  A call that fails while recording makes ctr_graph_end fail (the
+ * capture is closed and discarded).  Launch counts of replays are added to the
+ * launch accounting; per-kernel event timing is not recorded for replays. */
+typedef struct ctr_graph ctr_graph;
+int ctr_graph_begin(void* stream);
+int ctr_graph_end(void* stream, ctr_graph** graph);
+int ctr_graph_launch(ctr_graph* graph, void* stream);
+/* segments, kernel nodes per replay, bytes of device memory the graph owns */
+int ctr_graph_info(const ctr_graph* graph, int* nsegments, long long* nkernels, long long* device_bytes);
+void ctr_graph_destroy(ctr_graph* graph);
+
+/* --------------------------------------------------------------- autotuner
+ * Tunable choices (tile schedules, kernel variants, batch sizes) are keyed by
+ * knob and problem shape.  mode 0: use the cached choice, else the default;
+ * mode 1: a call that meets an uncached key times the candidates on its own
+ * live data and caches the fastest (kernel variants are re-launched on the same
+ * inputs; batch sizes are timed on successive batches of real work, so nothing
+ * is computed twice); mode 2: as 1, re-measuring cached keys.  Candidates give
+ * the same results up to rounding.  ctr_tune_force(knob, value) pins a knob
+ * (value -1 releases it).  The table is saved and loaded as text lines
+ * "key choice". */
+int ctr_tune_set_mode(int mode);
+int ctr_tune_force(const char* knob, int value);
+int ctr_tune_report(char* buf, int buflen); /* JSON {"key": {"choice": c, "ms": [...]}, ...} */
+void ctr_tune_clear(void);
+int ctr_tune_save(const char* path);
+int ctr_tune_load(const char* path);
+
 #ifdef __cplusplus
 }
 #endif
