@@ -186,8 +186,10 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
       const uint32_t off = core_offset(nn, kk);
 #pragma unroll
       for (int s = 0; s < SPLIT_NSLICE; s++) {
-        *(__nv_bfloat16*)(stage + (s * 2 + 0) * SPLIT_B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 2 + 1) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, ni);
+        // planes -im, re, im (packed complex MMAs)
+        *(__nv_bfloat16*)(stage + (s * 3 + 0) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, !ni);
+        *(__nv_bfloat16*)(stage + (s * 3 + 1) * SPLIT_B_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 3 + 2) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, ni);
       }
     }
     __syncthreads();
@@ -317,8 +319,14 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
       const uint32_t off = core_offset(nn, kk);
 #pragma unroll
       for (int s = 0; s < C::NS; s++) {
-        *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
+        if (C::PACK) {
+          *(__nv_bfloat16*)(stage + (s * 3 + 0) * C::B_SUB + off) = slice_bf16(Ui, s, !ni);
+          *(__nv_bfloat16*)(stage + (s * 3 + 1) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
+          *(__nv_bfloat16*)(stage + (s * 3 + 2) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
+        } else {
+          *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
+          *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
+        }
       }
     }
     __syncthreads();
@@ -403,6 +411,7 @@ template <class C>
 __device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
   constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, C::BN, false);
   constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, C::BN, true);
+  constexpr uint32_t id_wide = idesc_bf16_f32(SPLIT_M, 2 * C::BN, false);
 #pragma unroll
   for (int i = 0; i < C::NS; i++) {
 #pragma unroll
@@ -412,14 +421,23 @@ __device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint
       const uint32_t accum = (!first_chunk || !(i == 0 && j <= C::NL - 1)) ? 1u : 0u;
       const uint64_t ar = adesc + (uint64_t)(((i * 2 + 0) * C::A_SUB) >> 4);
       const uint64_t ai = adesc + (uint64_t)(((i * 2 + 1) * C::A_SUB) >> 4);
-      const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * C::B_SUB) >> 4);
-      const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * C::B_SUB) >> 4);
-      const uint32_t dre = tbase + (uint32_t)(lvl * C::BN);
-      const uint32_t dim = tbase + (uint32_t)((C::NL + lvl) * C::BN);
-      umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
-      umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
-      umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
-      umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
+      if (C::PACK) {
+        // planes -Yi, Yr, Yi of slice j are adjacent along N (row groups 256 B apart)
+        const uint64_t b_nr = bdesc + (uint64_t)(((j * 3 + 0) * C::B_SUB) >> 4);  // [-Yi | Yr]
+        const uint64_t b_ri = bdesc + (uint64_t)(((j * 3 + 1) * C::B_SUB) >> 4);  // [Yr | Yi]
+        const uint32_t d = tbase + (uint32_t)C::acc_col(0, lvl);
+        umma_f16(d, ar, b_ri, id_wide, accum);  // [Re | Im] += Xr [Yr | Yi]
+        umma_f16(d, ai, b_nr, id_wide, 1u);     // [Re | Im] += Xi [-Yi | Yr]
+      } else {
+        const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * C::B_SUB) >> 4);
+        const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * C::B_SUB) >> 4);
+        const uint32_t dre = tbase + (uint32_t)C::acc_col(0, lvl);
+        const uint32_t dim = tbase + (uint32_t)C::acc_col(1, lvl);
+        umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
+        umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
+        umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
+        umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
+      }
     }
   }
 }
@@ -578,7 +596,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 #pragma unroll
             for (int l = 0; l < C::NL; l++) {
               float v[16];
-              tmem_ld16(tl + (uint32_t)((part * C::NL + l) * C::BN + c0), v);
+              tmem_ld16(tl + (uint32_t)(C::acc_col(part, l) + c0), v);
               tmem_ld_wait();
 #pragma unroll
               for (int c = 0; c < 16; c++) acc[part][c] += f2i_scaled(v[c], 54);
@@ -603,7 +621,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         for (int part = 0; part < 2; part++) {
           float v[C::NL][16];
 #pragma unroll
-          for (int l = 0; l < C::NL; l++) tmem_ld16(tl + (uint32_t)((part * C::NL + l) * C::BN + c0), v[l]);
+          for (int l = 0; l < C::NL; l++) tmem_ld16(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
           tmem_ld_wait();
           if (g.levels && rvalid) {
             for (int c = 0; c < 16; c++) {

@@ -17,8 +17,9 @@ constexpr int SPLIT_NSLICE = 5;  // BF16 slices (balanced base-512 digits) per F
 constexpr int SPLIT_MAXK = 128;  // largest Nev the engine takes (exactness bound of the leading level)
 constexpr int SPLIT_A_SUB = SPLIT_M * SPLIT_K * 2;                  // one (slice, plane) sub-tile, bytes
 constexpr int SPLIT_B_SUB = SPLIT_N * SPLIT_K * 2;
+constexpr int SPLIT_B_PLANES = 3;                                   // -im, re, im (packed complex MMAs)
 constexpr int SPLIT_A_STAGE = SPLIT_NSLICE * 2 * SPLIT_A_SUB;       // 40960 B: all slices, re+im, one K chunk
-constexpr int SPLIT_B_STAGE = SPLIT_NSLICE * 2 * SPLIT_B_SUB;       // 20480 B
+constexpr int SPLIT_B_STAGE = SPLIT_NSLICE * SPLIT_B_PLANES * SPLIT_B_SUB;  // 30720 B
 constexpr int SPLIT_MAXBLK = 32;
 
 // Kernel configurations: slices per value, TMEM accumulation levels, tile N.
@@ -28,16 +29,27 @@ constexpr int SPLIT_MAXBLK = 32;
 //    6 slices (21 slice pairs, 54 bits), levels 0-3 exact and >= 4 in FP32,
 //    N = 48 (10 x 48 = 480 TMEM columns); the epilogue sums the levels exactly
 //    in 64-bit integers, so products keep ~2^-53 of their row/column scales.
-template <int NS_, int NL_, int BN_>
+//
+// Packed complex MMAs (PACK): the right operand keeps three planes per slice,
+// -Yi, Yr, Yi, adjacent along N, so that the complex product takes two MMAs of
+// width 2 BN per slice pair, Xr [Yr | Yi] and Xi [-Yi | Yr], into one [Re | Im]
+// accumulator per level (instead of four MMAs of width BN); the left operand
+// tile is then read from shared memory half as often per flop.
+template <int NS_, int NL_, int BN_, bool PACK_>
 struct SplitCfg {
   static constexpr int NS = NS_, NL = NL_, BN = BN_;
+  static constexpr bool PACK = PACK_;
+  static constexpr int B_PLANES = PACK ? 3 : 2;
   static constexpr int A_SUB = SPLIT_M * SPLIT_K * 2;
   static constexpr int B_SUB = BN * SPLIT_K * 2;
   static constexpr int A_STAGE = NS * 2 * A_SUB;
-  static constexpr int B_STAGE = NS * 2 * B_SUB;
+  static constexpr int B_STAGE = NS * B_PLANES * B_SUB;
+  // TMEM column of accumulator (part 0 = Re / 1 = Im, level l)
+  __host__ __device__ static constexpr int acc_col(int part, int l) { return PACK ? (l * 2 + part) * BN : (part * NL + l) * BN; }
 };
-using CfgStd = SplitCfg<SPLIT_NSLICE, 4, SPLIT_N>;
-using CfgHP = SplitCfg<6, 5, 48>;
+using CfgStd = SplitCfg<SPLIT_NSLICE, 4, SPLIT_N, true>;
+using CfgHP = SplitCfg<6, 5, 48, true>;
+static_assert(CfgStd::B_STAGE == SPLIT_B_STAGE && CfgStd::A_STAGE == SPLIT_A_STAGE, "standard stage sizes");
 
 // Slicing of a stacked operand.  Left: rows r -> row r%nev of blk[r/nev].
 struct SliceLeftJob {
