@@ -344,7 +344,9 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
 // warps 2..5: epilogue (TMEM lanes 32*(warp%4) .. +31).  The MMA warp and the
 // epilogue hand the TMEM accumulators back and forth with two mbarriers
 // (tmem_full after the last MMA of a tile, tmem_empty once drained).
-constexpr int GEMM_THREADS = 192;
+// Threads of a GEMM CTA: producer and MMA warps plus C::EPI_WARPS epilogue warps.
+template <class C>
+constexpr int gemm_threads() { return 64 + 32 * C::EPI_WARPS; }
 constexpr int NSTAGE = 3;
 constexpr uint32_t TMEM_COLS = 512;  // (re, im) x NL levels x BN columns fit in 512 for both configurations
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
@@ -400,7 +402,8 @@ __device__ __forceinline__ double pow2d(int e) {
   return __longlong_as_double((long long)(1023 + e) << 52);
 }
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+template <int NTHR>
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(NTHR) : "memory"); }
 
 // All MMAs of one K chunk: NS(NS+1)/2 slice pairs (i + j < NS) x 4 real
 // products into the 2 NL level accumulators.  adesc / bdesc describe sub-tile
@@ -459,7 +462,7 @@ __device__ __forceinline__ void tile_coords(const SplitGemmBatch& g, int tile, i
 }
 
 template <class C>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
+__global__ void __launch_bounds__(gemm_threads<C>(), 1)
     split_gemm_kernel(SplitGemmBatch g, int ntiles_total, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;
@@ -481,7 +484,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, 4);  // one arrival per epilogue warp
+    mbar_init(tempty, C::EPI_WARPS);  // one arrival per epilogue warp
     mbar_init(drainb, 1);
     fence_mbar_init();
     // A CTA that starts after another one recorded a failure does nothing.
@@ -555,8 +558,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     }
   } else {
     // epilogue: warps 2..5 -> TMEM lane quadrant warp % 4
-    const int q = warp & 3;
-    const int et = threadIdx.x - 64;  // 0..127 within the epilogue group
+    // TMEM lane quadrant warp % 4; with 8 epilogue warps each quadrant has two,
+    // which split the tile's columns between them
+    constexpr int EPH = C::EPI_WARPS / 4, CPW = C::BN / EPH;
+    const int q = warp & 3, half = (warp - 2) / 4;
+    const int et = threadIdx.x - 64;  // 0 .. 32 * EPI_WARPS - 1 within the epilogue group
     const int row = q * 32 + lane;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
     uint32_t local = 0;
@@ -566,7 +572,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       const SplitGemmInst* I = &g.inst[inst];
       // stage this tile's column exponents; the barrier also keeps the previous
       // tile's values until every epilogue thread has used them
-      epi_bar();
+      epi_bar<32 * C::EPI_WARPS>();
       if (et < C::BN) sexp[et] = I->rexp[nt * C::BN + et];
       const int grow = mt * SPLIT_M + row;
       const bool rvalid = grow < g.mrows;
@@ -578,13 +584,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (!done) atomicExch(err, 3);
         status[1] = done ? 0 : 1;
       }
-      epi_bar();
+      epi_bar<32 * C::EPI_WARPS>();
       if (status[1]) break;
       tc_fence_after();
       float4* outp = I->out;
       const int ldo = g.ldo;
-      for (int c0 = 0; c0 < C::BN; c0 += 16) {
-        if (g.out_mode == 1) {
+      for (int c0 = half * CPW; c0 < (half + 1) * CPW; c0 += 16) {
+        if constexpr (C::INT_OUT) {
           // complex128 output: the exact levels and the last one summed exactly
           // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
           // below 2^8, so no overflow), then rounded once to double
@@ -613,7 +619,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             I->outs[j][(size_t)grow * g.blkn + cc] = make_double2(i2d_scaled(acc[0][c], e), i2d_scaled(acc[1][c], e));
           }
           continue;
-        }
+        } else {
         // float-float output: levels 0 .. NL-2 exact, combined by exact two-sums;
         // the rounding errors and the last level go to the low word
         float hi[2][16], lo[2][16];
@@ -651,6 +657,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           if (gcol >= g.ncols) continue;
           const float sc = srow * pow2f(sexp[c0 + c]);
           outp[(size_t)gcol * ldo + grow] = make_float4(hi[0][c] * sc, lo[0][c] * sc, hi[1][c] * sc, lo[1][c] * sc);
+        }
         }
       }
       // accumulators drained: hand TMEM back to the MMA warp
@@ -874,7 +881,7 @@ static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err,
   if (total > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
   const int grid = (int)std::min<long long>(total, nsm);
   TimedLaunch tl(s, name);
-  split_gemm_kernel<C><<<grid, GEMM_THREADS, smem, s>>>(g, (int)total, d_err);
+  split_gemm_kernel<C><<<grid, gemm_threads<C>(), smem, s>>>(g, (int)total, d_err);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
@@ -885,6 +892,7 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
     if (g.out_mode != 1 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: the high-precision tiles write complex128");
     return launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");
   }
+  if (g.out_mode != 0) return fail(CTR_ERR_ARG, "split GEMM: the standard tiles write float-float");
   return launch_split_gemm_cfg<CfgStd>(g, ninst, d_err, s, "split_gemm");
 }
 

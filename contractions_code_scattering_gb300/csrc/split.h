@@ -35,10 +35,12 @@ constexpr int SPLIT_MAXBLK = 32;
 // width 2 BN per slice pair, Xr [Yr | Yi] and Xi [-Yi | Yr], into one [Re | Im]
 // accumulator per level (instead of four MMAs of width BN); the left operand
 // tile is then read from shared memory half as often per flop.
-template <int NS_, int NL_, int BN_, bool PACK_>
+template <int NS_, int NL_, int BN_, bool PACK_, bool INT_OUT_>
 struct SplitCfg {
   static constexpr int NS = NS_, NL = NL_, BN = BN_;
   static constexpr bool PACK = PACK_;
+  static constexpr bool INT_OUT = INT_OUT_;  // epilogue: complex128 via exact integer sums (else float-float)
+  static constexpr int EPI_WARPS = INT_OUT ? 4 : 8;  // the integer epilogue needs ~255 registers a thread
   static constexpr int B_PLANES = PACK ? 3 : 2;
   static constexpr int A_SUB = SPLIT_M * SPLIT_K * 2;
   static constexpr int B_SUB = BN * SPLIT_K * 2;
@@ -47,9 +49,11 @@ struct SplitCfg {
   // TMEM column of accumulator (part 0 = Re / 1 = Im, level l)
   __host__ __device__ static constexpr int acc_col(int part, int l) { return PACK ? (l * 2 + part) * BN : (part * NL + l) * BN; }
 };
-using CfgStd = SplitCfg<SPLIT_NSLICE, 4, SPLIT_N, true>;
-using CfgHP = SplitCfg<6, 5, 48, true>;
+using CfgStd = SplitCfg<SPLIT_NSLICE, 4, SPLIT_N, true, false>;
+using CfgHP = SplitCfg<6, 5, 48, true, true>;
 static_assert(CfgStd::B_STAGE == SPLIT_B_STAGE && CfgStd::A_STAGE == SPLIT_A_STAGE, "standard stage sizes");
+static_assert(CfgStd::BN % (16 * (CfgStd::EPI_WARPS / 4)) == 0 && CfgHP::BN % (16 * (CfgHP::EPI_WARPS / 4)) == 0,
+              "epilogue column split");
 
 // Slicing of a stacked operand.  Left: rows r -> row r%nev of blk[r/nev].
 struct SliceLeftJob {
