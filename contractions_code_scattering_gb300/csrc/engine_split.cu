@@ -612,33 +612,40 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
     const size_t le_b = align256(SPLIT_M * 4), re_b = align256((size_t)ntiles * CfgHP::BN * 4);
     const size_t per = l_b + r_b + le_b + re_b;  // one left and at most one distinct right per instance
     const std::vector<Inst>& all = bk.second;
-    const int batch = (int)std::max<size_t>(1, std::min<size_t>(all.size(), ((size_t)2 << 30) / per));
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(all.size(), ((size_t)4 << 30) / per));
     for (size_t i0 = 0; i0 < all.size(); i0 += batch) {
       const int ni = (int)std::min<size_t>(batch, all.size() - i0);
       void* mem;
       CTR_TRY(workspace(WS_SPLITTASK).get((size_t)ni * per, &mem));
       uint8_t* lbase = (uint8_t*)mem;                       // ni x (left slices + row exponents)
       uint8_t* rbase = lbase + (size_t)ni * (l_b + le_b);   // <= ni x (right slices + column exponents)
-      std::vector<SliceTaskLJob> lj(ni);
+      std::vector<SliceTaskLJob> lj;
       std::vector<SliceTaskRJob> rj;
+      std::map<int, int> lid;                     // instances of one left group share its slices
       std::map<std::vector<uintptr_t>, int> rid;  // identical right sides are sliced once
       std::vector<SplitGemmInst> gi(ni);
       std::vector<double2*> outs((size_t)ni * SPLIT_TASK_NB, nullptr);
       for (int i = 0; i < ni; i++) {
         const Inst& in = all[i0 + i];
         const LeftKey& k = gkey[in.g];
-        uint8_t* p = lbase + (size_t)i * (l_b + le_b);
-        SliceTaskLJob& L = lj[i];
-        std::memset(&L, 0, sizeof(L));
-        for (int q = 0; q < nterm; q++) {
-          L.a[q] = k.a[q];
-          L.w[q] = k.w[q];
+        auto lt = lid.find(in.g);
+        if (lt == lid.end()) {
+          uint8_t* p = lbase + lj.size() * (l_b + le_b);
+          SliceTaskLJob L;
+          std::memset(&L, 0, sizeof(L));
+          for (int q = 0; q < nterm; q++) {
+            L.a[q] = k.a[q];
+            L.w[q] = k.w[q];
+          }
+          L.nterm = nterm;
+          L.dag = k.dag;
+          L.eplus = eplus;
+          L.out = p;
+          L.exps = (int*)(p + l_b);
+          lt = lid.emplace(in.g, (int)lj.size()).first;
+          lj.push_back(L);
         }
-        L.nterm = nterm;
-        L.dag = k.dag;
-        L.eplus = eplus;
-        L.out = p;
-        L.exps = (int*)(p + l_b);
+        const SliceTaskLJob& L = lj[lt->second];
         SliceTaskRJob R;
         std::memset(&R, 0, sizeof(R));
         R.nb = in.nb;
@@ -672,7 +679,7 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
       CTR_TRY(upload(WS_SPLITJOBS3, outs.data(), outs.size() * sizeof(double2*), &d_outs, stream));
       for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d_outs + (size_t)i * SPLIT_TASK_NB;
       CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
-      CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, ni, N, nchunk, stream));
+      CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, (int)lj.size(), N, nchunk, stream));
       CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, (int)rj.size(), N, nchunk, ntiles, stream));
       SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N, 1};
       CTR_TRY(launch_split_gemm(G, ni, d_err, stream));

@@ -589,29 +589,30 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       tc_fence_after();
       float4* outp = I->out;
       const int ldo = g.ldo;
-      for (int c0 = half * CPW; c0 < (half + 1) * CPW; c0 += 16) {
+      for (int c0 = half * CPW; c0 < (half + 1) * CPW; c0 += C::EPI_CW) {
         if constexpr (C::INT_OUT) {
           // complex128 output: the exact levels and the last one summed exactly
           // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
-          // below 2^8, so no overflow), then rounded once to double
-          long long acc[2][16];
+          // below 2^8, so no overflow), then rounded once to double; 8 columns
+          // at a time, which keeps the registers within the 8-warp budget
+          long long acc[2][8];
 #pragma unroll
           for (int part = 0; part < 2; part++) {
 #pragma unroll
-            for (int c = 0; c < 16; c++) acc[part][c] = 0;
+            for (int c = 0; c < 8; c++) acc[part][c] = 0;
 #pragma unroll
             for (int l = 0; l < C::NL; l++) {
-              float v[16];
-              tmem_ld16(tl + (uint32_t)(C::acc_col(part, l) + c0), v);
+              float v[8];
+              tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v);
               tmem_ld_wait();
 #pragma unroll
-              for (int c = 0; c < 16; c++) acc[part][c] += f2i_scaled(v[c], 54);
+              for (int c = 0; c < 8; c++) acc[part][c] += f2i_scaled(v[c], 54);
             }
           }
           if (!rvalid) continue;
           const int erow = I->lexp[grow];
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
+          for (int c = 0; c < 8; c++) {
             const int gcol = nt * C::BN + c0 + c;
             if (gcol >= g.ncols) continue;
             const int e = erow + sexp[c0 + c] - 54;

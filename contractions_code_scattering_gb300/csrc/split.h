@@ -40,7 +40,8 @@ struct SplitCfg {
   static constexpr int NS = NS_, NL = NL_, BN = BN_;
   static constexpr bool PACK = PACK_;
   static constexpr bool INT_OUT = INT_OUT_;  // epilogue: complex128 via exact integer sums (else float-float)
-  static constexpr int EPI_WARPS = INT_OUT ? 4 : 8;  // the integer epilogue needs ~255 registers a thread
+  static constexpr int EPI_WARPS = 8;              // two per TMEM lane quadrant, splitting the columns
+  static constexpr int EPI_CW = INT_OUT ? 8 : 16;  // columns per TMEM load in the epilogue
   static constexpr int B_PLANES = PACK ? 3 : 2;
   static constexpr int A_SUB = SPLIT_M * SPLIT_K * 2;
   static constexpr int B_SUB = BN * SPLIT_K * 2;
@@ -52,7 +53,8 @@ struct SplitCfg {
 using CfgStd = SplitCfg<SPLIT_NSLICE, 4, SPLIT_N, true, false>;
 using CfgHP = SplitCfg<6, 5, 48, true, true>;
 static_assert(CfgStd::B_STAGE == SPLIT_B_STAGE && CfgStd::A_STAGE == SPLIT_A_STAGE, "standard stage sizes");
-static_assert(CfgStd::BN % (16 * (CfgStd::EPI_WARPS / 4)) == 0 && CfgHP::BN % (16 * (CfgHP::EPI_WARPS / 4)) == 0,
+static_assert(CfgStd::BN % (CfgStd::EPI_CW * (CfgStd::EPI_WARPS / 4)) == 0 &&
+                  CfgHP::BN % (CfgHP::EPI_CW * (CfgHP::EPI_WARPS / 4)) == 0,
               "epilogue column split");
 
 // Slicing of a stacked operand.  Left: rows r -> row r%nev of blk[r/nev].
