@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--graph", type=int, default=1, help="time replays of the step recorded as a CUDA graph "
                     "(the eager calls are timed beside them); 0 = eager calls only")
     ap.add_argument("--tune", type=int, default=1, help="autotune the knobs on the first warm-up step")
+    ap.add_argument("--tune-force", action="append", default=[], metavar="KNOB=VALUE",
+                    help="pin an autotuner knob (e.g. trace_rows=1), repeatable")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--nt", type=int, default=None, help="time extent (default: the workload's; a smaller value "
                                                               "gives a small case of the same kernels, e.g. for ncu)")
@@ -264,6 +266,9 @@ def main():
     ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
     api.device_init(local)
+    for kv in args.tune_force:
+        knob, val = kv.split("=")
+        api.tune_force(knob, int(val))
     nt, nev = args.nt or NT, args.nev
     moms, rows, coef, oi, nout = workload(nt, nev)
     diagrams = nt * nt * nout

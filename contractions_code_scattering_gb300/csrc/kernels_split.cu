@@ -788,6 +788,84 @@ __global__ void __launch_bounds__(TPB) trace_rows_flat_kernel(const TraceRow* __
   }
 }
 
+// Flattened walk with U independent element streams per thread: the U pairs of
+// loads of one step are issued before their sums, so each thread keeps 2U
+// 16-byte loads in flight (the traces are bound by memory latency otherwise).
+template <int TPB, int U>
+__global__ void __launch_bounds__(TPB) trace_rows_ilp_kernel(const TraceRow* __restrict__ rt, int nrows,
+                                                             const float4* const* __restrict__ abase,
+                                                             const float4* const* __restrict__ bbase, int lda,
+                                                             int ldb, int nev, double2* __restrict__ rows,
+                                                             double* __restrict__ rabs) {
+  constexpr int NW = TPB / 32;
+  const int q = blockIdx.x / nrows, r = blockIdx.x % nrows;
+  const TraceRow T = rt[r];
+  const float4* pa = abase[q] + T.aoff;
+  const float4* pb = bbase[q] + T.boff;
+  float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f, sa = 0.f;
+  const int total = nev * nev, step = TPB * U, di = step % nev, dj = step / nev;
+  int iu[U], ju[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int e = threadIdx.x + u * TPB;
+    iu[u] = e % nev;
+    ju[u] = e / nev;
+  }
+  for (int e0 = threadIdx.x; e0 < total; e0 += step) {
+    float4 a[U], b[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (e0 + u * TPB < total) {
+        a[u] = pa[(size_t)ju[u] * lda + iu[u]];
+        b[u] = pb[(size_t)ju[u] * ldb + iu[u]];
+      } else {
+        a[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        b[u] = a[u];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      ff_mac(sr, er, a[u].x, a[u].y, b[u].x, b[u].y);    // + ar br
+      ff_mac(sr, er, a[u].z, a[u].w, b[u].z, b[u].w);    // + ai bi
+      ff_mac(si, ei, a[u].z, a[u].w, b[u].x, b[u].y);    // + ai br
+      ff_mac(si, ei, -a[u].x, -a[u].y, b[u].z, b[u].w);  // - ar bi
+      sa = fmaf(fabsf(a[u].x) + fabsf(a[u].z), fabsf(b[u].x) + fabsf(b[u].z), sa);
+      iu[u] += di;
+      ju[u] += dj;
+      if (iu[u] >= nev) {
+        iu[u] -= nev;
+        ju[u]++;
+      }
+    }
+  }
+  double re = (double)sr + (double)er, im = (double)si + (double)ei, ab = (double)sa;
+  __shared__ double red[3][NW];
+  for (int o = 16; o; o >>= 1) {
+    re += __shfl_down_sync(0xffffffffu, re, o);
+    im += __shfl_down_sync(0xffffffffu, im, o);
+    ab += __shfl_down_sync(0xffffffffu, ab, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = re;
+    red[1][threadIdx.x >> 5] = im;
+    red[2][threadIdx.x >> 5] = ab;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    re = 0.0;
+    im = 0.0;
+    ab = 0.0;
+    for (int w = 0; w < NW; w++) {
+      re += red[0][w];
+      im += red[1][w];
+      ab += red[2][w];
+    }
+    const double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+    rows[blockIdx.x] = cmul(c, make_double2(re, im));
+    rabs[blockIdx.x] = sqrt(c.x * c.x + c.y * c.y) * ab;
+  }
+}
+
 // --------------------------------------------------------------- launchers
 // Dynamic shared-memory limits are raised once per kernel (before any graph
 // capture, through split_kernels_prepare, or at the first launch).
@@ -919,6 +997,18 @@ int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_
     case 3:
       trace_rows_flat_kernel<512>
           <<<(unsigned)nblk, 512, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 4:
+      trace_rows_ilp_kernel<128, 4>
+          <<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 5:
+      trace_rows_ilp_kernel<256, 2>
+          <<<(unsigned)nblk, 256, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 6:
+      trace_rows_ilp_kernel<64, 4>
+          <<<(unsigned)nblk, 64, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
       break;
     default: return fail(CTR_ERR_ARG, "traces: unknown variant %d", variant);
   }

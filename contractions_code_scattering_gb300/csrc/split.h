@@ -158,8 +158,10 @@ int split_kernels_prepare();
 // (leading dimensions lda / ldb); rows[q * nrows + r] = coef_r * trace and
 // rabs[q * nrows + r] = |coef_r| sum |A|_1 |B|_1.
 // variant: 0 one thread per row i walking the columns (128 threads), 1/2/3 the
-// flattened element walk with 128/256/512 threads (TRACE_VARIANTS candidates).
-constexpr int TRACE_VARIANTS = 4;
+// flattened element walk with 128/256/512 threads, 4/5/6 the flattened walk with
+// 4/2/4 independent streams a thread and 128/256/64 threads (TRACE_VARIANTS
+// candidates).
+constexpr int TRACE_VARIANTS = 7;
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
                       int lda, int ldb, int npair, int nev, double2* rows, double* rabs, int variant,
                       cudaStream_t s);
