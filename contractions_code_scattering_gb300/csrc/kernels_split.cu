@@ -351,24 +351,14 @@ constexpr int NSTAGE = 3;
 constexpr uint32_t TMEM_COLS = 512;  // (re, im) x NL levels x BN columns fit in 512 for both configurations
 constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
 
+constexpr int GEMM_SMEM_TAIL = 1024;  // barriers, TMEM slot, column exponents and output pointers
+
 template <class C>
 constexpr size_t gemm_smem_bytes() {
-  return (size_t)NSTAGE * (C::A_STAGE + C::B_STAGE) + 512;
+  return (size_t)NSTAGE * (C::A_STAGE + C::B_STAGE) + GEMM_SMEM_TAIL;
 }
 static_assert(2 * CfgStd::NL * CfgStd::BN <= (int)TMEM_COLS && 2 * CfgHP::NL * CfgHP::BN <= (int)TMEM_COLS,
               "accumulators exceed TMEM");
-
-// x * 2^K as an exact 64-bit integer (|x| 2^K < 2^62), bits below 2^0 dropped
-// toward zero; integer operations only.
-__device__ __forceinline__ long long f2i_scaled(float x, int K) {
-  const uint32_t b = __float_as_uint(x);
-  const int be = (int)((b >> 23) & 0xFF);
-  if (be == 0) return 0;
-  const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
-  const int sh = be - 150 + K;
-  const long long v = sh >= 0 ? (m << sh) : (sh > -40 ? (m >> -sh) : 0);
-  return (b >> 31) ? -v : v;
-}
 
 // I * 2^e as a double, rounded to nearest even; integer operations only
 // (normal results; magnitudes below 2^-1022 flush to zero).
@@ -474,6 +464,9 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
   uint64_t* drainb = tempty + 1;
   uint32_t* tslot = (uint32_t*)(drainb + 1);
   int* sexp = (int*)(tslot + 4);  // C::BN column exponents of the current tile
+  // complex128 output: destination of row 0 of each column of the current tile
+  double2** colp = (double2**)(smem + NSTAGE * (C::A_STAGE + C::B_STAGE) + 512);
+  static_assert(512 + 8 * C::BN <= GEMM_SMEM_TAIL && 16 * 8 + 16 + 4 * C::BN <= 512, "GEMM shared-memory tail");
 
   volatile int* status = (volatile int*)(tslot + 1);  // block-uniform decisions
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -573,7 +566,13 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       // stage this tile's column exponents; the barrier also keeps the previous
       // tile's values until every epilogue thread has used them
       epi_bar<32 * C::EPI_WARPS>();
-      if (et < C::BN) sexp[et] = I->rexp[nt * C::BN + et];
+      if (et < C::BN) {
+        sexp[et] = I->rexp[nt * C::BN + et];
+        if constexpr (C::INT_OUT) {
+          const int gcol = nt * C::BN + et;
+          colp[et] = gcol < g.ncols ? I->outs[gcol / g.blkn] + (gcol % g.blkn) : nullptr;
+        }
+      }
       const int grow = mt * SPLIT_M + row;
       const bool rvalid = grow < g.mrows;
       const float srow = pow2f(I->lexp[grow]);
@@ -595,29 +594,35 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
           // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
           // below 2^8, so no overflow), then rounded once to double; 8 columns
           // at a time, which keeps the registers within the 8-warp budget
+          // Level l < NL-1 holds integer multiples of 2^-(16+9l) (products of
+          // digits d_i 2^(-8-9i) with i+j = l), at most 2^28 of them, so one
+          // FP32 -> int32 conversion of v 2^(16+9l) is exact; the last level is
+          // rounded to 2^-54 (|v| < 2^-20 there).
           long long acc[2][8];
 #pragma unroll
           for (int part = 0; part < 2; part++) {
+            float v[C::NL][8];
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[part][c] = 0;
+            for (int l = 0; l < C::NL; l++) tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+            tmem_ld_wait();
 #pragma unroll
-            for (int l = 0; l < C::NL; l++) {
-              float v[8];
-              tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v);
-              tmem_ld_wait();
+            for (int c = 0; c < 8; c++) {
+              long long a = 0;
 #pragma unroll
-              for (int c = 0; c < 8; c++) acc[part][c] += f2i_scaled(v[c], 54);
+              for (int l = 0; l < C::NL - 1; l++)
+                a += (long long)__float2int_rn(v[l][c] * __int_as_float((127 + 16 + 9 * l) << 23)) << (38 - 9 * l);
+              a += __float2ll_rn(v[C::NL - 1][c] * __int_as_float((127 + 54) << 23));
+              acc[part][c] = a;
             }
           }
           if (!rvalid) continue;
           const int erow = I->lexp[grow];
 #pragma unroll
           for (int c = 0; c < 8; c++) {
-            const int gcol = nt * C::BN + c0 + c;
-            if (gcol >= g.ncols) continue;
+            double2* dst = colp[c0 + c];
+            if (!dst) continue;
             const int e = erow + sexp[c0 + c] - 54;
-            const int j = gcol / g.blkn, cc = gcol - j * g.blkn;
-            I->outs[j][(size_t)grow * g.blkn + cc] = make_double2(i2d_scaled(acc[0][c], e), i2d_scaled(acc[1][c], e));
+            dst[(size_t)grow * g.blkn] = make_double2(i2d_scaled(acc[0][c], e), i2d_scaled(acc[1][c], e));
           }
           continue;
         } else {
