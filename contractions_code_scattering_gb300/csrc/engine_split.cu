@@ -679,6 +679,8 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
       CTR_TRY(upload(WS_SPLITJOBS3, outs.data(), outs.size() * sizeof(double2*), &d_outs, stream));
       for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d_outs + (size_t)i * SPLIT_TASK_NB;
       CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
+      CTR_TRY(launch_slice_task_exp((const SliceTaskLJob*)d_lj, (int)lj.size(), (const SliceTaskRJob*)d_rj,
+                                    (int)rj.size(), N, ntiles, stream));
       CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, (int)lj.size(), N, nchunk, stream));
       CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, (int)rj.size(), N, nchunk, ntiles, stream));
       SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N, 1};

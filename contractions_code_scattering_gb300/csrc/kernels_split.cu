@@ -122,13 +122,22 @@ __global__ void __launch_bounds__(256) slice_left_kernel(const SliceLeftJob* __r
   }
   __syncthreads();
   uint8_t* dst_tile = J.out + (size_t)mt * nchunk * SPLIT_A_STAGE;
+  constexpr int PER = SPLIT_M * SPLIT_K / 256;
   for (int kc = 0; kc < nchunk; kc++) {
-    // 128 rows x 16 k: 16 consecutive threads read one row segment (coalesced)
-    for (int e = threadIdx.x; e < SPLIT_M * SPLIT_K; e += 256) {
+    // 128 rows x 16 k: 16 consecutive threads read one row segment (coalesced);
+    // a thread's 8 loads are issued before any of them is sliced
+    double2 vv[PER];
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u;
+      const int r = mt * SPLIT_M + (e >> 4), k = kc * SPLIT_K + (e & 15);
+      vv[u] = (r < J.rows && k < nev) ? J.blk[r / nev][(size_t)(r % nev) * nev + k] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u;
       const int rr = e >> 4, kk = e & 15;
-      const int r = mt * SPLIT_M + rr, k = kc * SPLIT_K + kk;
-      double2 v = make_double2(0.0, 0.0);
-      if (r < J.rows && k < nev) v = J.blk[r / nev][(size_t)(r % nev) * nev + k];
+      const double2 v = vv[u];
       const int E = sexp[rr];
       bool nr, ni;
       const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
@@ -157,29 +166,47 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
   uint8_t* stage = sm + 512;
   const SliceRightJob& J = jobs[blockIdx.x / ntiles];
   const int nt = blockIdx.x % ntiles;
-  // column exponents: thread n scans column n (consecutive threads read consecutive columns)
-  if (threadIdx.x < SPLIT_N) {
-    const int n = nt * SPLIT_N + threadIdx.x;
+  // column exponents: 4 threads per column (rows k = kq mod 4; consecutive
+  // threads read consecutive columns), partial maxima combined in shared memory
+  __shared__ int part[256];
+  {
+    const int nn = threadIdx.x % SPLIT_N, kq = threadIdx.x / SPLIT_N;
+    const int n = nt * SPLIT_N + nn;
     int e = -30000;
     if (n < J.cols) {
       const double2* col = J.blk[n / nev] + (n % nev);
-      for (int k = 0; k < nev; k++) {
-        double2 v = col[(size_t)k * nev];
+#pragma unroll 5
+      for (int k = kq; k < nev; k += 4) {
+        const double2 v = col[(size_t)k * nev];
         e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
       }
     }
+    part[threadIdx.x] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x < SPLIT_N) {
+    const int* q = part + threadIdx.x;
+    const int e = max(max(q[0], q[SPLIT_N]), max(q[2 * SPLIT_N], q[3 * SPLIT_N]));
     const int E = e < -1000 ? 0 : e;
     sexp[threadIdx.x] = E;
-    J.exps[n] = E;  // exps sized ntiles * SPLIT_N (padding columns get 0)
+    J.exps[nt * SPLIT_N + threadIdx.x] = E;  // exps sized ntiles * SPLIT_N (padding columns get 0)
   }
   __syncthreads();
   uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE;
+  constexpr int PER = SPLIT_N * SPLIT_K / 256;
   for (int kc = 0; kc < nchunk; kc++) {
-    for (int e = threadIdx.x; e < SPLIT_N * SPLIT_K; e += 256) {
+    double2 vv[PER];
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u;
+      const int n = nt * SPLIT_N + e % SPLIT_N, k = kc * SPLIT_K + e / SPLIT_N;
+      vv[u] = (n < J.cols && k < nev) ? J.blk[n / nev][(size_t)k * nev + (n % nev)] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u;
       const int nn = e % SPLIT_N, kk = e / SPLIT_N;
-      const int n = nt * SPLIT_N + nn, k = kc * SPLIT_K + kk;
-      double2 v = make_double2(0.0, 0.0);
-      if (n < J.cols && k < nev) v = J.blk[n / nev][(size_t)k * nev + (n % nev)];
+      const double2 v = vv[u];
       const int E = sexp[nn];
       bool nr, ni;
       const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
@@ -229,112 +256,223 @@ __device__ __forceinline__ double2 task_right_elem(const SliceTaskRJob& J, int n
   return v;
 }
 
-// Left operand of a task instance (one M tile: rows < nev; K = nterm * nev).
+// Every (block, term) of a right job conjugate-transposed.
+__device__ __forceinline__ bool task_right_all_dag(const SliceTaskRJob& J) {
+  const int m = (1 << J.nterm) - 1;
+  for (int j = 0; j < J.nb; j++)
+    if (((J.dag >> (4 * j)) & m) != m) return false;
+  return true;
+}
+
+// Task-form slicing runs in two launches: the scale exponents (one CTA per left
+// operand and one per right N tile, scanning their rows / columns over all K),
+// then the slices, one CTA per (operand tile, K chunk), so that a stage with few
+// operands still spreads over every SM.
+//
+// Exponents.  Blocks [0, nleft): left job b, 8 warps x 16 rows; blocks
+// [nleft, nleft + nright * ntiles): right job (b - nleft) / ntiles, N tile
+// (b - nleft) % ntiles, 4 threads per column.
+template <class C>
+__global__ void __launch_bounds__(256) slice_task_exp_kernel(const SliceTaskLJob* __restrict__ ljobs, int nleft,
+                                                             const SliceTaskRJob* __restrict__ rjobs, int nev,
+                                                             int ntiles) {
+  __shared__ int part[256];
+  if ((int)blockIdx.x < nleft) {
+    const SliceTaskLJob& J = ljobs[blockIdx.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int K = J.nterm * nev;
+    if (J.dag == (1 << J.nterm) - 1) {
+      // conjugate-transposed terms: row r is contiguous across threads; a thread
+      // owns row r = tid % 128 and the k of one parity
+      const int r = threadIdx.x % SPLIT_M, kq = threadIdx.x / SPLIT_M;
+      int e = -30000;
+      if (r < nev)
+        for (int k0 = kq; k0 < K; k0 += 8) {
+          double2 v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int k = k0 + 2 * u;
+            v[u] = k < K ? task_left_elem(J, nev, r, k) : make_double2(0.0, 0.0);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) e = max(e, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
+        }
+      part[threadIdx.x] = e;
+      __syncthreads();
+      if (threadIdx.x < SPLIT_M) {
+        const int m = max(part[threadIdx.x], part[threadIdx.x + SPLIT_M]);
+        J.exps[threadIdx.x] = (m < -1000 ? 0 : m) + J.eplus;
+      }
+      return;
+    }
+    // two rows at a time, four loads of each in flight per lane
+    for (int r0 = 2 * warp; r0 < SPLIT_M; r0 += 16) {
+      int e[2] = {-30000, -30000};
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int rr = r0 + h;
+        if (rr >= nev) continue;
+        for (int k0 = lane; k0 < K; k0 += 128) {
+          double2 v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int k = k0 + 32 * u;
+            v[u] = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) e[h] = max(e[h], max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        for (int o = 16; o; o >>= 1) e[h] = max(e[h], __shfl_xor_sync(0xffffffffu, e[h], o));
+        if (lane == 0) J.exps[r0 + h] = (e[h] < -1000 ? 0 : e[h]) + J.eplus;
+      }
+    }
+    return;
+  }
+  const int b = blockIdx.x - nleft;
+  const SliceTaskRJob& J = rjobs[b / ntiles];
+  const int nt = b % ntiles;
+  const int K = J.nterm * nev, ncols = J.nb * nev;
+  if (task_right_all_dag(J)) {
+    // conjugate-transposed blocks: a column is contiguous in k; warp w scans
+    // columns w, w + 8, ... with its lanes along k
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int nn = warp; nn < C::BN; nn += 8) {
+      const int n = nt * C::BN + nn;
+      int e = -30000;
+      if (n < ncols)
+        for (int k0 = lane; k0 < K; k0 += 128) {
+          double2 v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int k = k0 + 32 * u;
+            v[u] = k < K ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) e = max(e, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
+        }
+      for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+      if (lane == 0) J.exps[nt * C::BN + nn] = (e < -1000 ? 0 : e) + J.eplus;
+    }
+    return;
+  }
+  // 4 threads per column (k = kq mod 4), four loads in flight each
+  const int nn = threadIdx.x % C::BN, kq = threadIdx.x / C::BN;
+  const int n = nt * C::BN + nn;
+  int e = -30000;
+  if (n < ncols && kq < 4)
+    for (int k0 = kq; k0 < K; k0 += 16) {
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int k = k0 + 4 * u;
+        v[u] = k < K ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) e = max(e, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
+    }
+  part[threadIdx.x] = e;
+  __syncthreads();
+  if (threadIdx.x < C::BN) {
+    const int* q = part + threadIdx.x;
+    const int m = max(max(q[0], q[C::BN]), max(q[2 * C::BN], q[3 * C::BN]));
+    J.exps[nt * C::BN + threadIdx.x] = (m < -1000 ? 0 : m) + J.eplus;
+  }
+}
+
+// Left operand slices: CTA = (job, K chunk); 128 rows x 16 k, 8 elements a thread.
 template <class C>
 __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJob* __restrict__ jobs, int nev,
                                                               int nchunk) {
   extern __shared__ __align__(128) uint8_t sm[];
   int* sexp = (int*)sm;
   uint8_t* stage = sm + 512;
-  const SliceTaskLJob& J = jobs[blockIdx.x];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const SliceTaskLJob& J = jobs[blockIdx.x / nchunk];
+  const int kc = blockIdx.x % nchunk;
   const int K = J.nterm * nev;
-  for (int rr = warp; rr < SPLIT_M; rr += 8) {
-    int e = -30000;
-    if (rr < nev)
-      for (int k = lane; k < K; k += 32) {
-        const double2 v = task_left_elem(J, nev, rr, k);
-        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
-      }
-    for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-    if (lane == 0) {
-      const int E = (e < -1000 ? 0 : e) + J.eplus;
-      sexp[rr] = E;
-      J.exps[rr] = E;
+  if (threadIdx.x < SPLIT_M) sexp[threadIdx.x] = J.exps[threadIdx.x];
+  // 16 consecutive threads along k: shared-memory stores without bank conflicts
+  constexpr int PER = SPLIT_M * SPLIT_K / 256;
+  double2 v[PER];
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 256;
+    const int rr = e >> 4, k = kc * SPLIT_K + (e & 15);
+    v[u] = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 256;
+    const int rr = e >> 4, kk = e & 15;
+    const int E = sexp[rr];
+    bool nr, ni;
+    const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v[u].x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v[u].y, E, ni));
+    const uint32_t off = core_offset(rr, kk);
+#pragma unroll
+    for (int s = 0; s < C::NS; s++) {
+      *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::A_SUB + off) = slice_bf16(Ur, s, nr);
+      *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::A_SUB + off) = slice_bf16(Ui, s, ni);
     }
   }
   __syncthreads();
-  for (int kc = 0; kc < nchunk; kc++) {
-    for (int e = threadIdx.x; e < SPLIT_M * SPLIT_K; e += 256) {
-      const int rr = e >> 4, kk = e & 15, k = kc * SPLIT_K + kk;
-      const double2 v = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
-      const int E = sexp[rr];
-      bool nr, ni;
-      const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v.x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v.y, E, ni));
-      const uint32_t off = core_offset(rr, kk);
-#pragma unroll
-      for (int s = 0; s < C::NS; s++) {
-        *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::A_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::A_SUB + off) = slice_bf16(Ui, s, ni);
-      }
-    }
-    __syncthreads();
-    int4* d = (int4*)(J.out + (size_t)kc * C::A_STAGE);
-    const int4* src = (const int4*)stage;
-    for (int i = threadIdx.x; i < C::A_STAGE / 16; i += 256) d[i] = src[i];
-    __syncthreads();
-  }
+  int4* d = (int4*)(J.out + (size_t)kc * C::A_STAGE);
+  const int4* src = (const int4*)stage;
+  for (int i = threadIdx.x; i < C::A_STAGE / 16; i += 256) d[i] = src[i];
 }
 
-// Right operand of a task instance: N tile nt of the nb stacked output blocks.
+// Right operand slices: CTA = (job, N tile, K chunk); BN columns x 16 k.
 template <class C>
 __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
                                                                int nchunk, int ntiles) {
   extern __shared__ __align__(128) uint8_t sm[];
-  int* sexp = (int*)sm;  // [0, 64): exponents; [64, 320): per-thread partial maxima (4 per column)
-  uint8_t* stage = sm + 2048;
-  const SliceTaskRJob& J = jobs[blockIdx.x / ntiles];
-  const int nt = blockIdx.x % ntiles;
+  int* sexp = (int*)sm;
+  uint8_t* stage = sm + 512;
+  const int kc = blockIdx.x % nchunk, t = blockIdx.x / nchunk;
+  const SliceTaskRJob& J = jobs[t / ntiles];
+  const int nt = t % ntiles;
   const int K = J.nterm * nev, ncols = J.nb * nev;
-  // column exponents: 4 threads per column (k = kq, kq+4, ...), combined in shared memory
-  {
-    const int nn = threadIdx.x % C::BN, kq = threadIdx.x / C::BN;
-    const int n = nt * C::BN + nn;
-    int e = -30000;
-    if (n < ncols && kq < 4)
-      for (int k = kq; k < K; k += 4) {
-        const double2 v = task_right_elem(J, nev, k, n);
-        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
-      }
-    sexp[64 + threadIdx.x] = e;
-  }
-  __syncthreads();
-  if (threadIdx.x < C::BN) {
-    const int* q = sexp + 64 + threadIdx.x;
-    const int e = max(max(q[0], q[C::BN]), max(q[2 * C::BN], q[3 * C::BN]));
-    const int E = (e < -1000 ? 0 : e) + J.eplus;
-    sexp[threadIdx.x] = E;
-    J.exps[nt * C::BN + threadIdx.x] = E;
-  }
-  __syncthreads();
-  uint8_t* dst_tile = J.out + (size_t)nt * nchunk * C::B_STAGE;
-  for (int kc = 0; kc < nchunk; kc++) {
-    for (int e = threadIdx.x; e < C::BN * SPLIT_K; e += 256) {
-      const int nn = e % C::BN, kk = e / C::BN;
-      const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
-      const double2 v = (n < ncols && k < K) ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
-      const int E = sexp[nn];
-      bool nr, ni;
-      const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v.x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v.y, E, ni));
-      const uint32_t off = core_offset(nn, kk);
+  if (threadIdx.x < C::BN) sexp[threadIdx.x] = J.exps[nt * C::BN + threadIdx.x];
+  // consecutive threads along the columns, or, for conjugate-transposed blocks
+  // (contiguous in k), along k
+  const bool tr = task_right_all_dag(J);
+  constexpr int PER = (C::BN * SPLIT_K + 255) / 256;
+  double2 v[PER];
 #pragma unroll
-      for (int s = 0; s < C::NS; s++) {
-        if (C::PACK) {
-          *(__nv_bfloat16*)(stage + (s * 3 + 0) * C::B_SUB + off) = slice_bf16(Ui, s, !ni);
-          *(__nv_bfloat16*)(stage + (s * 3 + 1) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
-          *(__nv_bfloat16*)(stage + (s * 3 + 2) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
-        } else {
-          *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
-          *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
-        }
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 256;
+    const int nn = tr ? (e >> 4) : (e % C::BN), kk = tr ? (e & 15) : (e / C::BN);
+    const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
+    v[u] = (e < C::BN * SPLIT_K && n < ncols && k < K) ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 256;
+    if (e >= C::BN * SPLIT_K) break;
+    const int nn = tr ? (e >> 4) : (e % C::BN), kk = tr ? (e & 15) : (e / C::BN);
+    const int E = sexp[nn];
+    bool nr, ni;
+    const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v[u].x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v[u].y, E, ni));
+    const uint32_t off = core_offset(nn, kk);
+#pragma unroll
+    for (int s = 0; s < C::NS; s++) {
+      if (C::PACK) {
+        *(__nv_bfloat16*)(stage + (s * 3 + 0) * C::B_SUB + off) = slice_bf16(Ui, s, !ni);
+        *(__nv_bfloat16*)(stage + (s * 3 + 1) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 3 + 2) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
+      } else {
+        *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
+        *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
       }
     }
-    __syncthreads();
-    int4* d = (int4*)(dst_tile + (size_t)kc * C::B_STAGE);
-    const int4* src = (const int4*)stage;
-    for (int i = threadIdx.x; i < C::B_STAGE / 16; i += 256) d[i] = src[i];
-    __syncthreads();
   }
+  __syncthreads();
+  int4* d = (int4*)(J.out + ((size_t)nt * nchunk + kc) * C::B_STAGE);
+  const int4* src = (const int4*)stage;
+  for (int i = threadIdx.x; i < C::B_STAGE / 16; i += 256) d[i] = src[i];
 }
 
 // ------------------------------------------------------------------ GEMM
@@ -909,7 +1047,7 @@ int split_kernels_prepare() {
   CTR_TRY(ensure_smem(slice_left_kernel, 512 + SPLIT_A_STAGE, g_attr_sl));
   CTR_TRY(ensure_smem(slice_right_kernel, 512 + SPLIT_B_STAGE, g_attr_sr));
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
-  CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 2048 + CfgHP::B_STAGE, g_attr_tr));
+  CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
   return CTR_OK;
@@ -940,17 +1078,27 @@ int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int 
   const size_t smem = 512 + CfgHP::A_STAGE;
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, smem, g_attr_tl));
   TimedLaunch tl(s, "slice_task_left");
-  slice_task_left_kernel<CfgHP><<<njobs, 256, smem, s>>>(d_jobs, nev, nchunk);
+  slice_task_left_kernel<CfgHP><<<njobs * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
 
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
-  const size_t smem = 2048 + CfgHP::B_STAGE;
+  const size_t smem = 512 + CfgHP::B_STAGE;
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, smem, g_attr_tr));
   TimedLaunch tl(s, "slice_task_right");
-  slice_task_right_kernel<CfgHP><<<njobs * ntiles, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+  slice_task_right_kernel<CfgHP><<<njobs * ntiles * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_slice_task_exp(const SliceTaskLJob* d_ljobs, int nleft, const SliceTaskRJob* d_rjobs, int nright, int nev,
+                          int ntiles, cudaStream_t s) {
+  const long long nblk = (long long)nleft + (long long)nright * ntiles;
+  if (nblk == 0) return CTR_OK;
+  TimedLaunch tl(s, "slice_task_exp");
+  slice_task_exp_kernel<CfgHP><<<(unsigned)nblk, 256, 0, s>>>(d_ljobs, nleft, d_rjobs, nev, ntiles);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

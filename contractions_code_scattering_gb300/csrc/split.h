@@ -165,6 +165,10 @@ constexpr int TRACE_VARIANTS = 7;
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
                       int lda, int ldb, int npair, int nev, double2* rows, double* rabs, int variant,
                       cudaStream_t s);
+// Task-form slicing: the exponents of every left job and right N tile first
+// (launch_slice_task_exp), then the slices of each (operand tile, K chunk).
+int launch_slice_task_exp(const SliceTaskLJob* d_ljobs, int nleft, const SliceTaskRJob* d_rjobs, int nright, int nev,
+                          int ntiles, cudaStream_t s);
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s);
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
 
