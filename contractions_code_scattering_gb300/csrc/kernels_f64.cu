@@ -2,10 +2,11 @@
 // deterministic row sums and the source-time average.
 //
 // On GB300 the FP64 pipe delivers about 2 DFMA per clock per SM, so these
-// kernels are bound by that pipe, not by memory: the design goal is to keep the
-// pipe busy with no padded work (threads whose outputs fall outside the Nev x
-// Nev block issue no DFMA) and to keep the summation order of the reference
-// (k ascending for every matrix element).
+// kernels are bound by that pipe, not by memory.  A warp's DFMA occupies the
+// pipe for all 32 lanes, also where lanes are masked off, so the design goal is
+// tiles that cover the Nev x Nev block without padded lanes (the tile edge is
+// an autotuner choice: 32, 50 or 20) while keeping the summation order of the
+// reference (k ascending for every matrix element).
 #include <algorithm>
 
 #include "kernels.h"
@@ -93,6 +94,97 @@ __global__ void __launch_bounds__(256) zgemm_f64_kernel(const ZTask* __restrict_
       int gi = i0 + ty + 16 * a, gj = j0 + tx + 16 * b;
       if (gi < N && gj < N) T.C[(size_t)gi * N + gj] = acc[a][b];
     }
+}
+
+// The same product with a T x T output tile: (T/TM) x (T/TN) threads, thread
+// (ty, tx) computing rows ty + a T/TM (a < TM) and columns tx + b T/TN (b < TN),
+// K staged KC at a time.  T = 50 covers Nev = 100 with 250 busy lanes of 256.
+template <int T, int TM, int TN, int KC>
+__global__ void __launch_bounds__((T / TM) * (T / TN), 2) zgemm_f64_tile_kernel(const ZTask* __restrict__ tasks,
+                                                                             int ntask, int N, int tiles_per_dim) {
+  constexpr int RY = T / TM, RX = T / TN, NT = RY * RX;
+  static_assert(RY * TM == T && RX * TN == T, "tile split");
+  __shared__ double2 As[T][KC + 1];
+  __shared__ double2 Bs[KC][T + 1];
+  const int tiles = tiles_per_dim * tiles_per_dim;
+  const int task_id = blockIdx.x / tiles;
+  if (task_id >= ntask) return;
+  const int tile = blockIdx.x % tiles;
+  const int i0 = (tile / tiles_per_dim) * T, j0 = (tile % tiles_per_dim) * T;
+  const ZTask& Tk = tasks[task_id];
+  const int ty = threadIdx.x / RX, tx = threadIdx.x % RX;
+  bool rv[TM], cv[TN];
+#pragma unroll
+  for (int a = 0; a < TM; a++) rv[a] = i0 + ty + a * RY < N;
+#pragma unroll
+  for (int b = 0; b < TN; b++) cv[b] = j0 + tx + b * RX < N;
+
+  double2 acc[TM][TN];
+#pragma unroll
+  for (int a = 0; a < TM; a++)
+#pragma unroll
+    for (int b = 0; b < TN; b++) acc[a][b] = make_double2(0.0, 0.0);
+
+  for (int q = 0; q < Tk.nterm; q++) {
+    const double2* A = Tk.A[q];
+    const double2* B = Tk.B[q];
+    const bool ca = (Tk.flags >> q) & 1, cb = (Tk.flags >> (4 + q)) & 1;
+    double2 part[TM][TN];
+#pragma unroll
+    for (int a = 0; a < TM; a++)
+#pragma unroll
+      for (int b = 0; b < TN; b++) part[a][b] = make_double2(0.0, 0.0);
+    for (int k0 = 0; k0 < N; k0 += KC) {
+      for (int e = threadIdx.x; e < T * KC; e += NT) {
+        const int r = e / KC, c = e % KC, gi = i0 + r, gk = k0 + c;
+        double2 v = make_double2(0.0, 0.0);
+        if (gi < N && gk < N) {
+          if (!ca) v = A[(size_t)gi * N + gk];
+          else { v = A[(size_t)gk * N + gi]; v.y = -v.y; }
+        }
+        As[r][c] = v;
+        const int rk = e / T, cj = e % T, gk2 = k0 + rk, gj = j0 + cj;
+        double2 u = make_double2(0.0, 0.0);
+        if (gk2 < N && gj < N) {
+          if (!cb) u = B[(size_t)gk2 * N + gj];
+          else { u = B[(size_t)gj * N + gk2]; u.y = -u.y; }
+        }
+        Bs[rk][cj] = u;
+      }
+      __syncthreads();
+      const int kmax = min(KC, N - k0);
+      for (int kk = 0; kk < kmax; kk++) {
+        double2 av[TM], bv[TN];
+#pragma unroll
+        for (int a = 0; a < TM; a++) av[a] = As[ty + a * RY][kk];
+#pragma unroll
+        for (int b = 0; b < TN; b++) bv[b] = Bs[kk][tx + b * RX];
+#pragma unroll
+        for (int a = 0; a < TM; a++)
+#pragma unroll
+          for (int b = 0; b < TN; b++)
+            if (rv[a] && cv[b]) cmac(part[a][b], av[a], bv[b]);
+      }
+      __syncthreads();
+    }
+    const double2 w = make_double2((double)Tk.wre[q], (double)Tk.wim[q]);
+#pragma unroll
+    for (int a = 0; a < TM; a++)
+#pragma unroll
+      for (int b = 0; b < TN; b++) {
+        if (q == 0 && w.x == 1.0 && w.y == 0.0) acc[a][b] = part[a][b];
+        else {
+          const double2 t = cmul(w, part[a][b]);
+          acc[a][b].x += t.x;
+          acc[a][b].y += t.y;
+        }
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < TM; a++)
+#pragma unroll
+    for (int b = 0; b < TN; b++)
+      if (rv[a] && cv[b]) Tk.C[(size_t)(i0 + ty + a * RY) * N + (j0 + tx + b * RX)] = acc[a][b];
 }
 
 // ---------------------------------------------------------------- trace
@@ -219,15 +311,38 @@ __global__ void source_average_kernel(int Nt, int ncorr, const double2* __restri
 }
 
 // --------------------------------------------------------------- launchers
-int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s) {
-  if (ntask == 0) return CTR_OK;
-  int tpd = (N + GT - 1) / GT;
-  long long blocks = (long long)ntask * tpd * tpd;
+// Tile variants of the FP64 block GEMM (autotuner knob "zgemm_f64.tile").
+static const int kTileEdge[] = {32, 50, 20};
+constexpr int kTileVariants = 3;
+
+static int launch_zgemm_variant(int v, const ZTask* d_tasks, int ntask, int N, cudaStream_t s) {
+  const int T = kTileEdge[v];
+  const int tpd = (N + T - 1) / T;
+  const long long blocks = (long long)ntask * tpd * tpd;
   if (blocks > 0x7fffffffLL) return fail(CTR_ERR_ARG, "zgemm_f64: too many tasks (%d)", ntask);
   TimedLaunch tl(s, "zgemm_f64");
-  zgemm_f64_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_tasks, ntask, N, tpd);
+  switch (v) {
+    case 0: zgemm_f64_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_tasks, ntask, N, tpd); break;
+    case 1: zgemm_f64_tile_kernel<50, 5, 2, 10><<<(unsigned)blocks, 250, 0, s>>>(d_tasks, ntask, N, tpd); break;
+    default: zgemm_f64_tile_kernel<20, 2, 1, 10><<<(unsigned)blocks, 200, 0, s>>>(d_tasks, ntask, N, tpd); break;
+  }
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
+}
+
+int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s) {
+  if (ntask == 0) return CTR_OK;
+  // default: the edge whose tiles pad Nev least (ties to the larger tile)
+  int dflt = 0;
+  long long best = -1;
+  for (int v = 0; v < kTileVariants; v++) {
+    const long long T = kTileEdge[v], cover = ((N + T - 1) / T) * T;
+    if (best < 0 || cover < best) best = cover, dflt = v;
+  }
+  int v = dflt;
+  CTR_TRY(tune_resolve("zgemm_f64.tile", "nev=" + std::to_string(N), kTileVariants, dflt, s,
+                       [&](int c) { return launch_zgemm_variant(c, d_tasks, ntask, N, s); }, &v));
+  return launch_zgemm_variant(v, d_tasks, ntask, N, s);
 }
 
 int launch_trace_f64(const TraceTask* d_tasks, int ntask, int N, cudaStream_t s) {

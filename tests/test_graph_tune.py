@@ -249,3 +249,20 @@ def test_autotuner_measures_and_candidates_agree(cuda):
     finally:
         api.tune_set_mode(0)
         api.tune_clear()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [20, 37, 50])
+def test_fp64_gemm_tile_variants(cuda, n):
+    """Every FP64 block-GEMM tile edge (32, 50, 20) gives the oracle's rho to 1e-12."""
+    nt = 3
+    prop, mom5 = _rho_inputs(nt, n, seed=404 + n)
+    ref = O.rho(prop, mom5)
+    d_prop, d_mom = torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda)
+    try:
+        for v in range(3):
+            api.tune_force("zgemm_f64.tile", v)
+            got = api.run_contract_rho(d_prop, d_mom, engine="fp64").cpu().numpy()
+            assert np.abs(got - ref).max() / np.abs(ref).max() <= 1e-12, v
+    finally:
+        api.tune_force("zgemm_f64.tile", -1)
