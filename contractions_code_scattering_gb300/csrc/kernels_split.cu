@@ -766,15 +766,21 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
         } else {
         // float-float output: levels 0 .. NL-2 exact, combined by exact two-sums;
         // the rounding errors and the last level go to the low word
-        float hi[2][16], lo[2][16];
+        constexpr int CW = C::EPI_CW;
+        float hi[2][CW], lo[2][CW];
 #pragma unroll
         for (int part = 0; part < 2; part++) {
-          float v[C::NL][16];
+          float v[C::NL][CW];
 #pragma unroll
-          for (int l = 0; l < C::NL; l++) tmem_ld16(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+          for (int l = 0; l < C::NL; l++) {
+            if constexpr (CW == 16)
+              tmem_ld16(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+            else
+              tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+          }
           tmem_ld_wait();
           if (g.levels && rvalid) {
-            for (int c = 0; c < 16; c++) {
+            for (int c = 0; c < CW; c++) {
               const int gcol = nt * C::BN + c0 + c;
               if (gcol < g.ncols)
                 for (int l = 0; l < C::NL; l++)
@@ -782,7 +788,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             }
           }
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
+          for (int c = 0; c < CW; c++) {
             float s = v[0][c], e = 0.f;
 #pragma unroll
             for (int l = 1; l < C::NL - 1; l++) {
@@ -796,7 +802,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
         }
         if (!rvalid || g.levels) continue;
 #pragma unroll
-        for (int c = 0; c < 16; c++) {
+        for (int c = 0; c < CW; c++) {
           const int gcol = nt * C::BN + c0 + c;
           if (gcol >= g.ncols) continue;
           const float sc = srow * pow2f(sexp[c0 + c]);
