@@ -305,7 +305,7 @@ int ChainProgram::run(const double* f, double2* values, double* grad, cudaStream
     CTR_TRY(upload(WS_GEMM_A, tasks.data(), tasks.size() * sizeof(ZTask), &dt, s));
     for (int d = 2; d <= maxd; d++) {
       const size_t n0 = level_off[d], n1 = level_off[d + 1];
-      if (n1 > n0) CTR_TRY(launch_zgemm_f64((const ZTask*)dt + n0, (int)(n1 - n0), N_, s));
+      if (n1 > n0) CTR_TRY(launch_zgemm_f64((const ZTask*)dt + n0, (int)(n1 - n0), N_, s, tasks.data() + n0));
     }
   }
 

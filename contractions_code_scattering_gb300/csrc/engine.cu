@@ -133,7 +133,7 @@ int twosided_fp64(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
     }
     void *d_gt, *d_tt;
     CTR_TRY(upload(WS_TASKS, gt.data(), gt.size() * sizeof(ZTask), &d_gt, stream));
-    CTR_TRY(launch_zgemm_f64((const ZTask*)d_gt, (int)gt.size(), N, stream));
+    CTR_TRY(launch_zgemm_f64((const ZTask*)d_gt, (int)gt.size(), N, stream, gt.data()));
     // The trace tasks live behind the GEMM tasks in a second upload slot.
     CTR_TRY(upload(WS_ROWTASKS, tt.data(), tt.size() * sizeof(TraceTask), &d_tt, stream));
     CTR_TRY(launch_trace_f64((const TraceTask*)d_tt, (int)tt.size(), N, stream));
@@ -271,7 +271,7 @@ int ctr_zgemm_batched(int engine, int nev, int nbatch, const double* const* x, c
   }
   void* d;
   CTR_TRY(ctr::upload(ctr::WS_TASKS, t.data(), t.size() * sizeof(ctr::ZTask), &d, s));
-  return ctr::launch_zgemm_f64((const ctr::ZTask*)d, nbatch, nev, s);
+  return ctr::launch_zgemm_f64((const ctr::ZTask*)d, nbatch, nev, s, t.data());
 }
 
 }  // extern "C"
@@ -291,5 +291,5 @@ extern "C" int ctr_zgemm_tasks(int engine, int nev, int ntask, const ctr_ztask* 
   if (engine != CTR_ENGINE_FP64) return ctr::fail(CTR_ERR_ARG, "unknown engine %d", engine);
   void* d;
   CTR_TRY(ctr::upload(ctr::WS_GEMM_A, zt, (size_t)ntask * sizeof(ctr::ZTask), &d, s));
-  return ctr::launch_zgemm_f64((const ctr::ZTask*)d, ntask, nev, s);
+  return ctr::launch_zgemm_f64((const ctr::ZTask*)d, ntask, nev, s, zt);
 }

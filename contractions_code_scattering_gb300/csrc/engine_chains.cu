@@ -52,7 +52,7 @@ int run_stage(const Ctx& c, const std::vector<ZTask>& tasks, int slot) {
   if (c.engine == CTR_ENGINE_SPLIT) return zgemm_split_tasks(c.N, tasks.data(), (int)tasks.size(), c.s);
   void* d;
   CTR_TRY(upload(slot, tasks.data(), tasks.size() * sizeof(ZTask), &d, c.s));
-  return launch_zgemm_f64((const ZTask*)d, (int)tasks.size(), c.N, c.s);
+  return launch_zgemm_f64((const ZTask*)d, (int)tasks.size(), c.N, c.s, tasks.data());
 }
 
 int run_traces(const Ctx& c, const std::vector<TraceTask>& t) {

@@ -54,7 +54,9 @@ __device__ inline double block_sum_256(double v) {
   return r;  // valid in thread 0
 }
 
-int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s);
+// h_tasks: the same tasks on the host (optional); it lets the launcher check
+// that the weights allow the DMMA form.
+int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s, const ZTask* h_tasks = nullptr);
 int launch_trace_f64(const TraceTask* d_tasks, int ntask, int N, cudaStream_t s);
 int launch_rowsum(const double2* rows, int nrows, const int* off, const int* idx, int nout, int npair,
                   double2* out, size_t out_pair_stride, cudaStream_t s);

@@ -8,6 +8,7 @@
 // an autotuner choice: 32, 50 or 20) while keeping the summation order of the
 // reference (k ascending for every matrix element).
 #include <algorithm>
+#include <cmath>
 
 #include "kernels.h"
 
@@ -187,6 +188,90 @@ __global__ void __launch_bounds__((T / TM) * (T / TN), 2) zgemm_f64_tile_kernel(
       if (rv[a] && cv[b]) Tk.C[(size_t)(i0 + ty + a * RY) * N + (j0 + tx + b * RX)] = acc[a][b];
 }
 
+// FP64 matrix-instruction form (mma.sync m8n8k4 f64, the "DMMA" path of the
+// FP64 pipe, which delivers more flops per pipe cycle than DFMA on GB300).
+// CTA = one task x one block of NFC column fragments; warp w owns output rows
+// 8w .. 8w+7 (NFR warps cover N <= 8 NFR rows); fragments past N are skipped.  Fragment layouts (PTX ISA,
+// m8n8k4 .f64): A 8x4 row-major, lane holds A[lane/4][lane%4]; B 4x8
+// column-major, lane holds B[lane%4][lane/4]; C 8x8, lane holds
+// C[lane/4][2 (lane%4) + {0,1}].  Complex: Cr += Ar Br + (-Ai) Bi,
+// Ci += Ar Bi + Ai Br.  The task weights must be exact multipliers (a real or
+// an imaginary power of two, or zero), which the launcher checks: they scale
+// A as it is staged, and all terms accumulate into one sum.
+__device__ __forceinline__ void dmma884(double& c0, double& c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+template <int NFR, int NFC>
+__global__ void __launch_bounds__(NFR * 32, 1) zgemm_f64_dmma_kernel(const ZTask* __restrict__ tasks, int ntask,
+                                                                     int N, int ncb) {
+  constexpr int KC = 8, RM = NFR * 8, CN = NFC * 8, NT = NFR * 32;
+  __shared__ double2 As[RM][KC + 1];
+  __shared__ double2 Bs[KC][CN + 1];
+  const int task_id = blockIdx.x / ncb;
+  if (task_id >= ntask) return;
+  const int j0 = (blockIdx.x % ncb) * CN;
+  const ZTask& Tk = tasks[task_id];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  double cr[NFC][2], ci[NFC][2];
+#pragma unroll
+  for (int f = 0; f < NFC; f++) cr[f][0] = cr[f][1] = ci[f][0] = ci[f][1] = 0.0;
+  for (int q = 0; q < Tk.nterm; q++) {
+    const double2* A = Tk.A[q];
+    const double2* B = Tk.B[q];
+    const bool ca = (Tk.flags >> q) & 1, cb = (Tk.flags >> (4 + q)) & 1;
+    const double wr = (double)Tk.wre[q], wi = (double)Tk.wim[q];
+    for (int k0 = 0; k0 < N; k0 += KC) {
+      for (int e = threadIdx.x; e < RM * KC; e += NT) {
+        const int r = e / KC, c = e % KC, gk = k0 + c;
+        double2 v = make_double2(0.0, 0.0);
+        if (r < N && gk < N) {
+          if (!ca) v = A[(size_t)r * N + gk];
+          else { v = A[(size_t)gk * N + r]; v.y = -v.y; }
+          v = make_double2(wr * v.x - wi * v.y, wr * v.y + wi * v.x);  // exact: w is +-2^e or +-i 2^e
+        }
+        As[r][c] = v;
+      }
+      for (int e = threadIdx.x; e < KC * CN; e += NT) {
+        const int rk = e / CN, cj = e % CN, gk = k0 + rk, gj = j0 + cj;
+        double2 u = make_double2(0.0, 0.0);
+        if (gk < N && gj < N) {
+          if (!cb) u = B[(size_t)gk * N + gj];
+          else { u = B[(size_t)gj * N + gk]; u.y = -u.y; }
+        }
+        Bs[rk][cj] = u;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int ks = 0; ks < KC; ks += 4) {
+        const double2 a = As[warp * 8 + g][ks + t];
+        const double nai = -a.y;
+#pragma unroll
+        for (int f = 0; f < NFC; f++) {
+          if (j0 + f * 8 >= N) break;  // fragments past the block (uniform across the CTA)
+          const double2 b = Bs[ks + t][f * 8 + g];
+          dmma884(cr[f][0], cr[f][1], a.x, b.x);
+          dmma884(cr[f][0], cr[f][1], nai, b.y);
+          dmma884(ci[f][0], ci[f][1], a.x, b.y);
+          dmma884(ci[f][0], ci[f][1], a.y, b.x);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const int row = warp * 8 + g;
+  if (row < N)
+#pragma unroll
+    for (int f = 0; f < NFC; f++)
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const int col = j0 + f * 8 + 2 * t + i;
+        if (col < N) Tk.C[(size_t)row * N + col] = make_double2(cr[f][i], ci[f][i]);
+      }
+}
+
 // ---------------------------------------------------------------- trace
 // out = coef * sum_e X_e * conj(Y_e) over the Nev*Nev elements (mode 0), or
 // coef * sum_ij X_ij * Y_ji = coef * Tr[X Y] (mode 1).  One CTA per task; the
@@ -311,11 +396,28 @@ __global__ void source_average_kernel(int Nt, int ncorr, const double2* __restri
 }
 
 // --------------------------------------------------------------- launchers
-// Tile variants of the FP64 block GEMM (autotuner knob "zgemm_f64.tile").
+// Variants of the FP64 block GEMM (autotuner knob "zgemm_f64.tile"): DFMA
+// tiles of edge 32, 50 and 20, and matrix-instruction (DMMA) forms for
+// N <= 104 (13 row strips x 7 column fragments a CTA) and N <= 128 (16 x 8).
 static const int kTileEdge[] = {32, 50, 20};
-constexpr int kTileVariants = 3;
+constexpr int kTileVariants = 5;
+
+static bool dmma_fits(int v, int N) { return (v == 3 && N <= 104) || (v == 4 && N <= 128); }
 
 static int launch_zgemm_variant(int v, const ZTask* d_tasks, int ntask, int N, cudaStream_t s) {
+  if (v >= 3) {
+    if (!dmma_fits(v, N)) return fail(CTR_ERR_ARG, "zgemm_f64: variant %d does not cover Nev = %d", v, N);
+    const int nfc = v == 3 ? 7 : 8, ncb = ((N + 7) / 8 + nfc - 1) / nfc;
+    const long long blocks = (long long)ntask * ncb;
+    if (blocks > 0x7fffffffLL) return fail(CTR_ERR_ARG, "zgemm_f64: too many tasks (%d)", ntask);
+    TimedLaunch tl(s, "zgemm_f64");
+    if (v == 3)
+      zgemm_f64_dmma_kernel<13, 7><<<(unsigned)blocks, 13 * 32, 0, s>>>(d_tasks, ntask, N, ncb);
+    else
+      zgemm_f64_dmma_kernel<16, 8><<<(unsigned)blocks, 16 * 32, 0, s>>>(d_tasks, ntask, N, ncb);
+    CTR_CUDA(cudaGetLastError());
+    return CTR_OK;
+  }
   const int T = kTileEdge[v];
   const int tpd = (N + T - 1) / T;
   const long long blocks = (long long)ntask * tpd * tpd;
@@ -330,18 +432,41 @@ static int launch_zgemm_variant(int v, const ZTask* d_tasks, int ntask, int N, c
   return CTR_OK;
 }
 
-int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s) {
+// A weight the DMMA form can fold into A exactly: zero, or a real or imaginary
+// power of two (the gamma5 signs and dyadic factors of the diagram tables).
+static bool exact_weight(float re, float im) {
+  auto pow2 = [](float x) {
+    int e;
+    return std::fabs(std::frexp(x, &e)) == 0.5f;
+  };
+  return (re == 0.f && (im == 0.f || pow2(im))) || (im == 0.f && pow2(re));
+}
+
+int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s, const ZTask* h_tasks) {
   if (ntask == 0) return CTR_OK;
-  // default: the edge whose tiles pad Nev least (ties to the larger tile)
+  // DMMA forms need exact weights; without the host copy they are not offered
+  bool exact = h_tasks != nullptr;
+  for (int t = 0; exact && t < ntask; t++)
+    for (int q = 0; q < h_tasks[t].nterm; q++)
+      if (!exact_weight(h_tasks[t].wre[q], h_tasks[t].wim[q])) exact = false;
+  // default: a DMMA form where it covers Nev > 64, else the DFMA edge that pads
+  // Nev least (ties to the larger tile)
   int dflt = 0;
   long long best = -1;
-  for (int v = 0; v < kTileVariants; v++) {
+  for (int v = 0; v < 3; v++) {
     const long long T = kTileEdge[v], cover = ((N + T - 1) / T) * T;
     if (best < 0 || cover < best) best = cover, dflt = v;
   }
+  if (exact && N > 64) dflt = dmma_fits(3, N) ? 3 : (dmma_fits(4, N) ? 4 : dflt);
+  const int ncand = exact && N > 64 ? kTileVariants : 3;
   int v = dflt;
-  CTR_TRY(tune_resolve("zgemm_f64.tile", "nev=" + std::to_string(N), kTileVariants, dflt, s,
-                       [&](int c) { return launch_zgemm_variant(c, d_tasks, ntask, N, s); }, &v));
+  CTR_TRY(tune_resolve("zgemm_f64.tile", "nev=" + std::to_string(N) + (exact ? ",exact" : ""), ncand, dflt, s,
+                       [&](int c) {
+                         if (c >= 3 && !dmma_fits(c, N)) return launch_zgemm_variant(dflt, d_tasks, ntask, N, s);
+                         return launch_zgemm_variant(c, d_tasks, ntask, N, s);
+                       },
+                       &v));
+  if (v >= 3 && !dmma_fits(v, N)) v = dflt;
   return launch_zgemm_variant(v, d_tasks, ntask, N, s);
 }
 

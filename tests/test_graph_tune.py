@@ -252,15 +252,17 @@ def test_autotuner_measures_and_candidates_agree(cuda):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [20, 37, 50])
+@pytest.mark.parametrize("n", [20, 37, 50, 72, 100, 128])
 def test_fp64_gemm_tile_variants(cuda, n):
-    """Every FP64 block-GEMM tile edge (32, 50, 20) gives the oracle's rho to 1e-12."""
-    nt = 3
+    """Every FP64 block-GEMM variant gives the oracle's rho to 1e-12: DFMA tile
+    edges 32, 50, 20, and above Nev = 64 the FP64 matrix-instruction forms."""
+    nt = 2
     prop, mom5 = _rho_inputs(nt, n, seed=404 + n)
     ref = O.rho(prop, mom5)
     d_prop, d_mom = torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda)
+    variants = [0, 1, 2] + ([3] if 64 < n <= 104 else []) + ([4] if n > 64 else [])
     try:
-        for v in range(3):
+        for v in variants:
             api.tune_force("zgemm_f64.tile", v)
             got = api.run_contract_rho(d_prop, d_mom, engine="fp64").cpu().numpy()
             assert np.abs(got - ref).max() / np.abs(ref).max() <= 1e-12, v
