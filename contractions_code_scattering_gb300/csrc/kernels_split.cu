@@ -730,21 +730,27 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
         if constexpr (C::INT_OUT) {
           // complex128 output: the exact levels and the last one summed exactly
           // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
-          // below 2^8, so no overflow), then rounded once to double; 8 columns
-          // at a time, which keeps the registers within the 8-warp budget
+          // below 2^8, so no overflow), then rounded once to double; EPI_CW
+          // columns at a time, which keeps the registers within the 16-warp budget
           // Level l < NL-1 holds integer multiples of 2^-(16+9l) (products of
           // digits d_i 2^(-8-9i) with i+j = l), at most 2^28 of them, so one
           // FP32 -> int32 conversion of v 2^(16+9l) is exact; the last level is
           // rounded to 2^-54 (|v| < 2^-20 there).
-          long long acc[2][8];
+          constexpr int CW = C::EPI_CW;
+          long long acc[2][CW];
 #pragma unroll
           for (int part = 0; part < 2; part++) {
-            float v[C::NL][8];
+            float v[C::NL][CW];
 #pragma unroll
-            for (int l = 0; l < C::NL; l++) tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+            for (int l = 0; l < C::NL; l++) {
+              if constexpr (CW == 8)
+                tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+              else
+                tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+            }
             tmem_ld_wait();
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
+            for (int c = 0; c < CW; c++) {
               long long a = 0;
 #pragma unroll
               for (int l = 0; l < C::NL - 1; l++)
@@ -756,7 +762,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
           if (!rvalid) continue;
           const int erow = I->lexp[grow];
 #pragma unroll
-          for (int c = 0; c < 8; c++) {
+          for (int c = 0; c < CW; c++) {
             double2* dst = colp[c0 + c];
             if (!dst) continue;
             const int e = erow + sexp[c0 + c] - 54;
