@@ -93,6 +93,8 @@ enum {
   WS_SPLITJOBS2,
   WS_SPLITJOBS3,
   WS_RPHI,          // per-time-slice products of a recomputation call
+  WS_SPLITJOBS4,    // distinct blocks of a task launch
+  WS_BLOCKEXP,      // their row / column exponent bounds
   WS_COUNT
 };
 

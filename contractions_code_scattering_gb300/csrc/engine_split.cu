@@ -621,6 +621,16 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
       uint8_t* rbase = lbase + (size_t)ni * (l_b + le_b);   // <= ni x (right slices + column exponents)
       std::vector<SliceTaskLJob> lj;
       std::vector<SliceTaskRJob> rj;
+      std::map<const double2*, int> bid;          // distinct blocks -> exponent table index
+      std::vector<const double2*> blks;
+      auto block_index = [&](const double2* p) {
+        auto b = bid.find(p);
+        if (b == bid.end()) {
+          b = bid.emplace(p, (int)blks.size()).first;
+          blks.push_back(p);
+        }
+        return b->second;
+      };
       std::map<int, int> lid;                     // instances of one left group share its slices
       std::map<std::vector<uintptr_t>, int> rid;  // identical right sides are sliced once
       std::vector<SplitGemmInst> gi(ni);
@@ -634,8 +644,12 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
           SliceTaskLJob L;
           std::memset(&L, 0, sizeof(L));
           for (int q = 0; q < nterm; q++) {
+            int ex;
+            std::frexp(k.w[q], &ex);  // |w| = 2^(ex-1), checked when the groups were formed
             L.a[q] = k.a[q];
             L.w[q] = k.w[q];
+            L.bi[q] = block_index(k.a[q]);
+            L.wexp[q] = ex - 1;
           }
           L.nterm = nterm;
           L.dag = k.dag;
@@ -667,6 +681,8 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
           uint8_t* q = rbase + rj.size() * (r_b + re_b);
           R.out = q;
           R.exps = (int*)(q + r_b);
+          for (int j = 0; j < in.nb; j++)
+            for (int t = 0; t < nterm; t++) R.bi[j][t] = block_index(R.b[j][t]);
           it = rid.emplace(key, (int)rj.size()).first;
           rj.push_back(R);
         }
@@ -679,10 +695,15 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
       CTR_TRY(upload(WS_SPLITJOBS3, outs.data(), outs.size() * sizeof(double2*), &d_outs, stream));
       for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d_outs + (size_t)i * SPLIT_TASK_NB;
       CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
-      CTR_TRY(launch_slice_task_exp((const SliceTaskLJob*)d_lj, (int)lj.size(), (const SliceTaskRJob*)d_rj,
-                                    (int)rj.size(), N, ntiles, stream));
-      CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, (int)lj.size(), N, nchunk, stream));
-      CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, (int)rj.size(), N, nchunk, ntiles, stream));
+      // exponent bounds of every distinct block once, then the slices
+      void *d_blk, *d_bexp;
+      CTR_TRY(upload(WS_SPLITJOBS4, blks.data(), blks.size() * sizeof(const double2*), &d_blk, stream));
+      CTR_TRY(workspace(WS_BLOCKEXP).get(blks.size() * 2 * N * sizeof(int), &d_bexp));
+      CTR_TRY(launch_block_exp((const double2* const*)d_blk, (int)blks.size(), N, (int*)d_bexp, stream));
+      CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, (int)lj.size(), N, nchunk, (const int*)d_bexp,
+                                     stream));
+      CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d_rj, (int)rj.size(), N, nchunk, ntiles,
+                                      (const int*)d_bexp, stream));
       SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N, 1};
       CTR_TRY(launch_split_gemm(G, ni, d_err, stream));
     }

@@ -264,135 +264,61 @@ __device__ __forceinline__ bool task_right_all_dag(const SliceTaskRJob& J) {
   return true;
 }
 
-// Task-form slicing runs in two launches: the scale exponents (one CTA per left
-// operand and one per right N tile, scanning their rows / columns over all K),
-// then the slices, one CTA per (operand tile, K chunk), so that a stage with few
-// operands still spreads over every SM.
+// Task-form slicing runs in two launches: the exponent bounds of every distinct
+// block of the launch (one read of each block), then one CTA per (operand tile,
+// K chunk), which combines the bounds of its operand's blocks into the row or
+// column scale exponents, so that a stage with few operands still spreads over
+// every SM.
 //
-// Exponents.  Blocks [0, nleft): left job b, 8 warps x 16 rows; blocks
-// [nleft, nleft + nright * ntiles): right job (b - nleft) / ntiles, N tile
-// (b - nleft) % ntiles, 4 threads per column.
-template <class C>
-__global__ void __launch_bounds__(256) slice_task_exp_kernel(const SliceTaskLJob* __restrict__ ljobs, int nleft,
-                                                             const SliceTaskRJob* __restrict__ rjobs, int nev,
-                                                             int ntiles) {
-  __shared__ int part[256];
-  if ((int)blockIdx.x < nleft) {
-    const SliceTaskLJob& J = ljobs[blockIdx.x];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int K = J.nterm * nev;
-    if (J.dag == (1 << J.nterm) - 1) {
-      // conjugate-transposed terms: row r is contiguous across threads; a thread
-      // owns row r = tid % 128 and the k of one parity
-      const int r = threadIdx.x % SPLIT_M, kq = threadIdx.x / SPLIT_M;
-      int e = -30000;
-      if (r < nev)
-        for (int k0 = kq; k0 < K; k0 += 8) {
-          double2 v[4];
-#pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const int k = k0 + 2 * u;
-            v[u] = k < K ? task_left_elem(J, nev, r, k) : make_double2(0.0, 0.0);
-          }
-#pragma unroll
-          for (int u = 0; u < 4; u++) e = max(e, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
-        }
-      part[threadIdx.x] = e;
-      __syncthreads();
-      if (threadIdx.x < SPLIT_M) {
-        const int m = max(part[threadIdx.x], part[threadIdx.x + SPLIT_M]);
-        J.exps[threadIdx.x] = (m < -1000 ? 0 : m) + J.eplus;
-      }
-      return;
-    }
-    // two rows at a time, four loads of each in flight per lane
-    for (int r0 = 2 * warp; r0 < SPLIT_M; r0 += 16) {
-      int e[2] = {-30000, -30000};
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int rr = r0 + h;
-        if (rr >= nev) continue;
-        for (int k0 = lane; k0 < K; k0 += 128) {
-          double2 v[4];
-#pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const int k = k0 + 32 * u;
-            v[u] = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
-          }
-#pragma unroll
-          for (int u = 0; u < 4; u++) e[h] = max(e[h], max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
-        }
-      }
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        for (int o = 16; o; o >>= 1) e[h] = max(e[h], __shfl_xor_sync(0xffffffffu, e[h], o));
-        if (lane == 0) J.exps[r0 + h] = (e[h] < -1000 ? 0 : e[h]) + J.eplus;
-      }
-    }
-    return;
-  }
-  const int b = blockIdx.x - nleft;
-  const SliceTaskRJob& J = rjobs[b / ntiles];
-  const int nt = b % ntiles;
-  const int K = J.nterm * nev, ncols = J.nb * nev;
-  if (task_right_all_dag(J)) {
-    // conjugate-transposed blocks: a column is contiguous in k; warp w scans
-    // columns w, w + 8, ... with its lanes along k
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int nn = warp; nn < C::BN; nn += 8) {
-      const int n = nt * C::BN + nn;
-      int e = -30000;
-      if (n < ncols)
-        for (int k0 = lane; k0 < K; k0 += 128) {
-          double2 v[4];
-#pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const int k = k0 + 32 * u;
-            v[u] = k < K ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
-          }
-#pragma unroll
-          for (int u = 0; u < 4; u++) e = max(e, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
-        }
-      for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-      if (lane == 0) J.exps[nt * C::BN + nn] = (e < -1000 ? 0 : e) + J.eplus;
-    }
-    return;
-  }
-  // 4 threads per column (k = kq mod 4), four loads in flight each
-  const int nn = threadIdx.x % C::BN, kq = threadIdx.x / C::BN;
-  const int n = nt * C::BN + nn;
-  int e = -30000;
-  if (n < ncols && kq < 4)
-    for (int k0 = kq; k0 < K; k0 += 16) {
-      double2 v[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int k = k0 + 4 * u;
-        v[u] = k < K ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) e = max(e, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
-    }
-  part[threadIdx.x] = e;
+// Block exponents: CTA b scans block blk[b] (nev x nev, row-major) once;
+// bexp[b][0][r] = max_c bound(row r), bexp[b][1][c] = max_r bound(column c).
+__global__ void __launch_bounds__(256) block_exp_kernel(const double2* const* __restrict__ blk, int nev,
+                                                        int* __restrict__ bexp) {
+  __shared__ int rmax[SPLIT_MAXK], cmax[SPLIT_MAXK];
+  for (int i = threadIdx.x; i < nev; i += 256) rmax[i] = cmax[i] = -30000;
   __syncthreads();
-  if (threadIdx.x < C::BN) {
-    const int* q = part + threadIdx.x;
-    const int m = max(max(q[0], q[C::BN]), max(q[2 * C::BN], q[3 * C::BN]));
-    J.exps[nt * C::BN + threadIdx.x] = (m < -1000 ? 0 : m) + J.eplus;
+  const double2* B = blk[blockIdx.x];
+  const int total = nev * nev;
+  for (int e = threadIdx.x; e < total; e += 256) {
+    const double2 v = B[e];
+    const int x = max(f64_exp_bound(v.x), f64_exp_bound(v.y));
+    if (x > -30000) {
+      atomicMax(&rmax[e / nev], x);
+      atomicMax(&cmax[e % nev], x);
+    }
+  }
+  __syncthreads();
+  int* o = bexp + (size_t)blockIdx.x * 2 * nev;
+  for (int i = threadIdx.x; i < nev; i += 256) {
+    o[i] = rmax[i];
+    o[nev + i] = cmax[i];
   }
 }
 
 // Left operand slices: CTA = (job, K chunk); 128 rows x 16 k, 8 elements a thread.
 template <class C>
 __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJob* __restrict__ jobs, int nev,
-                                                              int nchunk) {
+                                                              int nchunk, const int* __restrict__ bexp) {
   extern __shared__ __align__(128) uint8_t sm[];
   int* sexp = (int*)sm;
   uint8_t* stage = sm + 512;
   const SliceTaskLJob& J = jobs[blockIdx.x / nchunk];
   const int kc = blockIdx.x % nchunk;
   const int K = J.nterm * nev;
-  if (threadIdx.x < SPLIT_M) sexp[threadIdx.x] = J.exps[threadIdx.x];
+  if (threadIdx.x < SPLIT_M) {
+    // row r over all K: the row (column, for a conjugate-transposed term) bounds of
+    // the terms' blocks, shifted by the weights' exponents
+    const int r = threadIdx.x;
+    int e = -30000;
+    if (r < nev)
+      for (int q = 0; q < J.nterm; q++) {
+        const int b = bexp[((size_t)J.bi[q] * 2 + ((J.dag >> q) & 1)) * nev + r];
+        if (b > -30000) e = max(e, b + J.wexp[q]);
+      }
+    const int E = (e < -1000 ? 0 : e) + J.eplus;
+    sexp[r] = E;
+    if (kc == 0) J.exps[r] = E;
+  }
   // 16 consecutive threads along k: shared-memory stores without bank conflicts
   constexpr int PER = SPLIT_M * SPLIT_K / 256;
   double2 v[PER];
@@ -426,7 +352,7 @@ __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJo
 // Right operand slices: CTA = (job, N tile, K chunk); BN columns x 16 k.
 template <class C>
 __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
-                                                               int nchunk, int ntiles) {
+                                                               int nchunk, int ntiles, const int* __restrict__ bexp) {
   extern __shared__ __align__(128) uint8_t sm[];
   int* sexp = (int*)sm;
   uint8_t* stage = sm + 512;
@@ -434,7 +360,22 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
   const SliceTaskRJob& J = jobs[t / ntiles];
   const int nt = t % ntiles;
   const int K = J.nterm * nev, ncols = J.nb * nev;
-  if (threadIdx.x < C::BN) sexp[threadIdx.x] = J.exps[nt * C::BN + threadIdx.x];
+  if (threadIdx.x < C::BN) {
+    // column n = (block jb, column c) over all K: the column (row, for a
+    // conjugate-transposed term) bounds of block jb's terms
+    const int n = nt * C::BN + threadIdx.x;
+    int e = -30000;
+    if (n < ncols) {
+      const int jb = n / nev, c = n - jb * nev;
+      for (int q = 0; q < J.nterm; q++) {
+        const int dag = (J.dag >> (4 * jb + q)) & 1;
+        e = max(e, bexp[((size_t)J.bi[jb][q] * 2 + (dag ? 0 : 1)) * nev + c]);
+      }
+    }
+    const int E = (e < -1000 ? 0 : e) + J.eplus;
+    sexp[threadIdx.x] = E;
+    if (kc == 0) J.exps[n] = E;  // exps sized ntiles * BN (padding columns get 0)
+  }
   // consecutive threads along the columns, or, for conjugate-transposed blocks
   // (contiguous in k), along k
   const bool tr = task_right_all_dag(J);
@@ -1085,32 +1026,33 @@ int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchu
   return CTR_OK;
 }
 
-int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s) {
+int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, const int* bexp,
+                           cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
   const size_t smem = 512 + CfgHP::A_STAGE;
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, smem, g_attr_tl));
   TimedLaunch tl(s, "slice_task_left");
-  slice_task_left_kernel<CfgHP><<<njobs * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk);
+  slice_task_left_kernel<CfgHP><<<njobs * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk, bexp);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
 
-int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
+int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, const int* bexp,
+                            cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
   const size_t smem = 512 + CfgHP::B_STAGE;
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, smem, g_attr_tr));
   TimedLaunch tl(s, "slice_task_right");
-  slice_task_right_kernel<CfgHP><<<njobs * ntiles * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+  slice_task_right_kernel<CfgHP><<<njobs * ntiles * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles, bexp);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
 
-int launch_slice_task_exp(const SliceTaskLJob* d_ljobs, int nleft, const SliceTaskRJob* d_rjobs, int nright, int nev,
-                          int ntiles, cudaStream_t s) {
-  const long long nblk = (long long)nleft + (long long)nright * ntiles;
+int launch_block_exp(const double2* const* d_blk, int nblk, int nev, int* bexp, cudaStream_t s) {
   if (nblk == 0) return CTR_OK;
-  TimedLaunch tl(s, "slice_task_exp");
-  slice_task_exp_kernel<CfgHP><<<(unsigned)nblk, 256, 0, s>>>(d_ljobs, nleft, d_rjobs, nev, ntiles);
+  if (nev > SPLIT_MAXK) return fail(CTR_ERR_ARG, "block exponents: Nev %d above %d", nev, SPLIT_MAXK);
+  TimedLaunch tl(s, "block_exp");
+  block_exp_kernel<<<nblk, 256, 0, s>>>(d_blk, nev, bexp);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
@@ -1174,6 +1116,14 @@ int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_
     case 6:
       trace_rows_ilp_kernel<64, 4>
           <<<(unsigned)nblk, 64, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 7:
+      trace_rows_ilp_kernel<64, 8>
+          <<<(unsigned)nblk, 64, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
+      break;
+    case 8:
+      trace_rows_ilp_kernel<128, 8>
+          <<<(unsigned)nblk, 128, 0, s>>>(d_rows, nrows, d_abase, d_bbase, lda, ldb, nev, rows, rabs);
       break;
     default: return fail(CTR_ERR_ARG, "traces: unknown variant %d", variant);
   }

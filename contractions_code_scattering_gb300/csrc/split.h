@@ -103,16 +103,22 @@ struct SplitGemmBatch {
 // stacked along N.  dag bit q (left) / bit 4j+q (right): conjugate transpose.
 // eplus = 1 halves the leading digit (|d_0| <= 128) so that level 0 stays
 // exact for K <= 512.
+// The scale exponents come from per-block tables: bi indexes a table of
+// [2][nev] ints per distinct block of the launch (row-wise and column-wise
+// exponent bounds, launch_block_exp); wexp is the exponent of the power-of-two
+// weight w.
 constexpr int SPLIT_TASK_NB = 8;
 struct SliceTaskLJob {
   const double2* a[4];
   float w[4];
+  int bi[4], wexp[4];
   int nterm, dag, eplus, pad;
   uint8_t* out;  // [nchunk][CfgHP::A_STAGE]
   int* exps;     // [SPLIT_M]
 };
 struct SliceTaskRJob {
   const double2* b[SPLIT_TASK_NB][4];
+  int bi[SPLIT_TASK_NB][4];
   int nb, nterm, dag, eplus;
   uint8_t* out;  // [ntiles][nchunk][CfgHP::B_STAGE]
   int* exps;     // [ntiles * CfgHP::BN]
@@ -158,18 +164,21 @@ int split_kernels_prepare();
 // (leading dimensions lda / ldb); rows[q * nrows + r] = coef_r * trace and
 // rabs[q * nrows + r] = |coef_r| sum |A|_1 |B|_1.
 // variant: 0 one thread per row i walking the columns (128 threads), 1/2/3 the
-// flattened element walk with 128/256/512 threads, 4/5/6 the flattened walk with
-// 4/2/4 independent streams a thread and 128/256/64 threads (TRACE_VARIANTS
-// candidates).
-constexpr int TRACE_VARIANTS = 7;
+// flattened element walk with 128/256/512 threads, 4/5/6/7/8 the flattened walk
+// with 4/2/4/8/8 independent streams a thread and 128/256/64/64/128 threads
+// (TRACE_VARIANTS candidates).
+constexpr int TRACE_VARIANTS = 9;
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
                       int lda, int ldb, int npair, int nev, double2* rows, double* rabs, int variant,
                       cudaStream_t s);
-// Task-form slicing: the exponents of every left job and right N tile first
-// (launch_slice_task_exp), then the slices of each (operand tile, K chunk).
-int launch_slice_task_exp(const SliceTaskLJob* d_ljobs, int nleft, const SliceTaskRJob* d_rjobs, int nright, int nev,
-                          int ntiles, cudaStream_t s);
-int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, cudaStream_t s);
-int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
+// Task-form slicing: the row and column exponent bounds of every distinct block
+// of a launch first (bexp [nblk][2][nev]: bound of row r at [0][r], of column c at
+// [1][c]), then the slices of each (operand tile, K chunk), whose scale exponents
+// combine those bounds.
+int launch_block_exp(const double2* const* d_blk, int nblk, int nev, int* bexp, cudaStream_t s);
+int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, const int* bexp,
+                           cudaStream_t s);
+int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, const int* bexp,
+                            cudaStream_t s);
 
 }  // namespace ctr
