@@ -147,6 +147,10 @@ int tune_resolve(const char* knob, const std::string& shape, int ncand, int dflt
 // Upload a host array into a workspace slot (async on stream, host buffer is
 // kept alive by a pinned staging copy owned by the slot).
 int upload(int slot, const void* host, size_t bytes, void** dev, cudaStream_t stream);
+// Several host arrays in one upload (one staging copy): devs[i] receives the
+// device address of parts[i] (256-byte aligned inside the slot).
+int upload_group(int slot, const std::vector<std::pair<const void*, size_t>>& parts, void** devs,
+                 cudaStream_t stream);
 // dst (device) <- src (device-accessible, e.g. mapped pinned host memory), by a kernel.
 int launch_stage_copy(void* dst, const void* src, size_t bytes, cudaStream_t stream);
 // dst <- src for any alignment (a kernel; dst may be mapped pinned host memory).

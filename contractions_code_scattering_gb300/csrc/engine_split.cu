@@ -271,13 +271,16 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
       abase[q] = A;
       bbase[q] = B;
     }
-    void *d_lj, *d_rj, *d_ga, *d_gb, *d_tt;
-    CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &d_lj, stream));
+    void* d4[4];
+    CTR_TRY(upload_group(WS_TASKS,
+                         {{lj.data(), lj.size() * sizeof(SliceLeftJob)},
+                          {rj.data(), rj.size() * sizeof(SliceRightJob)},
+                          {ga.data(), ga.size() * sizeof(SplitGemmInst)},
+                          {gb.data(), gb.size() * sizeof(SplitGemmInst)}},
+                         d4, stream));
+    void *d_lj = d4[0], *d_rj = d4[1], *d_ga = d4[2], *d_gb = d4[3], *d_tt;
     CTR_TRY(launch_slice_left((const SliceLeftJob*)d_lj, np, N, nchunk, mtT, stream));
-    CTR_TRY(upload(WS_TASKS2, rj.data(), rj.size() * sizeof(SliceRightJob), &d_rj, stream));
     CTR_TRY(launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream));
-    CTR_TRY(upload(WS_GEMM_A, ga.data(), ga.size() * sizeof(SplitGemmInst), &d_ga, stream));
-    CTR_TRY(upload(WS_GEMM_B, gb.data(), gb.size() * sizeof(SplitGemmInst), &d_gb, stream));
     // tile walk of each GEMM (autotuned; idempotent, so candidates re-run on the same data)
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
     SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
@@ -689,15 +692,20 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
         const SliceTaskRJob& Ru = rj[it->second];
         gi[i] = SplitGemmInst{L.out, Ru.out, L.exps, Ru.exps, nullptr, nullptr};
       }
-      void *d_lj, *d_rj, *d_gi, *d_outs;
-      CTR_TRY(upload(WS_SPLITJOBS, lj.data(), lj.size() * sizeof(SliceTaskLJob), &d_lj, stream));
-      CTR_TRY(upload(WS_SPLITJOBS2, rj.data(), rj.size() * sizeof(SliceTaskRJob), &d_rj, stream));
-      CTR_TRY(upload(WS_SPLITJOBS3, outs.data(), outs.size() * sizeof(double2*), &d_outs, stream));
+      // the launch's tables in two staging copies (the instances need the
+      // device address of their output pointer lists)
+      void* d1[4];
+      CTR_TRY(upload_group(WS_SPLITJOBS,
+                           {{lj.data(), lj.size() * sizeof(SliceTaskLJob)},
+                            {rj.data(), rj.size() * sizeof(SliceTaskRJob)},
+                            {outs.data(), outs.size() * sizeof(double2*)},
+                            {blks.data(), blks.size() * sizeof(const double2*)}},
+                           d1, stream));
+      void *d_lj = d1[0], *d_rj = d1[1], *d_outs = d1[2], *d_blk = d1[3], *d_gi;
       for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d_outs + (size_t)i * SPLIT_TASK_NB;
       CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
       // exponent bounds of every distinct block once, then the slices
-      void *d_blk, *d_bexp;
-      CTR_TRY(upload(WS_SPLITJOBS4, blks.data(), blks.size() * sizeof(const double2*), &d_blk, stream));
+      void* d_bexp;
       CTR_TRY(workspace(WS_BLOCKEXP).get(blks.size() * 2 * N * sizeof(int), &d_bexp));
       CTR_TRY(launch_block_exp((const double2* const*)d_blk, (int)blks.size(), N, (int*)d_bexp, stream));
       CTR_TRY(launch_slice_task_left((const SliceTaskLJob*)d_lj, (int)lj.size(), N, nchunk, (const int*)d_bexp,

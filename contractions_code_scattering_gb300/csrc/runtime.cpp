@@ -258,6 +258,23 @@ int upload(int slot, const void* host, size_t bytes, void** dev, cudaStream_t st
   return CTR_OK;
 }
 
+int upload_group(int slot, const std::vector<std::pair<const void*, size_t>>& parts, void** devs,
+                 cudaStream_t stream) {
+  std::vector<size_t> off(parts.size());
+  size_t total = 0;
+  for (size_t i = 0; i < parts.size(); i++) {
+    off[i] = total;
+    total += (parts[i].second + 255) & ~(size_t)255;
+  }
+  std::vector<uint8_t> packed(std::max<size_t>(total, 1));
+  for (size_t i = 0; i < parts.size(); i++)
+    if (parts[i].second) std::memcpy(packed.data() + off[i], parts[i].first, parts[i].second);
+  void* d;
+  CTR_TRY(upload(slot, packed.data(), total, &d, stream));
+  for (size_t i = 0; i < parts.size(); i++) devs[i] = (uint8_t*)d + off[i];
+  return CTR_OK;
+}
+
 static std::mutex g_down_mutex;
 static void* g_down_host = nullptr;
 static void* g_down_dev = nullptr;
