@@ -676,7 +676,8 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
           // Level l < NL-1 holds integer multiples of 2^-(16+9l) (products of
           // digits d_i 2^(-8-9i) with i+j = l), at most 2^28 of them, so one
           // FP32 -> int32 conversion of v 2^(16+9l) is exact; the last level is
-          // rounded to 2^-54 (|v| < 2^-20 there).
+          // rounded to 2^-54 (|v| < 2^-24 there, so it fits an int32 as well;
+          // 64-bit conversions would go through GB300's slow FP64 pipe).
           constexpr int CW = C::EPI_CW;
           long long acc[2][CW];
 #pragma unroll
@@ -696,7 +697,8 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
 #pragma unroll
               for (int l = 0; l < C::NL - 1; l++)
                 a += (long long)__float2int_rn(v[l][c] * __int_as_float((127 + 16 + 9 * l) << 23)) << (38 - 9 * l);
-              a += __float2ll_rn(v[C::NL - 1][c] * __int_as_float((127 + 54) << 23));
+              // the last level holds pairs i+j >= NL-1: |v| 2^54 <= 5 K 2^16 2^-52 2^54 < 2^30
+              a += (long long)__float2int_rn(v[C::NL - 1][c] * __int_as_float((127 + 54) << 23));
               acc[part][c] = a;
             }
           }
