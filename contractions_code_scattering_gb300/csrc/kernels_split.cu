@@ -420,9 +420,10 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
 // Persistent kernel: each CTA walks output tiles t = blockIdx.x, +gridDim.x, ...
 // of 128 x SPLIT_N.  Warp 0: TMEM allocation and the bulk-copy producer, which
 // runs ahead across tile boundaries through an NSTAGE ring; warp 1: MMA issue;
-// warps 2..5: epilogue (TMEM lanes 32*(warp%4) .. +31).  The MMA warp and the
-// epilogue hand the TMEM accumulators back and forth with two mbarriers
-// (tmem_full after the last MMA of a tile, tmem_empty once drained).
+// warps 2 .. 2 + EPI_WARPS - 1: epilogue (TMEM lanes 32*(warp%4) .. +31).  The
+// MMA warp and the epilogue hand the TMEM accumulators back and forth with two
+// mbarriers (tmem_full after the last MMA of a tile, tmem_empty once the
+// epilogue holds them in registers, before its global stores).
 // Threads of a GEMM CTA: producer and MMA warps plus C::EPI_WARPS epilogue warps.
 template <class C>
 constexpr int gemm_threads() { return 64 + 32 * C::EPI_WARPS; }
@@ -629,9 +630,8 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       if (!mbar_wait(drainb, 0, WAIT_NS)) atomicExch(err, 5);
     }
   } else {
-    // epilogue: warps 2..5 -> TMEM lane quadrant warp % 4
-    // TMEM lane quadrant warp % 4; with 8 epilogue warps each quadrant has two,
-    // which split the tile's columns between them
+    // epilogue: warp w drains TMEM lane quadrant w % 4; the EPI_WARPS / 4
+    // warps of a quadrant split the tile's columns between them
     constexpr int EPH = C::EPI_WARPS / 4, CPW = C::BN / EPH;
     const int q = warp & 3, half = (warp - 2) / 4;
     const int et = threadIdx.x - 64;  // 0 .. 32 * EPI_WARPS - 1 within the epilogue group
@@ -665,30 +665,32 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       epi_bar<32 * C::EPI_WARPS>();
       if (status[1]) break;
       tc_fence_after();
-      float4* outp = I->out;
-      const int ldo = g.ldo;
-      for (int c0 = half * CPW; c0 < (half + 1) * CPW; c0 += C::EPI_CW) {
-        if constexpr (C::INT_OUT) {
-          // complex128 output: the exact levels and the last one summed exactly
-          // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
-          // below 2^8, so no overflow), then rounded once to double; EPI_CW
-          // columns at a time, which keeps the registers within the 16-warp budget
-          // Level l < NL-1 holds integer multiples of 2^-(16+9l) (products of
-          // digits d_i 2^(-8-9i) with i+j = l), at most 2^28 of them, so one
-          // FP32 -> int32 conversion of v 2^(16+9l) is exact; the last level is
-          // rounded to 2^-54 (|v| < 2^-24 there, so it fits an int32 as well;
-          // 64-bit conversions would go through GB300's slow FP64 pipe).
-          constexpr int CW = C::EPI_CW;
-          long long acc[2][CW];
+      // Each warp drains its CPW columns into registers and hands TMEM back to
+      // the MMA warp before it writes anything to global memory, so the next
+      // tile's MMAs run while this tile's products are stored.
+      const int cbase = half * CPW;
+      if constexpr (C::INT_OUT) {
+        // complex128 output: the exact levels and the last one summed exactly
+        // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
+        // below 2^8, so no overflow), then rounded once to double.
+        // Level l < NL-1 holds integer multiples of 2^-(16+9l) (products of
+        // digits d_i 2^(-8-9i) with i+j = l), at most 2^28 of them, so one
+        // FP32 -> int32 conversion of v 2^(16+9l) is exact; the last level is
+        // rounded to 2^-54 (|v| < 2^-24 there, so it fits an int32 as well;
+        // 64-bit conversions would go through GB300's slow FP64 pipe).
+        constexpr int CW = C::EPI_CW;
+        long long acc[2][CPW];
+#pragma unroll
+        for (int cc = 0; cc < CPW; cc += CW) {
 #pragma unroll
           for (int part = 0; part < 2; part++) {
             float v[C::NL][CW];
 #pragma unroll
             for (int l = 0; l < C::NL; l++) {
               if constexpr (CW == 8)
-                tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+                tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
               else
-                tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
+                tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
             }
             tmem_ld_wait();
 #pragma unroll
@@ -699,70 +701,90 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
                 a += (long long)__float2int_rn(v[l][c] * __int_as_float((127 + 16 + 9 * l) << 23)) << (38 - 9 * l);
               // the last level holds pairs i+j >= NL-1: |v| 2^54 <= 5 K 2^16 2^-52 2^54 < 2^30
               a += (long long)__float2int_rn(v[C::NL - 1][c] * __int_as_float((127 + 54) << 23));
-              acc[part][c] = a;
+              acc[part][cc + c] = a;
             }
           }
-          if (!rvalid) continue;
+        }
+        // accumulators drained: hand TMEM back to the MMA warp
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty);
+        if (rvalid) {
           const int erow = I->lexp[grow];
 #pragma unroll
-          for (int c = 0; c < CW; c++) {
-            double2* dst = colp[c0 + c];
+          for (int c = 0; c < CPW; c++) {
+            double2* dst = colp[cbase + c];
             if (!dst) continue;
-            const int e = erow + sexp[c0 + c] - 54;
+            const int e = erow + sexp[cbase + c] - 54;
             dst[(size_t)grow * g.blkn] = make_double2(i2d_scaled(acc[0][c], e), i2d_scaled(acc[1][c], e));
           }
-          continue;
-        } else {
+        }
+      } else {
         // float-float output: levels 0 .. NL-2 exact, combined by exact two-sums;
-        // the rounding errors and the last level go to the low word
+        // the rounding errors and the last level go to the low word.
+        // res[c] = (re hi, re lo, im hi, im lo) of column cbase + c.
         constexpr int CW = C::EPI_CW;
-        float hi[2][CW], lo[2][CW];
+        const int ldo = g.ldo;
+        float4 res[CPW];
 #pragma unroll
-        for (int part = 0; part < 2; part++) {
-          float v[C::NL][CW];
+        for (int cc = 0; cc < CPW; cc += CW) {
 #pragma unroll
-          for (int l = 0; l < C::NL; l++) {
-            if constexpr (CW == 16)
-              tmem_ld16(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
-            else
-              tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + c0), v[l]);
-          }
-          tmem_ld_wait();
-          if (g.levels && rvalid) {
+          for (int part = 0; part < 2; part++) {
+            float v[C::NL][CW];
+#pragma unroll
+            for (int l = 0; l < C::NL; l++) {
+              if constexpr (CW == 8)
+                tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
+              else
+                tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
+            }
+            tmem_ld_wait();
+            if (g.levels && rvalid) {
+              for (int c = 0; c < CW; c++) {
+                const int gcol = nt * C::BN + cbase + cc + c;
+                if (gcol < g.ncols)
+                  for (int l = 0; l < C::NL; l++)
+                    g.levels[((size_t)(part * C::NL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
+              }
+            }
+#pragma unroll
             for (int c = 0; c < CW; c++) {
-              const int gcol = nt * C::BN + c0 + c;
-              if (gcol < g.ncols)
-                for (int l = 0; l < C::NL; l++)
-                  g.levels[((size_t)(part * C::NL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
+              float s = v[0][c], e = 0.f;
+#pragma unroll
+              for (int l = 1; l < C::NL - 1; l++) {
+                float t, d;
+                two_sum(s, v[l][c], t, d);
+                s = t;
+                e += d;
+              }
+              float h, lw;
+              fast_two_sum(s, e + v[C::NL - 1][c], h, lw);
+              if (part == 0) {
+                res[cc + c].x = h;
+                res[cc + c].y = lw;
+              } else {
+                res[cc + c].z = h;
+                res[cc + c].w = lw;
+              }
             }
           }
+        }
+        // accumulators drained: hand TMEM back to the MMA warp
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty);
+        if (rvalid && !g.levels) {
+          float4* outp = I->out;
 #pragma unroll
-          for (int c = 0; c < CW; c++) {
-            float s = v[0][c], e = 0.f;
-#pragma unroll
-            for (int l = 1; l < C::NL - 1; l++) {
-              float t, d;
-              two_sum(s, v[l][c], t, d);
-              s = t;
-              e += d;
-            }
-            fast_two_sum(s, e + v[C::NL - 1][c], hi[part][c], lo[part][c]);
+          for (int c = 0; c < CPW; c++) {
+            const int gcol = nt * C::BN + cbase + c;
+            if (gcol >= g.ncols) continue;
+            const float sc = srow * pow2f(sexp[cbase + c]);
+            outp[(size_t)gcol * ldo + grow] =
+                make_float4(res[c].x * sc, res[c].y * sc, res[c].z * sc, res[c].w * sc);
           }
-        }
-        if (!rvalid || g.levels) continue;
-#pragma unroll
-        for (int c = 0; c < CW; c++) {
-          const int gcol = nt * C::BN + c0 + c;
-          if (gcol >= g.ncols) continue;
-          const float sc = srow * pow2f(sexp[c0 + c]);
-          outp[(size_t)gcol * ldo + grow] = make_float4(hi[0][c] * sc, lo[0][c] * sc, hi[1][c] * sc, lo[1][c] * sc);
-        }
         }
       }
-      // accumulators drained: hand TMEM back to the MMA warp
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(tempty);
     }
   }
   tc_fence_before();

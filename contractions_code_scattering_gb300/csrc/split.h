@@ -41,7 +41,7 @@ struct SplitCfg {
   static constexpr bool PACK = PACK_;
   static constexpr bool INT_OUT = INT_OUT_;  // epilogue: complex128 via exact integer sums (else float-float)
   static constexpr int EPI_WARPS = 16;             // 4 per TMEM lane quadrant, splitting the columns
-  static constexpr int EPI_CW = BN % 32 ? 4 : 8;   // columns per TMEM load in the epilogue
+  static constexpr int EPI_CW = 4;                 // columns per TMEM load in the epilogue
   static constexpr int B_PLANES = PACK ? 3 : 2;
   static constexpr int A_SUB = SPLIT_M * SPLIT_K * 2;
   static constexpr int B_SUB = BN * SPLIT_K * 2;
