@@ -265,7 +265,7 @@ def tune_set_mode(mode):
 
 
 def tune_force(knob, value):
-    """Pin a knob ("twosided.batch", "trace_rows", "split_gemm.order") to a value; -1 releases it."""
+    """Pin a knob ("twosided.batch", "trace_rows", "slice_tau", "split_gemm.order", "zgemm_f64.tile") to a value; -1 releases it."""
     check(lib().ctr_tune_force(knob.encode(), int(value)))
 
 

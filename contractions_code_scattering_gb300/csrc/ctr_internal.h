@@ -95,6 +95,7 @@ enum {
   WS_RPHI,          // per-time-slice products of a recomputation call
   WS_SPLITJOBS4,    // distinct blocks of a task launch
   WS_BLOCKEXP,      // their row / column exponent bounds
+  WS_TRACEGROUPS,   // grouped closing traces of a two-sided call
   WS_COUNT
 };
 

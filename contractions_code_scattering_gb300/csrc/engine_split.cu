@@ -215,8 +215,16 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     }
   }
   const int ntr = (int)trow.size();
-  void *d_trow, *d_tix, *d_rcoef;
+  // the same traces in groups that share their product blocks (trace_groups)
+  // (trace_groups), and in quad groups of at most 2 + 2 blocks (trace_quads)
+  std::vector<TraceGroup> tgroups, tquads;
+  const int tg_maxcols = build_trace_groups(trow.data(), ntr, TG_MAXA, TG_MAXB, TG_MAXT, tgroups);
+  build_trace_groups(trow.data(), ntr, 2, 2, 4, tquads);
+  tgroups.insert(tgroups.end(), tquads.begin(), tquads.end());
+  const int ngroups = (int)(tgroups.size() - tquads.size()), nquads = (int)tquads.size();
+  void *d_trow, *d_tix, *d_rcoef, *d_tgroups;
   CTR_TRY(upload(WS_SPLITJOBS, trow.data(), trow.size() * sizeof(TraceRow), &d_trow, stream));
+  CTR_TRY(upload(WS_TRACEGROUPS, tgroups.data(), tgroups.size() * sizeof(TraceGroup), &d_tgroups, stream));
   CTR_TRY(upload(WS_SPLITJOBS2, tix.data(), tix.size() * sizeof(int), &d_tix, stream));
   CTR_TRY(upload(WS_SPLITJOBS3, coef.data(), coef.size() * sizeof(float), &d_rcoef, stream));
 
@@ -279,8 +287,14 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
                           {gb.data(), gb.size() * sizeof(SplitGemmInst)}},
                          d4, stream));
     void *d_lj = d4[0], *d_rj = d4[1], *d_ga = d4[2], *d_gb = d4[3], *d_tt;
-    CTR_TRY(launch_slice_left((const SliceLeftJob*)d_lj, np, N, nchunk, mtT, stream));
-    CTR_TRY(launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream));
+    // slicer form (autotuned; both write the same bytes, so candidates re-run)
+    auto slice_tau = [&](int form) {
+      CTR_TRY(launch_slice_left((const SliceLeftJob*)d_lj, np, N, nchunk, mtT, stream, form));
+      return launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream, form);
+    };
+    int sform = 0;
+    CTR_TRY(tune_resolve("slice_tau", shape, 2, 0, stream, slice_tau, &sform));
+    CTR_TRY(slice_tau(sform));
     // tile walk of each GEMM (autotuned; idempotent, so candidates re-run on the same data)
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
     SplitGemmBatch GB{(const SplitGemmInst*)d_gb, F.mtiles, ntT, nchunk, nR * N, nab * N, ldB};
@@ -300,12 +314,22 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     }
     abase.insert(abase.end(), bbase.begin(), bbase.end());
     CTR_TRY(upload(WS_ROWTASKS, abase.data(), abase.size() * sizeof(const float4*), &d_tt, stream));
+    // candidates: the TRACE_VARIANTS per-trace kernels, the grouped one, then
+    // the two quad-group kernels
     auto traces = [&](int variant) {
+      if (variant == TRACE_VARIANTS)
+        return launch_trace_groups((const TraceGroup*)d_tgroups, ngroups, tg_maxcols, (const TraceRow*)d_trow, ntr,
+                                   (const float4* const*)d_tt, (const float4* const*)d_tt + np, ldA, ldB, np, N, R,
+                                   Rabs, d_err, stream);
+      if (variant > TRACE_VARIANTS)
+        return launch_trace_quads((const TraceGroup*)d_tgroups + ngroups, nquads, (const TraceRow*)d_trow, ntr,
+                                  (const float4* const*)d_tt, (const float4* const*)d_tt + np, ldA, ldB, np, N, R,
+                                  Rabs, variant - TRACE_VARIANTS - 1, stream);
       return launch_trace_rows((const TraceRow*)d_trow, ntr, (const float4* const*)d_tt,
                                (const float4* const*)d_tt + np, ldA, ldB, np, N, R, Rabs, variant, stream);
     };
     int variant = 0;
-    CTR_TRY(tune_resolve("trace_rows", shape, TRACE_VARIANTS, 0, stream, traces, &variant));
+    CTR_TRY(tune_resolve("trace_rows", shape, TRACE_VARIANTS + 3, TRACE_VARIANTS + 1, stream, traces, &variant));
     CTR_TRY(traces(variant));
     return launch_rowsum_coef_refine(R, Rabs, ntr, (const int*)d_csr, (const int*)d_csr + (nout + 1),
                                      (const int*)d_tix, (const float*)d_rcoef, nout, np,

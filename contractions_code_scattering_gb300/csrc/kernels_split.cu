@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <map>
 
 #include "kernels.h"
 #include "sm100_ptx.cuh"
@@ -223,6 +224,163 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
     int4* d = (int4*)(dst_tile + (size_t)kc * SPLIT_B_STAGE);
     const int4* src = (const int4*)stage;
     for (int i = threadIdx.x; i < SPLIT_B_STAGE / 16; i += 256) d[i] = src[i];
+    __syncthreads();
+  }
+}
+
+// Staged forms of slice_left / slice_right (same output bytes): one CTA per
+// 32-row (left) or 32-column (right) quarter of an operand tile copies its
+// quarter of the FP64 operand into shared memory once (cp.async, all loads in
+// flight together), takes the scale exponents from there and slices every K
+// chunk from there, so the operand is read from memory once.  A quarter covers
+// 4 of the core-matrix row groups of each (slice, plane) sub-tile, i.e. 1 KB
+// contiguous in each.
+constexpr int SLQ = 32;  // rows / columns of a quarter
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// shared memory of the staged slicers: the quarter (SLQ x nev complex), the
+// staged output chunk (planes x 1 KB) and the exponents
+inline size_t slice_staged_smem(int nev, int planes) { return (size_t)SLQ * nev * 16 + (size_t)planes * 1024 + 256; }
+
+__global__ void __launch_bounds__(256) slice_left_staged_kernel(const SliceLeftJob* __restrict__ jobs, int nev,
+                                                                int nchunk, int mtiles) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  double2* data = (double2*)sm;  // [SLQ][nev]
+  uint8_t* stage = sm + (size_t)SLQ * nev * 16;
+  int* sexp = (int*)(stage + SPLIT_NSLICE * 2 * 1024);
+  const int quarters = SPLIT_M / SLQ;
+  const int job = blockIdx.x / (mtiles * quarters), rem = blockIdx.x - job * mtiles * quarters;
+  const int mt = rem / quarters, qt = rem - mt * quarters;
+  const SliceLeftJob& J = jobs[job];
+  const int r0 = mt * SPLIT_M + qt * SLQ;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // rows r0 .. r0 + SLQ - 1 (each row contiguous in its block); padding rows are zero
+  for (int e = threadIdx.x; e < SLQ * nev; e += 256) {
+    const int rr = e / nev, k = e - rr * nev, r = r0 + rr;
+    if (r < J.rows)
+      cp_async16(data + e, J.blk[r / nev] + (size_t)(r % nev) * nev + k);
+    else
+      data[e] = make_double2(0.0, 0.0);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // row exponents
+  for (int rr = warp; rr < SLQ; rr += 8) {
+    int e = -30000;
+    if (r0 + rr < J.rows)
+      for (int k = lane; k < nev; k += 32) {
+        const double2 v = data[rr * nev + k];
+        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
+      }
+    for (int o = 16; o; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if (lane == 0) {
+      const int E = e < -1000 ? 0 : e;
+      sexp[rr] = E;
+      J.exps[r0 + rr] = E;
+    }
+  }
+  __syncthreads();
+  uint8_t* dst_tile = J.out + (size_t)mt * nchunk * SPLIT_A_STAGE + qt * 1024;
+  for (int kc = 0; kc < nchunk; kc++) {
+#pragma unroll
+    for (int u = 0; u < SLQ * SPLIT_K / 256; u++) {
+      const int e = threadIdx.x + 256 * u;
+      const int rr = e >> 4, kk = e & 15, k = kc * SPLIT_K + kk;
+      const double2 v = k < nev ? data[rr * nev + k] : make_double2(0.0, 0.0);
+      const int E = sexp[rr];
+      bool nr, ni;
+      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
+      const uint32_t off = core_offset(rr, kk);
+#pragma unroll
+      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+        *(__nv_bfloat16*)(stage + (sl * 2 + 0) * 1024 + off) = slice_bf16(Ur, sl, nr);
+        *(__nv_bfloat16*)(stage + (sl * 2 + 1) * 1024 + off) = slice_bf16(Ui, sl, ni);
+      }
+    }
+    __syncthreads();
+    uint8_t* d = dst_tile + (size_t)kc * SPLIT_A_STAGE;
+    for (int i = threadIdx.x; i < SPLIT_NSLICE * 2 * 64; i += 256) {
+      const int piece = i >> 6, w = i & 63;
+      ((int4*)(d + (size_t)piece * SPLIT_A_SUB))[w] = ((const int4*)(stage + piece * 1024))[w];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRightJob* __restrict__ jobs, int nev,
+                                                                 int nchunk, int ntiles) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  double2* data = (double2*)sm;  // [nev][SLQ]
+  uint8_t* stage = sm + (size_t)SLQ * nev * 16;
+  int* sexp = (int*)(stage + SPLIT_NSLICE * 3 * 1024);
+  __shared__ int part[256];
+  const int quarters = SPLIT_N / SLQ;
+  const int job = blockIdx.x / (ntiles * quarters), rem = blockIdx.x - job * ntiles * quarters;
+  const int nt = rem / quarters, qt = rem - nt * quarters;
+  const SliceRightJob& J = jobs[job];
+  const int n0 = nt * SPLIT_N + qt * SLQ;
+  // columns n0 .. n0 + SLQ - 1: a warp reads one row k of them; padding columns are zero
+  {
+    const int c = threadIdx.x & 31, n = n0 + c;
+    const double2* colp = n < J.cols ? J.blk[n / nev] + (n % nev) : nullptr;
+    for (int k = threadIdx.x >> 5; k < nev; k += 8) {
+      if (colp)
+        cp_async16(data + k * SLQ + c, colp + (size_t)k * nev);
+      else
+        data[k * SLQ + c] = make_double2(0.0, 0.0);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // column exponents: 8 threads per column, partial maxima combined in shared memory
+  {
+    const int c = threadIdx.x & 31, kq = threadIdx.x >> 5;
+    int e = -30000;
+    if (n0 + c < J.cols)
+      for (int k = kq; k < nev; k += 8) {
+        const double2 v = data[k * SLQ + c];
+        e = max(e, max(f64_exp_bound(v.x), f64_exp_bound(v.y)));
+      }
+    part[threadIdx.x] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x < SLQ) {
+    int e = part[threadIdx.x];
+    for (int w = 1; w < 8; w++) e = max(e, part[w * 32 + threadIdx.x]);
+    const int E = e < -1000 ? 0 : e;
+    sexp[threadIdx.x] = E;
+    J.exps[n0 + threadIdx.x] = E;
+  }
+  __syncthreads();
+  uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE + qt * 1024;
+  for (int kc = 0; kc < nchunk; kc++) {
+#pragma unroll
+    for (int u = 0; u < SLQ * SPLIT_K / 256; u++) {
+      const int e = threadIdx.x + 256 * u;
+      const int nn = e % SLQ, kk = e / SLQ, k = kc * SPLIT_K + kk;
+      const double2 v = k < nev ? data[k * SLQ + nn] : make_double2(0.0, 0.0);
+      const int E = sexp[nn];
+      bool nr, ni;
+      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
+      const uint32_t off = core_offset(nn, kk);
+#pragma unroll
+      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+        // planes -im, re, im (packed complex MMAs)
+        *(__nv_bfloat16*)(stage + (sl * 3 + 0) * 1024 + off) = slice_bf16(Ui, sl, !ni);
+        *(__nv_bfloat16*)(stage + (sl * 3 + 1) * 1024 + off) = slice_bf16(Ur, sl, nr);
+        *(__nv_bfloat16*)(stage + (sl * 3 + 2) * 1024 + off) = slice_bf16(Ui, sl, ni);
+      }
+    }
+    __syncthreads();
+    uint8_t* d = dst_tile + (size_t)kc * SPLIT_B_STAGE;
+    for (int i = threadIdx.x; i < SPLIT_NSLICE * 3 * 64; i += 256) {
+      const int piece = i >> 6, w = i & 63;
+      ((int4*)(d + (size_t)piece * SPLIT_B_SUB))[w] = ((const int4*)(stage + piece * 1024))[w];
+    }
     __syncthreads();
   }
 }
@@ -986,6 +1144,218 @@ __global__ void __launch_bounds__(TPB) trace_rows_ilp_kernel(const TraceRow* __r
   }
 }
 
+// Grouped traces.  CTA (pair q, group g): warp TG_CWARPS is the producer, whose
+// lane 0 copies column j of every block of the group (nev float-float complex
+// values, 16 nev contiguous bytes) into stage j % TG_NSTAGE by cp.async.bulk;
+// consumer warp w computes traces w and w + TG_CWARPS of the group, lane l over
+// the elements i = l, l + 32, ... of each column.  The stage ring is handed over
+// with full (transaction bytes) and empty (one arrival per consumer warp)
+// mbarriers; every wait is bounded and a timeout records an error code.
+constexpr int TG_NSTAGE = 4, TG_CWARPS = TG_MAXT / 2;
+constexpr int TG_THREADS = 32 * (TG_CWARPS + 1);
+
+__global__ void __launch_bounds__(TG_THREADS) trace_groups_kernel(
+    const TraceGroup* __restrict__ groups, int ngroups, int stage_bytes, const TraceRow* __restrict__ rt, int nrows,
+    const float4* const* __restrict__ abase, const float4* const* __restrict__ bbase, int lda, int ldb, int nev,
+    double2* __restrict__ rows, double* __restrict__ rabs, int* __restrict__ err) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  __shared__ TraceGroup G;
+  __shared__ uint64_t full[TG_NSTAGE], empty[TG_NSTAGE];
+  __shared__ int status;
+  const int q = blockIdx.x / ngroups, gi = blockIdx.x - q * ngroups;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  static_assert(sizeof(TraceGroup) % 4 == 0 && sizeof(TraceGroup) / 4 <= TG_THREADS, "group copy");
+  if (threadIdx.x < (int)(sizeof(TraceGroup) / 4))
+    ((int*)&G)[threadIdx.x] = ((const int*)(groups + gi))[threadIdx.x];
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TG_NSTAGE; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], TG_CWARPS);
+    }
+    fence_mbar_init();
+    status = *(volatile int*)err;
+  }
+  __syncthreads();
+  if (status) return;  // uniform: a failure was recorded before this CTA started
+  const int na = G.na, nb = G.nb;
+  const uint32_t colb = (uint32_t)nev * 16u;
+
+  if (warp == TG_CWARPS) {
+    if (lane == 0) {
+      const float4* pa = abase[q];
+      const float4* pb = bbase[q];
+      const uint32_t tx = (uint32_t)(na + nb) * colb;
+      int issued = 0;
+      for (int j = 0; j < nev; j++) {
+        const int s = j % TG_NSTAGE;
+        if (j >= TG_NSTAGE && !mbar_wait(&empty[s], ((j / TG_NSTAGE) - 1) & 1, WAIT_NS, err)) {
+          atomicExch(err, 6);
+          break;
+        }
+        uint8_t* dst = sm + (size_t)s * stage_bytes;
+        mbar_arrive_expect_tx(&full[s], tx);
+        for (int a = 0; a < na; a++) bulk_g2s(dst + a * colb, pa + G.aoff[a] + (size_t)j * lda, colb, &full[s]);
+        for (int b = 0; b < nb; b++)
+          bulk_g2s(dst + (na + b) * colb, pb + G.boff[b] + (size_t)j * ldb, colb, &full[s]);
+        issued++;
+      }
+      // copies still in flight (only after a failure): wait for them, bounded,
+      // before the CTA's shared memory is released
+      for (int j = issued - 1; j >= 0 && j >= issued - TG_NSTAGE; j--)
+        mbar_wait(&full[j % TG_NSTAGE], (j / TG_NSTAGE) & 1, WAIT_NS);
+    }
+    return;
+  }
+
+  float sr[2] = {0.f, 0.f}, er[2] = {0.f, 0.f}, si[2] = {0.f, 0.f}, ei[2] = {0.f, 0.f}, sa[2] = {0.f, 0.f};
+  bool ok = true;
+  for (int j = 0; j < nev; j++) {
+    const int s = j % TG_NSTAGE;
+    // every lane observes the stage's completion; the outcome is made warp-uniform
+    const bool got = mbar_wait(&full[s], (j / TG_NSTAGE) & 1, WAIT_NS, err);
+    if (!__all_sync(0xffffffffu, got)) {
+      if (lane == 0) atomicExch(err, 7);
+      ok = false;
+      break;
+    }
+    const float4* col = (const float4*)(sm + (size_t)s * stage_bytes);
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const int t = warp + u * TG_CWARPS;
+      if (t >= G.nt) continue;
+      const float4* A = col + G.ta[t] * nev;
+      const float4* B = col + (na + G.tb[t]) * nev;
+      for (int i = lane; i < nev; i += 32) {
+        const float4 a = A[i], b = B[i];
+        ff_mac(sr[u], er[u], a.x, a.y, b.x, b.y);    // + ar br
+        ff_mac(sr[u], er[u], a.z, a.w, b.z, b.w);    // + ai bi
+        ff_mac(si[u], ei[u], a.z, a.w, b.x, b.y);    // + ai br
+        ff_mac(si[u], ei[u], -a.x, -a.y, b.z, b.w);  // - ar bi
+        sa[u] = fmaf(fabsf(a.x) + fabsf(a.z), fabsf(b.x) + fabsf(b.z), sa[u]);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+  if (!ok) return;
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const int t = warp + u * TG_CWARPS;
+    if (t >= G.nt) continue;
+    double re = (double)sr[u] + (double)er[u], im = (double)si[u] + (double)ei[u], ab = (double)sa[u];
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+      ab += __shfl_down_sync(0xffffffffu, ab, o);
+    }
+    if (lane == 0) {
+      const int r = G.tr[t];
+      const TraceRow T = rt[r];
+      const double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+      rows[(size_t)q * nrows + r] = cmul(c, make_double2(re, im));
+      rabs[(size_t)q * nrows + r] = sqrt(c.x * c.x + c.y * c.y) * ab;
+    }
+  }
+}
+
+// Quad groups: at most 2 A blocks and 2 B blocks and the (up to 4) traces
+// between them.  One CTA per (pair, group) walks the nev*nev elements with U
+// independent streams a thread; each element of the group's (at most 4) blocks
+// is loaded once and feeds every trace of the group, so a block shared by two
+// traces is read once instead of twice.
+template <int TPB, int U>
+__global__ void __launch_bounds__(TPB) trace_quads_kernel(const TraceGroup* __restrict__ groups, int ngroups,
+                                                          const TraceRow* __restrict__ rt, int nrows,
+                                                          const float4* const* __restrict__ abase,
+                                                          const float4* const* __restrict__ bbase, int lda, int ldb,
+                                                          int nev, double2* __restrict__ rows,
+                                                          double* __restrict__ rabs) {
+  constexpr int NW = TPB / 32;
+  const int q = blockIdx.x / ngroups, gi = blockIdx.x - q * ngroups;
+  const TraceGroup& G = groups[gi];
+  const int na = G.na, nb = G.nb, nt = G.nt;
+  unsigned mask = 0;  // bit a * 2 + b: trace between A block a and B block b
+  for (int t = 0; t < nt; t++) mask |= 1u << (G.ta[t] * 2 + G.tb[t]);
+  const float4* pa0 = abase[q] + G.aoff[0];
+  const float4* pa1 = abase[q] + G.aoff[na > 1 ? 1 : 0];
+  const float4* pb0 = bbase[q] + G.boff[0];
+  const float4* pb1 = bbase[q] + G.boff[nb > 1 ? 1 : 0];
+  float sr[4], er[4], si[4], ei[4], sa[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) sr[k] = er[k] = si[k] = ei[k] = sa[k] = 0.f;
+  const int total = nev * nev, step = TPB * U, di = step % nev, dj = step / nev;
+  int iu[U], ju[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int e = threadIdx.x + u * TPB;
+    iu[u] = e % nev;
+    ju[u] = e / nev;
+  }
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int e0 = threadIdx.x; e0 < total; e0 += step) {
+    float4 a[U][2], b[U][2];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const bool in = e0 + u * TPB < total;
+      const size_t oa = (size_t)ju[u] * lda + iu[u], ob = (size_t)ju[u] * ldb + iu[u];
+      a[u][0] = in ? pa0[oa] : z;
+      a[u][1] = (in && na > 1) ? pa1[oa] : z;
+      b[u][0] = in ? pb0[ob] : z;
+      b[u][1] = (in && nb > 1) ? pb1[ob] : z;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (!((mask >> k) & 1u)) continue;
+        const float4 x = a[u][k >> 1], y = b[u][k & 1];
+        ff_mac(sr[k], er[k], x.x, x.y, y.x, y.y);    // + ar br
+        ff_mac(sr[k], er[k], x.z, x.w, y.z, y.w);    // + ai bi
+        ff_mac(si[k], ei[k], x.z, x.w, y.x, y.y);    // + ai br
+        ff_mac(si[k], ei[k], -x.x, -x.y, y.z, y.w);  // - ar bi
+        sa[k] = fmaf(fabsf(x.x) + fabsf(x.z), fabsf(y.x) + fabsf(y.z), sa[k]);
+      }
+      iu[u] += di;
+      ju[u] += dj;
+      if (iu[u] >= nev) {
+        iu[u] -= nev;
+        ju[u]++;
+      }
+    }
+  }
+  __shared__ double red[4][3][NW];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if (!((mask >> k) & 1u)) continue;
+    double re = (double)sr[k] + (double)er[k], im = (double)si[k] + (double)ei[k], ab = (double)sa[k];
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+      ab += __shfl_down_sync(0xffffffffu, ab, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[k][0][threadIdx.x >> 5] = re;
+      red[k][1][threadIdx.x >> 5] = im;
+      red[k][2][threadIdx.x >> 5] = ab;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nt) {
+    const int t = threadIdx.x, k = G.ta[t] * 2 + G.tb[t];
+    double re = 0.0, im = 0.0, ab = 0.0;
+    for (int w = 0; w < NW; w++) {
+      re += red[k][0][w];
+      im += red[k][1][w];
+      ab += red[k][2][w];
+    }
+    const int r = G.tr[t];
+    const TraceRow T = rt[r];
+    const double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+    rows[(size_t)q * nrows + r] = cmul(c, make_double2(re, im));
+    rabs[(size_t)q * nrows + r] = sqrt(c.x * c.x + c.y * c.y) * ab;
+  }
+}
+
 // --------------------------------------------------------------- launchers
 // Dynamic shared-memory limits are raised once per kernel (before any graph
 // capture, through split_kernels_prepare, or at the first launch).
@@ -1030,8 +1400,21 @@ int split_kernels_prepare() {
   return CTR_OK;
 }
 
-int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s) {
+int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s,
+                      int form) {
   if (njobs == 0) return CTR_OK;
+  if (form == 1) {
+    static size_t smem_set = 0;
+    const size_t smem = slice_staged_smem(nev, SPLIT_NSLICE * 2);
+    if (smem > smem_set) {
+      CTR_CUDA(cudaFuncSetAttribute(slice_left_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      smem_set = smem;
+    }
+    TimedLaunch tl(s, "slice_left");
+    slice_left_staged_kernel<<<njobs * mtiles * (SPLIT_M / SLQ), 256, smem, s>>>(d_jobs, nev, nchunk, mtiles);
+    CTR_CUDA(cudaGetLastError());
+    return CTR_OK;
+  }
   const size_t smem = 512 + SPLIT_A_STAGE;
   CTR_TRY(ensure_smem(slice_left_kernel, smem, g_attr_sl));
   TimedLaunch tl(s, "slice_left");
@@ -1040,8 +1423,21 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
   return CTR_OK;
 }
 
-int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s) {
+int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s,
+                       int form) {
   if (njobs == 0) return CTR_OK;
+  if (form == 1) {
+    static size_t smem_set = 0;
+    const size_t smem = slice_staged_smem(nev, SPLIT_NSLICE * 3);
+    if (smem > smem_set) {
+      CTR_CUDA(cudaFuncSetAttribute(slice_right_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      smem_set = smem;
+    }
+    TimedLaunch tl(s, "slice_right");
+    slice_right_staged_kernel<<<njobs * ntiles * (SPLIT_N / SLQ), 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+    CTR_CUDA(cudaGetLastError());
+    return CTR_OK;
+  }
   const size_t smem = 512 + SPLIT_B_STAGE;
   CTR_TRY(ensure_smem(slice_right_kernel, smem, g_attr_sr));
   TimedLaunch tl(s, "slice_right");
@@ -1153,6 +1549,138 @@ int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_
   }
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
+}
+
+int launch_trace_groups(const TraceGroup* d_groups, int ngroups, int maxcols, const TraceRow* d_rows, int nrows,
+                        const float4* const* d_abase, const float4* const* d_bbase, int lda, int ldb, int npair,
+                        int nev, double2* rows, double* rabs, int* d_err, cudaStream_t s) {
+  if (npair == 0 || ngroups == 0) return CTR_OK;
+  if (maxcols < 1 || maxcols > TG_MAXA + TG_MAXB) return fail(CTR_ERR_ARG, "trace groups: %d blocks per group", maxcols);
+  const long long nblk = (long long)npair * ngroups;
+  if (nblk > 0x7fffffffLL) return fail(CTR_ERR_ARG, "trace groups: grid too large");
+  const int stage_bytes = maxcols * nev * 16;
+  const size_t smem = (size_t)TG_NSTAGE * stage_bytes;
+  static size_t smem_set = 0;
+  if (smem > smem_set) {
+    CTR_CUDA(cudaFuncSetAttribute(trace_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_set = smem;
+  }
+  TimedLaunch tl(s, "trace_groups");
+  trace_groups_kernel<<<(unsigned)nblk, TG_THREADS, smem, s>>>(d_groups, ngroups, stage_bytes, d_rows, nrows,
+                                                                d_abase, d_bbase, lda, ldb, nev, rows, rabs, d_err);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_trace_quads(const TraceGroup* d_groups, int ngroups, const TraceRow* d_rows, int nrows,
+                       const float4* const* d_abase, const float4* const* d_bbase, int lda, int ldb, int npair,
+                       int nev, double2* rows, double* rabs, int variant, cudaStream_t s) {
+  if (npair == 0 || ngroups == 0) return CTR_OK;
+  const long long nblk = (long long)npair * ngroups;
+  if (nblk > 0x7fffffffLL) return fail(CTR_ERR_ARG, "trace quads: grid too large");
+  TimedLaunch tl(s, "trace_quads");
+  if (variant == 0)
+    trace_quads_kernel<128, 2><<<(unsigned)nblk, 128, 0, s>>>(d_groups, ngroups, d_rows, nrows, d_abase, d_bbase,
+                                                                lda, ldb, nev, rows, rabs);
+  else
+    trace_quads_kernel<64, 4><<<(unsigned)nblk, 64, 0, s>>>(d_groups, ngroups, d_rows, nrows, d_abase, d_bbase,
+                                                              lda, ldb, nev, rows, rabs);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int build_trace_groups(const TraceRow* rows, int nrows, int maxa, int maxb, int maxt,
+                       std::vector<TraceGroup>& groups) {
+  if (maxa > TG_MAXA || maxb > TG_MAXB || maxt > TG_MAXT) return -1;
+  groups.clear();
+  // connected components of the traces, linked by shared A or B blocks
+  std::vector<int> parent(nrows);
+  for (int r = 0; r < nrows; r++) parent[r] = r;
+  auto find = [&](int x) {
+    while (parent[x] != x) x = parent[x] = parent[parent[x]];
+    return x;
+  };
+  {
+    std::map<int, int> firsta, firstb;
+    for (int r = 0; r < nrows; r++) {
+      auto ia = firsta.emplace(rows[r].aoff, r).first;
+      parent[find(r)] = find(ia->second);
+      auto ib = firstb.emplace(rows[r].boff, r).first;
+      parent[find(r)] = find(ib->second);
+    }
+  }
+  std::vector<std::vector<int>> comps;
+  {
+    std::map<int, int> cix;
+    for (int r = 0; r < nrows; r++) {
+      auto it = cix.emplace(find(r), (int)comps.size()).first;
+      if (it->second == (int)comps.size()) comps.emplace_back();
+      comps[it->second].push_back(r);
+    }
+  }
+  int maxcols = 0;
+  TraceGroup cur;
+  auto reset = [&]() { std::memset(&cur, 0, sizeof(cur)); };
+  auto flush = [&]() {
+    if (cur.nt > 0) {
+      maxcols = std::max(maxcols, cur.na + cur.nb);
+      groups.push_back(cur);
+    }
+    reset();
+  };
+  auto slot = [](const int* v, int n, int x) {
+    for (int k = 0; k < n; k++)
+      if (v[k] == x) return k;
+    return -1;
+  };
+  // blocks of a trace list not yet in the current group
+  auto need = [&](const std::vector<int>& tl, int& da, int& db) {
+    std::vector<int> na_, nb_;
+    for (int r : tl) {
+      if (slot(cur.aoff, cur.na, rows[r].aoff) < 0 && std::find(na_.begin(), na_.end(), rows[r].aoff) == na_.end())
+        na_.push_back(rows[r].aoff);
+      if (slot(cur.boff, cur.nb, rows[r].boff) < 0 && std::find(nb_.begin(), nb_.end(), rows[r].boff) == nb_.end())
+        nb_.push_back(rows[r].boff);
+    }
+    da = (int)na_.size();
+    db = (int)nb_.size();
+  };
+  auto add = [&](int r) {
+    int a = slot(cur.aoff, cur.na, rows[r].aoff);
+    if (a < 0) {
+      a = cur.na++;
+      cur.aoff[a] = rows[r].aoff;
+    }
+    int b = slot(cur.boff, cur.nb, rows[r].boff);
+    if (b < 0) {
+      b = cur.nb++;
+      cur.boff[b] = rows[r].boff;
+    }
+    cur.ta[cur.nt] = a;
+    cur.tb[cur.nt] = b;
+    cur.tr[cur.nt] = r;
+    cur.nt++;
+  };
+  auto fits = [&](const std::vector<int>& tl) {
+    int da, db;
+    need(tl, da, db);
+    return cur.na + da <= maxa && cur.nb + db <= maxb && cur.nt + (int)tl.size() <= maxt;
+  };
+  reset();
+  for (const std::vector<int>& c : comps) {
+    if (!fits(c)) flush();
+    if (fits(c)) {
+      for (int r : c) add(r);
+      continue;
+    }
+    // a component larger than a group: trace by trace
+    for (int r : c) {
+      if (!fits({r})) flush();
+      add(r);
+    }
+  }
+  flush();
+  return maxcols;
 }
 
 }  // namespace ctr

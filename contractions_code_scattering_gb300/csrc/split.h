@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "ctr_internal.h"
 
 namespace ctr {
@@ -131,6 +133,17 @@ struct TraceRow {
   float coef[2];
 };
 
+// A group of closing traces that share product blocks: TG_MAXA source-side (A)
+// and TG_MAXB sink-side (B) blocks at most, TG_MAXT traces over them.  Trace k
+// of the group is TraceRow tr[k] (also its output slot) and multiplies block
+// ta[k] of the A list with block tb[k] of the B list.
+constexpr int TG_MAXA = 8, TG_MAXB = 8, TG_MAXT = 16;
+struct TraceGroup {
+  int na, nb, nt, pad;
+  int aoff[TG_MAXA], boff[TG_MAXB];
+  int ta[TG_MAXT], tb[TG_MAXT], tr[TG_MAXT];
+};
+
 // ------------------------------------------------------ float-float helpers
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -155,8 +168,14 @@ __device__ __forceinline__ void ff_mac(float& S, float& E, float xh, float xl, f
   E += t + e;
 }
 
-int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s);
-int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s);
+// Slicing of stacked operands.  form 0: one CTA per operand tile, which reads
+// the operand once for the scale exponents and once per K chunk; form 1: one
+// CTA per quarter tile, which stages its quarter in shared memory (read once).
+// Both write the same bytes.
+int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s,
+                      int form = 0);
+int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s,
+                       int form = 0);
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
 // Raises the shared-memory limits of the split kernels and caches the SM count.
 int split_kernels_prepare();
@@ -171,6 +190,25 @@ constexpr int TRACE_VARIANTS = 9;
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,
                       int lda, int ldb, int npair, int nev, double2* rows, double* rabs, int variant,
                       cudaStream_t s);
+// Grouped closing traces (same results as launch_trace_rows): one CTA per
+// (pair, group) streams the columns of the group's blocks into shared memory by
+// bulk copies and computes every trace of the group from them, so each block is
+// read once per group.  maxcols = the largest na + nb of the groups.
+int launch_trace_groups(const TraceGroup* d_groups, int ngroups, int maxcols, const TraceRow* d_rows, int nrows,
+                        const float4* const* d_abase, const float4* const* d_bbase, int lda, int ldb, int npair,
+                        int nev, double2* rows, double* rabs, int* d_err, cudaStream_t s);
+// Quad groups (at most 2 A blocks, 2 B blocks, 4 traces; build_trace_groups
+// with limits 2, 2, 4): one CTA per (pair, group) loads each element of the
+// group's blocks once into registers for all its traces.  variant 0: 128
+// threads x 2 element streams, 1: 64 threads x 4 streams.
+int launch_trace_quads(const TraceGroup* d_groups, int ngroups, const TraceRow* d_rows, int nrows,
+                       const float4* const* d_abase, const float4* const* d_bbase, int lda, int ldb, int npair,
+                       int nev, double2* rows, double* rabs, int variant, cudaStream_t s);
+// Builds the groups of a trace list: traces linked by a shared block go to the
+// same group where the limits (maxa A blocks, maxb B blocks, maxt traces; at
+// most TG_MAXA, TG_MAXB, TG_MAXT) allow.  Returns the largest na + nb.
+int build_trace_groups(const TraceRow* rows, int nrows, int maxa, int maxb, int maxt,
+                       std::vector<TraceGroup>& groups);
 // Task-form slicing: the row and column exponent bounds of every distinct block
 // of a launch first (bexp [nblk][2][nev]: bound of row r at [0][r], of column c at
 // [1][c]), then the slices of each (operand tile, K chunk), whose scale exponents

@@ -50,6 +50,53 @@ def test_rho_single_row_buffer(cuda, engine):
         _close(got[0].cpu().numpy(), ref, TOL[engine])
 
 
+@pytest.mark.parametrize("n", [9, 37, 100, 128])
+def test_grouped_traces_match_per_trace_kernel(cuda, n):
+    """The grouped closing-trace kernels (trace_rows candidate 9: blocks shared
+    by a group of traces staged once in shared memory by bulk copies; 10 and 11:
+    quad groups of at most 2 + 2 blocks loaded once into registers) give the
+    oracle's rho and sigma at the split tolerance, and the per-trace kernel's
+    values to float-float rounding (1e-12 of the largest entry)."""
+    nt = 2
+    prop, mom5 = _inputs(nt, n, seed=300 + n)
+    d_prop, d_mom = torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda)
+    ref_rho = O.rho(prop, mom5)
+    ref_sig = O.sigma(prop, np.ascontiguousarray(mom5[:, :2]))
+    got = {}
+    try:
+        for v in (9, 10, 11, 6):
+            api.tune_force("trace_rows", v)
+            got[v] = (api.run_contract_rho(d_prop, d_mom, engine="split").cpu().numpy(),
+                      api.run_contract_sigma(d_prop, torch.from_numpy(np.ascontiguousarray(mom5[:, :2])).to(cuda),
+                                             engine="split").cpu().numpy())
+    finally:
+        api.tune_force("trace_rows", -1)
+    for v in (9, 10, 11):
+        _close(got[v][0], ref_rho, TOL["split"])
+        _close(got[v][1], ref_sig, TOL["split"])
+        _close(got[v][0], got[6][0], 1e-12)
+        _close(got[v][1], got[6][1], 1e-12)
+
+
+@pytest.mark.parametrize("n", [9, 37, 100, 128])
+def test_staged_slicer_writes_the_same_bytes(cuda, n):
+    """The staged perambulator slicers (slice_tau form 1: one read of the operand
+    through shared memory) write the same operand bytes as form 0, so the split
+    engine's rho values are bitwise identical."""
+    nt = 2
+    prop, mom5 = _inputs(nt, n, seed=500 + n)
+    d_prop, d_mom = torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda)
+    got = {}
+    try:
+        for form in (0, 1):
+            api.tune_force("slice_tau", form)
+            got[form] = api.run_contract_rho(d_prop, d_mom, engine="split").cpu().numpy()
+    finally:
+        api.tune_force("slice_tau", -1)
+    assert np.array_equal(got[0], got[1])
+    _close(got[1], O.rho(prop, mom5), TOL["split"])
+
+
 @pytest.mark.parametrize("engine", ["fp64", "split"])
 def test_sigma_matches_oracle(cuda, engine):
     nt, n = 3, 20
