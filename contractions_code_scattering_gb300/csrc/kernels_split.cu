@@ -84,6 +84,19 @@ __device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t W, int s, bool neg)
   return __float2bfloat16_rn(neg ? -v : v);
 }
 
+// The value of slice_bf16 before its rounding to BF16 (exact in BF16).
+__device__ __forceinline__ float slice_f32(uint64_t W, int s, bool neg) {
+  const int d = s == 0 ? (int)(W >> 55) : (int)((W >> slice_shift(s)) & 511u) - 256;
+  const float v = (float)d * __int_as_float((127 + slice_shift(s) - 63) << 23);
+  return neg ? -v : v;
+}
+
+// Two slices of adjacent k as one packed BF16 pair (k in the low half).
+__device__ __forceinline__ uint32_t slice_pair(uint64_t W0, bool n0, uint64_t W1, bool n1, int s) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(slice_f32(W0, s, n0), slice_f32(W1, s, n1));
+  return *(const uint32_t*)&p;
+}
+
 // Byte offset of element (row, k) of one (slice, plane) sub-tile inside a
 // K-chunk stage: core matrices of 8 rows x 8 elements, K-adjacent at +128 B,
 // row-group-adjacent at +256 B.
@@ -285,21 +298,21 @@ __global__ void __launch_bounds__(256) slice_left_staged_kernel(const SliceLeftJ
   }
   __syncthreads();
   uint8_t* dst_tile = J.out + (size_t)mt * nchunk * SPLIT_A_STAGE + qt * 1024;
+  static_assert(SLQ * SPLIT_K == 2 * 256, "two adjacent k per thread");
+  const int rr = threadIdx.x >> 3, kk = (threadIdx.x & 7) * 2;
+  const uint32_t off = core_offset(rr, kk);  // k and k + 1 are adjacent
+  const int E = sexp[rr];
   for (int kc = 0; kc < nchunk; kc++) {
+    const int k = kc * SPLIT_K + kk;
+    const double2 v0 = k < nev ? data[rr * nev + k] : make_double2(0.0, 0.0);
+    const double2 v1 = k + 1 < nev ? data[rr * nev + k + 1] : make_double2(0.0, 0.0);
+    bool nr0, ni0, nr1, ni1;
+    const uint64_t Ur0 = round_fixed(f64_fixed(v0.x, E, nr0)), Ui0 = round_fixed(f64_fixed(v0.y, E, ni0));
+    const uint64_t Ur1 = round_fixed(f64_fixed(v1.x, E, nr1)), Ui1 = round_fixed(f64_fixed(v1.y, E, ni1));
 #pragma unroll
-    for (int u = 0; u < SLQ * SPLIT_K / 256; u++) {
-      const int e = threadIdx.x + 256 * u;
-      const int rr = e >> 4, kk = e & 15, k = kc * SPLIT_K + kk;
-      const double2 v = k < nev ? data[rr * nev + k] : make_double2(0.0, 0.0);
-      const int E = sexp[rr];
-      bool nr, ni;
-      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
-      const uint32_t off = core_offset(rr, kk);
-#pragma unroll
-      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
-        *(__nv_bfloat16*)(stage + (sl * 2 + 0) * 1024 + off) = slice_bf16(Ur, sl, nr);
-        *(__nv_bfloat16*)(stage + (sl * 2 + 1) * 1024 + off) = slice_bf16(Ui, sl, ni);
-      }
+    for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+      *(uint32_t*)(stage + (sl * 2 + 0) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
+      *(uint32_t*)(stage + (sl * 2 + 1) * 1024 + off) = slice_pair(Ui0, ni0, Ui1, ni1, sl);
     }
     __syncthreads();
     uint8_t* d = dst_tile + (size_t)kc * SPLIT_A_STAGE;
@@ -357,23 +370,23 @@ __global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRigh
   }
   __syncthreads();
   uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE + qt * 1024;
+  static_assert(SLQ * SPLIT_K == 2 * 256, "two adjacent k per thread");
+  const int nn = threadIdx.x & 31, kk = (threadIdx.x >> 5) * 2;
+  const uint32_t off = core_offset(nn, kk);  // k and k + 1 are adjacent
+  const int E = sexp[nn];
   for (int kc = 0; kc < nchunk; kc++) {
+    const int k = kc * SPLIT_K + kk;
+    const double2 v0 = k < nev ? data[k * SLQ + nn] : make_double2(0.0, 0.0);
+    const double2 v1 = k + 1 < nev ? data[(k + 1) * SLQ + nn] : make_double2(0.0, 0.0);
+    bool nr0, ni0, nr1, ni1;
+    const uint64_t Ur0 = round_fixed(f64_fixed(v0.x, E, nr0)), Ui0 = round_fixed(f64_fixed(v0.y, E, ni0));
+    const uint64_t Ur1 = round_fixed(f64_fixed(v1.x, E, nr1)), Ui1 = round_fixed(f64_fixed(v1.y, E, ni1));
 #pragma unroll
-    for (int u = 0; u < SLQ * SPLIT_K / 256; u++) {
-      const int e = threadIdx.x + 256 * u;
-      const int nn = e % SLQ, kk = e / SLQ, k = kc * SPLIT_K + kk;
-      const double2 v = k < nev ? data[k * SLQ + nn] : make_double2(0.0, 0.0);
-      const int E = sexp[nn];
-      bool nr, ni;
-      const uint64_t Ur = round_fixed(f64_fixed(v.x, E, nr)), Ui = round_fixed(f64_fixed(v.y, E, ni));
-      const uint32_t off = core_offset(nn, kk);
-#pragma unroll
-      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
-        // planes -im, re, im (packed complex MMAs)
-        *(__nv_bfloat16*)(stage + (sl * 3 + 0) * 1024 + off) = slice_bf16(Ui, sl, !ni);
-        *(__nv_bfloat16*)(stage + (sl * 3 + 1) * 1024 + off) = slice_bf16(Ur, sl, nr);
-        *(__nv_bfloat16*)(stage + (sl * 3 + 2) * 1024 + off) = slice_bf16(Ui, sl, ni);
-      }
+    for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+      // planes -im, re, im (packed complex MMAs)
+      *(uint32_t*)(stage + (sl * 3 + 0) * 1024 + off) = slice_pair(Ui0, !ni0, Ui1, !ni1, sl);
+      *(uint32_t*)(stage + (sl * 3 + 1) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
+      *(uint32_t*)(stage + (sl * 3 + 2) * 1024 + off) = slice_pair(Ui0, ni0, Ui1, ni1, sl);
     }
     __syncthreads();
     uint8_t* d = dst_tile + (size_t)kc * SPLIT_B_STAGE;
