@@ -1166,6 +1166,7 @@ __global__ void __launch_bounds__(TPB) trace_rows_ilp_kernel(const TraceRow* __r
 // mbarriers; every wait is bounded and a timeout records an error code.
 constexpr int TG_NSTAGE = 4, TG_CWARPS = TG_MAXT / 2;
 constexpr int TG_THREADS = 32 * (TG_CWARPS + 1);
+constexpr size_t trace_groups_max_smem() { return (size_t)TG_NSTAGE * (TG_MAXA + TG_MAXB) * SPLIT_MAXK * 16; }
 
 __global__ void __launch_bounds__(TG_THREADS) trace_groups_kernel(
     const TraceGroup* __restrict__ groups, int ngroups, int stage_bytes, const TraceRow* __restrict__ rt, int nrows,
@@ -1380,6 +1381,7 @@ static int ensure_smem(K kernel, size_t smem, bool& done) {
   }
   return CTR_OK;
 }
+static bool g_attr_sls = false, g_attr_srs = false, g_attr_tg = false;
 static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr = false, g_attr_std = false,
             g_attr_hp = false;
 static int g_nsm = 0;
@@ -1406,6 +1408,9 @@ int split_kernels_prepare() {
   CTR_TRY(sm_count(&nsm));
   CTR_TRY(ensure_smem(slice_left_kernel, 512 + SPLIT_A_STAGE, g_attr_sl));
   CTR_TRY(ensure_smem(slice_right_kernel, 512 + SPLIT_B_STAGE, g_attr_sr));
+  CTR_TRY(ensure_smem(slice_left_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 2), g_attr_sls));
+  CTR_TRY(ensure_smem(slice_right_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 3), g_attr_srs));
+  CTR_TRY(ensure_smem(trace_groups_kernel, trace_groups_max_smem(), g_attr_tg));
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
@@ -1417,12 +1422,9 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
                       int form) {
   if (njobs == 0) return CTR_OK;
   if (form == 1) {
-    static size_t smem_set = 0;
+    if (nev > SPLIT_MAXK) return fail(CTR_ERR_ARG, "slicer: Nev %d above %d", nev, SPLIT_MAXK);
     const size_t smem = slice_staged_smem(nev, SPLIT_NSLICE * 2);
-    if (smem > smem_set) {
-      CTR_CUDA(cudaFuncSetAttribute(slice_left_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      smem_set = smem;
-    }
+    CTR_TRY(ensure_smem(slice_left_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 2), g_attr_sls));
     TimedLaunch tl(s, "slice_left");
     slice_left_staged_kernel<<<njobs * mtiles * (SPLIT_M / SLQ), 256, smem, s>>>(d_jobs, nev, nchunk, mtiles);
     CTR_CUDA(cudaGetLastError());
@@ -1440,12 +1442,9 @@ int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchu
                        int form) {
   if (njobs == 0) return CTR_OK;
   if (form == 1) {
-    static size_t smem_set = 0;
+    if (nev > SPLIT_MAXK) return fail(CTR_ERR_ARG, "slicer: Nev %d above %d", nev, SPLIT_MAXK);
     const size_t smem = slice_staged_smem(nev, SPLIT_NSLICE * 3);
-    if (smem > smem_set) {
-      CTR_CUDA(cudaFuncSetAttribute(slice_right_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      smem_set = smem;
-    }
+    CTR_TRY(ensure_smem(slice_right_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 3), g_attr_srs));
     TimedLaunch tl(s, "slice_right");
     slice_right_staged_kernel<<<njobs * ntiles * (SPLIT_N / SLQ), 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
     CTR_CUDA(cudaGetLastError());
@@ -1571,13 +1570,10 @@ int launch_trace_groups(const TraceGroup* d_groups, int ngroups, int maxcols, co
   if (maxcols < 1 || maxcols > TG_MAXA + TG_MAXB) return fail(CTR_ERR_ARG, "trace groups: %d blocks per group", maxcols);
   const long long nblk = (long long)npair * ngroups;
   if (nblk > 0x7fffffffLL) return fail(CTR_ERR_ARG, "trace groups: grid too large");
+  if (nev > SPLIT_MAXK) return fail(CTR_ERR_ARG, "trace groups: Nev %d above %d", nev, SPLIT_MAXK);
   const int stage_bytes = maxcols * nev * 16;
   const size_t smem = (size_t)TG_NSTAGE * stage_bytes;
-  static size_t smem_set = 0;
-  if (smem > smem_set) {
-    CTR_CUDA(cudaFuncSetAttribute(trace_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    smem_set = smem;
-  }
+  CTR_TRY(ensure_smem(trace_groups_kernel, trace_groups_max_smem(), g_attr_tg));
   TimedLaunch tl(s, "trace_groups");
   trace_groups_kernel<<<(unsigned)nblk, TG_THREADS, smem, s>>>(d_groups, ngroups, stage_bytes, d_rows, nrows,
                                                                 d_abase, d_bbase, lda, ldb, nev, rows, rabs, d_err);
