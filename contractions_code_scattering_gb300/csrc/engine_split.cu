@@ -292,8 +292,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
       CTR_TRY(launch_slice_left((const SliceLeftJob*)d_lj, np, N, nchunk, mtT, stream, form));
       return launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream, form);
     };
-    int sform = 0;
-    CTR_TRY(tune_resolve("slice_tau", shape, 2, 0, stream, slice_tau, &sform));
+    int sform = 1;
+    CTR_TRY(tune_resolve("slice_tau", shape, 2, 1, stream, slice_tau, &sform));
     CTR_TRY(slice_tau(sform));
     // tile walk of each GEMM (autotuned; idempotent, so candidates re-run on the same data)
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};
