@@ -502,10 +502,10 @@ def roofline(engine, report, steps, nt, nev, nmom):
     mma_flops = steps * prods * 8.0 * n3 * 15 * (112.0 / 100.0)
     achieved = mma_flops / launches / (ms / launches / 1e3) / 1e12
     # DRAM traffic per launch: the ncu capture of one launch at Nt=8 (64 pairs, 7 momenta, Nev=100)
-    # read 0.245 GB and wrote 1.089 GB, i.e. 20.8 MB per (t_sink, t_src) pair; scaled by the
+    # read 0.390 GB and wrote 1.093 GB, i.e. 23.2 MB per (t_sink, t_src) pair; scaled by the
     # pairs one launch processes here (both GEMMs of a batch have the same output size)
     pairs_per_launch = steps * nt * nt * 2.0 / launches
-    traffic = 20.84e6 * pairs_per_launch * (nmom / 7.0) if nev == 100 else None
+    traffic = 23.17e6 * pairs_per_launch * (nmom / 7.0) if nev == 100 else None
     return {"kernel": "split_gemm", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at Nt=8, scaled "
