@@ -159,9 +159,9 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     }
     void *dl, *dr;
     CTR_TRY(upload(WS_TASKS, lj.data(), lj.size() * sizeof(SliceLeftJob), &dl, stream));
-    CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, Nt, N, nchunk, F.mtiles, stream));
+    CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, Nt, N, nchunk, F.mtiles, stream, 1));
     CTR_TRY(upload(WS_TASKS2, rj.data(), rj.size() * sizeof(SliceRightJob), &dr, stream));
-    CTR_TRY(launch_slice_right((const SliceRightJob*)dr, Nt, N, nchunk, F.ntiles, stream));
+    CTR_TRY(launch_slice_right((const SliceRightJob*)dr, Nt, N, nchunk, F.ntiles, stream, 1));
   }
 
   // ---- per (t_sink, t_src) pair buffers
@@ -503,9 +503,9 @@ int zgemm_split_batched(int N, int nb, const double* const* x, const double* con
   }
   void *dl, *dr, *dg;
   CTR_TRY(upload(WS_TASKS, lj.data(), nb * sizeof(SliceLeftJob), &dl, stream));
-  CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, nb, N, nchunk, 1, stream));
+  CTR_TRY(launch_slice_left((const SliceLeftJob*)dl, nb, N, nchunk, 1, stream, 1));
   CTR_TRY(upload(WS_TASKS2, rj.data(), nb * sizeof(SliceRightJob), &dr, stream));
-  CTR_TRY(launch_slice_right((const SliceRightJob*)dr, nb, N, nchunk, nt, stream));
+  CTR_TRY(launch_slice_right((const SliceRightJob*)dr, nb, N, nchunk, nt, stream, 1));
   CTR_TRY(upload(WS_GEMM_A, gi.data(), nb * sizeof(SplitGemmInst), &dg, stream));
   SplitGemmBatch G{(const SplitGemmInst*)dg, 1, nt, nchunk, N, N, ldo};
   CTR_TRY(launch_split_gemm(G, nb, d_err, stream));
