@@ -283,20 +283,25 @@ __global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restr
   const int n2 = N * N;
   const bool want_abs = T.absout != nullptr;
   double re = 0.0, im = 0.0, ab = 0.0;
+  // two FMAs into each accumulator per element (the FP64 pipe is the bound)
   if (T.mode == 0) {
     for (int e = threadIdx.x; e < n2; e += 256) {
       double2 x = T.X[e], y = T.Y[e];
-      re += x.x * y.x + x.y * y.y;
-      im += x.y * y.x - x.x * y.y;
-      if (want_abs) ab += (fabs(x.x) + fabs(x.y)) * (fabs(y.x) + fabs(y.y));
+      re = fma(x.x, y.x, re);
+      re = fma(x.y, y.y, re);
+      im = fma(x.y, y.x, im);
+      im = fma(-x.x, y.y, im);
+      if (want_abs) ab = fma(fabs(x.x) + fabs(x.y), fabs(y.x) + fabs(y.y), ab);
     }
   } else {
     for (int e = threadIdx.x; e < n2; e += 256) {
       int i = e / N, j = e % N;
       double2 x = T.X[e], y = T.Y[(size_t)j * N + i];
-      re += x.x * y.x - x.y * y.y;
-      im += x.x * y.y + x.y * y.x;
-      if (want_abs) ab += (fabs(x.x) + fabs(x.y)) * (fabs(y.x) + fabs(y.y));
+      re = fma(x.x, y.x, re);
+      re = fma(-x.y, y.y, re);
+      im = fma(x.x, y.y, im);
+      im = fma(x.y, y.x, im);
+      if (want_abs) ab = fma(fabs(x.x) + fabs(x.y), fabs(y.x) + fabs(y.y), ab);
     }
   }
   re = block_sum_256(re);

@@ -445,24 +445,44 @@ __device__ __forceinline__ bool task_right_all_dag(const SliceTaskRJob& J) {
 // bexp[b][0][r] = max_c bound(row r), bexp[b][1][c] = max_r bound(column c).
 __global__ void __launch_bounds__(256) block_exp_kernel(const double2* const* __restrict__ blk, int nev,
                                                         int* __restrict__ bexp) {
-  __shared__ int rmax[SPLIT_MAXK], cmax[SPLIT_MAXK];
-  for (int i = threadIdx.x; i < nev; i += 256) rmax[i] = cmax[i] = -30000;
-  __syncthreads();
+  // warp w scans rows w, w + 8, ...: the row bound by a shuffle reduction, and
+  // lane l keeps the bound of columns l, l + 32, ... over its warp's rows
+  // (nev <= SPLIT_MAXK = 128, so 4 columns a lane); the warps' column bounds
+  // are combined in shared memory at the end
+  __shared__ int cpart[8][SPLIT_MAXK];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double2* B = blk[blockIdx.x];
-  const int total = nev * nev;
-  for (int e = threadIdx.x; e < total; e += 256) {
-    const double2 v = B[e];
-    const int x = max(f64_exp_bound(v.x), f64_exp_bound(v.y));
-    if (x > -30000) {
-      atomicMax(&rmax[e / nev], x);
-      atomicMax(&cmax[e % nev], x);
-    }
-  }
-  __syncthreads();
   int* o = bexp + (size_t)blockIdx.x * 2 * nev;
-  for (int i = threadIdx.x; i < nev; i += 256) {
-    o[i] = rmax[i];
-    o[nev + i] = cmax[i];
+  int cm[SPLIT_MAXK / 32];
+#pragma unroll
+  for (int u = 0; u < SPLIT_MAXK / 32; u++) cm[u] = -30000;
+#pragma unroll 2
+  for (int r = warp; r < nev; r += 8) {
+    const double2* row = B + (size_t)r * nev;
+    double2 v[SPLIT_MAXK / 32];
+#pragma unroll
+    for (int u = 0; u < SPLIT_MAXK / 32; u++) {
+      const int c = lane + 32 * u;
+      v[u] = c < nev ? row[c] : make_double2(0.0, 0.0);
+    }
+    int rm = -30000;
+#pragma unroll
+    for (int u = 0; u < SPLIT_MAXK / 32; u++) {
+      if (lane + 32 * u >= nev) continue;
+      const int x = max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y));
+      rm = max(rm, x);
+      cm[u] = max(cm[u], x);
+    }
+    for (int off = 16; off; off >>= 1) rm = max(rm, __shfl_xor_sync(0xffffffffu, rm, off));
+    if (lane == 0) o[r] = rm;
+  }
+#pragma unroll
+  for (int u = 0; u < SPLIT_MAXK / 32; u++) cpart[warp][lane + 32 * u] = cm[u];
+  __syncthreads();
+  for (int c = threadIdx.x; c < nev; c += 256) {
+    int m = cpart[0][c];
+    for (int w = 1; w < 8; w++) m = max(m, cpart[w][c]);
+    o[nev + c] = m;
   }
 }
 
