@@ -353,6 +353,9 @@ __global__ void rowsum_refine_kernel(const double2* __restrict__ rows, const dou
   }
 }
 
+// Smallest trusted error scale sum |coef| sum |A||B| of a float-float entry.
+constexpr double FF_MIN_SCALE = 0x1p-90;
+
 __global__ void rowsum_coef_refine_kernel(const double2* __restrict__ tr, const double* __restrict__ trabs, int ntr,
                                           const int* __restrict__ off, const int* __restrict__ idx,
                                           const int* __restrict__ tix, const float* __restrict__ coef, int nout,
@@ -372,7 +375,10 @@ __global__ void rowsum_coef_refine_kernel(const double2* __restrict__ tr, const 
     sc += sqrt(cr * cr + ci * ci) * trabs[t];
   }
   out[(size_t)p * nout + o] = make_double2(re, im);
-  if (eps_over_tol > 0.0 && sc * eps_over_tol > sqrt(re * re + im * im)) {
+  // flagged: an error estimate above the tolerance, a NaN (a product whose
+  // scale left the float-float range), or an error scale so small that the
+  // FP32 words of its traces may have underflowed
+  if (eps_over_tol > 0.0 && (!(sc * eps_over_tol <= sqrt(re * re + im * im)) || sc < FF_MIN_SCALE)) {
     const int slot = atomicAdd(count, 1);
     list[slot] = (pair_base + p) * nout + o;
   }

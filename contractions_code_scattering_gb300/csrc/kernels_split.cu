@@ -653,6 +653,10 @@ __device__ __forceinline__ double i2d_scaled(long long I, int e) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
+// Smallest row + column scale exponent of a float-float product (below it the
+// FP32 words of the products' traces would leave the normal range).
+constexpr int FF_MIN_EXP = -100;
+
 __device__ __forceinline__ float pow2f(int e) {
   e = max(-126, min(127, e));
   return __int_as_float((127 + e) << 23);
@@ -845,7 +849,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       }
       const int grow = mt * SPLIT_M + row;
       const bool rvalid = grow < g.mrows;
-      const float srow = pow2f(I->lexp[grow]);
+      const int erow = I->lexp[grow];
       // one thread waits for the accumulators; the outcome is shared so that
       // all epilogue threads leave the loop together
       if (et == 0) {
@@ -970,7 +974,12 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
           for (int c = 0; c < CPW; c++) {
             const int gcol = nt * C::BN + cbase + c;
             if (gcol >= g.ncols) continue;
-            const float sc = srow * pow2f(sexp[cbase + c]);
+            // the float-float products and their traces stay accurate while the
+            // scale stays well inside FP32's normal range; below 2^-100 the
+            // product is written as NaN, which flags the entries that use it for
+            // recomputation in FP64 range
+            const int e = erow + sexp[cbase + c];
+            const float sc = e < FF_MIN_EXP ? __int_as_float(0x7fc00000) : pow2f(e);
             outp[(size_t)gcol * ldo + grow] =
                 make_float4(res[c].x * sc, res[c].y * sc, res[c].z * sc, res[c].w * sc);
           }

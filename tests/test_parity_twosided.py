@@ -97,6 +97,23 @@ def test_staged_slicer_writes_the_same_bytes(cuda, n):
     _close(got[1], O.rho(prop, mom5), TOL["split"])
 
 
+@pytest.mark.parametrize("shift", [60, 110])
+def test_split_rho_beyond_float_float_range(cuda, shift):
+    """Perambulators scaled by 2^-shift push the split engine's two-sided form
+    out of its float-float range: at 2^-60 the products' traces would reach
+    FP32's subnormals (their error scales fall below 2^-90), at 2^-110 the
+    product scales themselves (below 2^-100, written as NaN).  Those entries are
+    flagged and recomputed with FP64 range, so the results still meet the oracle."""
+    nt, n = 2, 16
+    prop, mom5 = _inputs(nt, n, seed=700 + shift)
+    prop = prop * 2.0 ** -shift
+    ref = O.rho(prop, mom5)
+    got = api.run_contract_rho(torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda), engine="split")
+    got = got.cpu().numpy()
+    assert np.isfinite(got).all()
+    _close(got, ref, TOL["split"])
+
+
 @pytest.mark.parametrize("engine", ["fp64", "split"])
 def test_sigma_matches_oracle(cuda, engine):
     nt, n = 3, 20
