@@ -102,7 +102,9 @@ __global__ void __launch_bounds__(256) diag_reduce_kernel(const DiagTask* __rest
         }
       }
       __syncthreads();
-      for (int mm = ty; mm < 32; mm += 8) cmac(acc, xs[tx][mm], ys[mm][tx]);
+      // only the tile's valid m (the padding beyond N would still cost the FP64 pipe)
+      const int mlim = min(32, N - m0);
+      for (int mm = ty; mm < mlim; mm += 8) cmac(acc, xs[tx][mm], ys[mm][tx]);
       __syncthreads();
     }
     part[ty][tx] = acc;
