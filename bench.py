@@ -37,7 +37,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--engine", default="auto", choices=["auto", "split", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine (0 = skip)")
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--graph", type=int, default=1, help="time replays of the step recorded as a CUDA graph "
                     "(the eager calls are timed beside them); 0 = eager calls only")
     ap.add_argument("--tune", type=int, default=1, help="autotune the knobs on the first warm-up step")
