@@ -146,8 +146,10 @@ __global__ void pipi_combine_kernel(const double2* __restrict__ tr, int ntr, int
     const double w[3] = {iso == 1 ? 2.0 : 1.0 / 3.0, iso == 1 ? 2.0 : 1.0 / 3.0, iso == 1 ? 0.0 : 5.0 / 3.0};
     const double scale[5] = {w[0] * ab[0], w[1] * ab[1], mag(sum[3]) * ab[4] + mag(sum[4]) * ab[3],
                              mag(sum[5]) * ab[6] + mag(sum[6]) * ab[5], w[2] * ab[2]};
+    // flagged: an error estimate above the tolerance (or not a number), or an
+    // error scale that underflowed while the value did not
     for (int k = 0; k < 5; k++)
-      if (scale[k] * eps_over_tol > mag(o[k])) {
+      if (!(scale[k] * eps_over_tol <= mag(o[k])) || (scale[k] == 0.0 && mag(o[k]) > 0.0)) {
         list[atomicAdd(count, 1)] = (pair_base + p) * 5 + k;
         break;
       }

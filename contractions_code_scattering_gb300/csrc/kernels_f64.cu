@@ -273,6 +273,27 @@ __global__ void __launch_bounds__(NFR * 32, 1) zgemm_f64_dmma_kernel(const ZTask
 }
 
 // ---------------------------------------------------------------- trace
+// The error scale sum (|Re x| + |Im x|)(|Re y| + |Im y|) of a trace needs a few
+// significant bits, not FP64: it is accumulated in FP32 from the doubles' high
+// words, scaled by 2^TRACE_ABS_SHIFT so that products from 2^-206 to 2^48 stay
+// in FP32's range (smaller ones flush to zero, which the refinement checks
+// treat as "flag if the value is not zero"), with integer operations only, so
+// that the FP64 pipe, the bound of these kernels on GB300, does just the four
+// FMAs of the complex product.
+constexpr int TRACE_ABS_SHIFT = 40;
+
+// |v| 2^TRACE_ABS_SHIFT as a float, the mantissa truncated to 20 bits; 0 below
+// FP32's normal range, infinity above it
+__device__ __forceinline__ float abs_scaled_f32(double v) {
+  const int hi = __double2hiint(v) & 0x7FFFFFFF;
+  const int e = (hi >> 20) - 1023 + 127 + TRACE_ABS_SHIFT;
+  if (e <= 0) return 0.f;
+  if (e >= 255) return __int_as_float(0x7F800000);
+  return __int_as_float((e << 23) | ((hi & 0xFFFFF) << 3));
+}
+
+__device__ __forceinline__ float abs1_scaled_f32(double2 v) { return abs_scaled_f32(v.x) + abs_scaled_f32(v.y); }
+
 // out = coef * sum_e X_e * conj(Y_e) over the Nev*Nev elements (mode 0), or
 // coef * sum_ij X_ij * Y_ji = coef * Tr[X Y] (mode 1).  One CTA per task; the
 // reduction tree is fixed, so results are bitwise reproducible.
@@ -282,7 +303,8 @@ __global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restr
   const TraceTask& T = tasks[t];
   const int n2 = N * N;
   const bool want_abs = T.absout != nullptr;
-  double re = 0.0, im = 0.0, ab = 0.0;
+  double re = 0.0, im = 0.0;
+  float abf = 0.f;
   // two FMAs into each accumulator per element (the FP64 pipe is the bound)
   if (T.mode == 0) {
     for (int e = threadIdx.x; e < n2; e += 256) {
@@ -291,7 +313,7 @@ __global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restr
       re = fma(x.y, y.y, re);
       im = fma(x.y, y.x, im);
       im = fma(-x.x, y.y, im);
-      if (want_abs) ab = fma(fabs(x.x) + fabs(x.y), fabs(y.x) + fabs(y.y), ab);
+      if (want_abs) abf = fmaf(abs1_scaled_f32(x), abs1_scaled_f32(y), abf);
     }
   } else {
     for (int e = threadIdx.x; e < n2; e += 256) {
@@ -301,12 +323,13 @@ __global__ void __launch_bounds__(256) trace_f64_kernel(const TraceTask* __restr
       re = fma(-x.y, y.y, re);
       im = fma(x.x, y.y, im);
       im = fma(x.y, y.x, im);
-      if (want_abs) ab = fma(fabs(x.x) + fabs(x.y), fabs(y.x) + fabs(y.y), ab);
+      if (want_abs) abf = fmaf(abs1_scaled_f32(x), abs1_scaled_f32(y), abf);
     }
   }
   re = block_sum_256(re);
   im = block_sum_256(im);
-  if (want_abs) ab = block_sum_256(ab);
+  double ab = 0.0;
+  if (want_abs) ab = block_sum_256((double)abf) * 0x1p-80;  // 2^(-2 TRACE_ABS_SHIFT)
   if (threadIdx.x == 0) {
     double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
     double2 s = make_double2(re, im);
@@ -347,7 +370,10 @@ __global__ void rowsum_refine_kernel(const double2* __restrict__ rows, const dou
     sc += rabs[r];
   }
   out[(size_t)p * nout + o] = make_double2(re, im);
-  if (eps_over_tol > 0.0 && sc * eps_over_tol > sqrt(re * re + im * im)) {
+  // flagged: an error estimate above the tolerance (or not a number), or an
+  // error scale that underflowed while the value did not
+  const double mag = sqrt(re * re + im * im);
+  if (eps_over_tol > 0.0 && (!(sc * eps_over_tol <= mag) || (sc == 0.0 && mag > 0.0))) {
     const int slot = atomicAdd(count, 1);
     list[slot] = (pair_base + p) * nout + o;
   }
