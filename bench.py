@@ -57,14 +57,20 @@ def parse():
 
 # ----------------------------------------------------------------- helpers
 def dist_setup():
+    """Replicas: one process per GPU (torchrun env), NCCL on GPUs, gloo without
+    them (the host-side logic is tested that way).  No collective touches the
+    data path; the ranks only meet at barriers and in the max-over-ranks time."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
         import torch
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     return ws, rank, local
 
 
@@ -75,13 +81,21 @@ def barrier(ws):
 
 
 def allmax(ws, x):
+    """The largest x over the ranks (the slowest replica's time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(ws, units_per_rank, seconds_max):
+    """Whole-job throughput of ws replicas: every rank processed units_per_rank
+    units, and the job took the slowest rank's time."""
+    return ws * units_per_rank / seconds_max
 
 
 class ClockSampler:
@@ -315,7 +329,7 @@ def main():
     t_eager, launches_eager = timed(lambda: step(engine), args.steps)
     report = _lib.timing_report()
     _lib.timing_enable(False)
-    eager = {"ms_per_step": 1e3 * t_eager / args.steps, "value": ws * diagrams * args.steps / t_eager,
+    eager = {"ms_per_step": 1e3 * t_eager / args.steps, "value": replica_value(ws, diagrams * args.steps, t_eager),
              "gpu_launches": int(launches_eager)}
     graph_info = None
     if args.graph:
@@ -332,7 +346,7 @@ def main():
     refined = int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
     clk = clocks.stop()
     ms_per_step = 1e3 * elapsed / args.steps
-    value = ws * diagrams * args.steps / elapsed
+    value = replica_value(ws, diagrams * args.steps, elapsed)
     tuned = api.tune_report()
 
     res_main = out.cpu().numpy()
@@ -427,7 +441,7 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         te = allmax(ws, e0.elapsed_time(e1) / 1e3) / K
-        e2e = {"value": ws * diagrams / te, "unit": "diagrams/s",
+        e2e = {"value": replica_value(ws, diagrams, te), "unit": "diagrams/s",
                "h2d_bytes_per_step": int(h_tau.numel() * 16 + h_phi.numel() * 16),
                "d2h_bytes_per_step": int(out.numel() * 16), "ms_per_step": 1e3 * te,
                "pipelining": "inputs of step i+1 copied on a second stream while step i computes", "steps": K,
