@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time extent (default: the workload's; a smaller value "
                                                               "gives a small case of the same kernels, e.g. for ncu)")
     ap.add_argument("--nev", type=int, default=NEV)
-    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu"],
+    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu", "elementals"],
                     help="rho: the headline rho two-point (Nev=100, Lt=64); rho_small: Nev=32, Lt=16 FP64; "
                          "pipi: pi pi I=0 diagram set, 19 momentum pairs; mixed: rho-pipi / sigma-pipi / "
                          "sigma loops at Nev=128, Lt=48, 27 momenta; adjoint: profile objective and gradient; "
@@ -846,8 +846,53 @@ def run_legacy_gpu(args):
     print(json.dumps(line))
 
 
+def run_elementals(args):
+    """Elementals from Laplacian eigenvectors, as the reference drivers build them
+    before calculateRho (tests/compute_rho.cpp:116-223): a 16^3 x Lt=64 lattice,
+    Nev=100, the 7 momenta |p|^2 <= 1, all five rho operators (plain, smeared,
+    three commutators with covariant derivatives).  Seeded synthetic eigenvectors
+    (orthonormal per time slice) and SU(3) links stand in for the lattice files."""
+    import numpy as np
+    import torch
+    from contractions_code_scattering_gb300 import api, synth
+    from oracle import elementals as E
+    api.device_init(0)
+    nt, nev, L = args.nt or 64, 100, 16
+    moms = synth.momenta(MAXP2)
+    V = synth.make_eigvecs(nt, nev, L, L, L, seed=SEED, backend="torch")
+    U = synth.make_links(nt, L, L, L, seed=SEED + 1, backend="torch")
+    out = torch.empty((len(moms), 5, nt, nev, nev), dtype=torch.complex128, device="cuda")
+    step = lambda: api.elementals(V, moms, links=U, out=out)
+    t, launches, kern = _timed(step, args.steps, args.warmup)
+    K = 3 * L ** 3
+    # 10 products X^dag diag(phase) Y of nev x nev over K per (t, p): 8 nev^2 K flops each
+    flops = 10 * 8.0 * nev * nev * K * nt * len(moms)
+    peak = fp64_peak_tflops()
+    achieved = flops / (kern["el_gemm"]["ms"] / 1e3 / args.steps) / 1e12
+    # parity on a sample: t = 0, two momenta, against the numpy restatement; and the
+    # same restatement timed on the host cores (numpy einsum, its own threads)
+    Vh, Uh = V[:1].cpu().numpy(), U[:1].cpu().numpy()
+    sample = [moms[0], moms[1]]
+    t0 = time.perf_counter()
+    ref = E.elementals(Vh, sample, Uh)
+    tcpu = time.perf_counter() - t0
+    got = out[:2, :, :1].cpu().numpy()
+    n_el = len(moms) * 5 * nt
+    line = {"workload": "elementals", "metric": "elementals/s @Nev=100,16^3x64: 7 momenta x 5 operators, FP64",
+            "value": n_el / t, "unit": "elementals/s", "ms_per_step": 1e3 * t, "steps": args.steps,
+            "warmup": args.warmup, "elementals_per_step": n_el, "gpu_launches": launches, "kernels": kern,
+            "roofline": {"kernel": "el_gemm", "bound": "fp64 pipe", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": "measured in bench.py: cuBLAS DGEMM 8192^3",
+                         "algorithmic": "10 products of 8 nev^2 (3 L^3) flops per (t, p)"},
+            "vs_restatement": _errs(got, ref),
+            "cpu_baseline": {"value": 2 * 5 / tcpu, "unit": "elementals/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "t = 0, 2 momenta, 5 operators (numpy restatement)"}}
+    print(json.dumps(line))
+
+
 WORKLOADS = {"rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint,
-             "legacy_gpu": run_legacy_gpu}
+             "legacy_gpu": run_legacy_gpu, "elementals": run_elementals}
 
 
 if __name__ == "__main__":

@@ -453,3 +453,29 @@ def zgemm_tasks(x, y, tasks, weights=None, a_dagger=False, b_dagger=False, engin
         z.c = out.data_ptr() + c * stride
     check(lib().ctr_zgemm_tasks(_engine(engine), n, len(tasks), ctypes.cast(arr, ctypes.c_void_p), _stream(stream)))
     return out
+
+
+def elementals(evec, moms, links=None, nops=None, out=None, stream=None):
+    """Momentum elementals from Laplacian eigenvectors (include/ctr.h:
+    ctr_elementals; the drivers' loops, tests/compute_rho.cpp:116-223).
+    evec [nt, nev, nz, ny, nx, 3] and links [nt, nz, ny, nx, 3, 3, 3] are device
+    complex128; moms is a list of integer 3-momenta.  Returns
+    [nmom, nops, nt, nev, nev] (nops = 5 with links, else 1)."""
+    import torch
+    nt, nev, nz, ny, nx, nc = evec.shape
+    if nc != 3:
+        raise ValueError("evec must be [nt, nev, nz, ny, nx, 3]")
+    _dev(evec, "evec")
+    if nops is None:
+        nops = 5 if links is not None else 1
+    lp = None
+    if links is not None:
+        if tuple(links.shape) != (nt, nz, ny, nx, 3, 3, 3):
+            raise ValueError("links must be [nt, nz, ny, nx, 3, 3, 3]")
+        lp = _dev(links, "links")
+    m = np.ascontiguousarray(np.asarray(moms, dtype=np.int32).reshape(-1, 3))
+    if out is None:
+        out = torch.empty((len(m), nops, nt, nev, nev), dtype=torch.complex128, device=evec.device)
+    check(lib().ctr_elementals(nev, nt, nx, ny, nz, _dev(evec, "evec"), lp, len(m), _np_ptr(m), nops,
+                               _dev(out, "out"), _stream(stream)))
+    return out

@@ -153,3 +153,49 @@ def make_phi_momenta_torch(nt, nev, moms, seed, device="cuda"):
 def mom_stack(phis, order):
     """Stack {key: [Nt,N,N]} into [Nt, len(order), N, N] (the op/momentum axis second)."""
     return np.ascontiguousarray(np.stack([phis[k] for k in order], axis=1))
+
+
+# ------------------------------------------------ eigenvectors and gauge links
+# The elemental construction (tests/compute_rho.cpp:116-201) reads Laplacian
+# eigenvectors and a smeared gauge configuration from lattice files; these stand
+# in for them: per time slice, nev orthonormal colour-vector fields (the Q factor
+# of a complex Gaussian matrix over sites x colours) and SU(3) links (the
+# phase-fixed Q factor of a complex Gaussian 3 x 3 matrix, divided by a cube
+# root of its determinant).  Layouts: evec [nt, nev, nz, ny, nx, 3] (colour
+# fastest), links [nt, nz, ny, nx, 3 directions, 3, 3].
+
+def make_eigvecs(nt, nev, nx, ny, nz, seed, backend="numpy", device="cuda"):
+    """Built on the host (LAPACK QR) for both backends, so the seeded data are
+    the same; backend "torch" returns them on the device."""
+    K = 3 * nx * ny * nz
+    rng = np.random.default_rng(seed)
+    out = np.empty((nt, nev, nz, ny, nx, 3), np.complex128)
+    for t in range(nt):
+        G = rng.normal(size=(K, nev)) + 1j * rng.normal(size=(K, nev))
+        Q, _ = np.linalg.qr(G)
+        out[t] = Q.T.reshape(nev, nz, ny, nx, 3)
+    if backend == "torch":
+        import torch
+        return torch.from_numpy(out).to(device)
+    return out
+
+
+def _su3(G):
+    """SU(3) matrices from complex Gaussian [..., 3, 3]."""
+    Q, R = np.linalg.qr(G)
+    d = np.diagonal(R, axis1=-2, axis2=-1)
+    Q = Q * (d / abs(d))[..., None, :]
+    det = np.linalg.det(Q)
+    return Q / (det ** (1.0 / 3.0))[..., None, None]
+
+
+def make_links(nt, nx, ny, nz, seed, backend="numpy", device="cuda"):
+    """Built on the host for both backends (as make_eigvecs)."""
+    shape = (nt, nz, ny, nx, 3, 3, 3)
+    rng = np.random.default_rng(seed)
+    G = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    out = np.ascontiguousarray(_su3(G))
+    if backend == "torch":
+        import torch
+        return torch.from_numpy(out).to(device)
+    return out

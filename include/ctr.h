@@ -188,6 +188,30 @@ int ctr_rho_noalloc(int nev, int nt, int tf, const double* prop_row, const doubl
 /* Size in bytes of ctr_rho_noalloc's fixed device scratch array. */
 size_t ctr_rho_noalloc_scratch_bytes(void);
 
+/* Momentum elementals from Laplacian eigenvectors, as the reference drivers build
+ * them before calling calculate* (tests/compute_rho.cpp:116-223; the same loops in
+ * tests/compute_{rhopi,pipi_I0,pipi_I1,sigma,sigmapi}.cpp), for every time slice t
+ * and momentum p, FP64:
+ *   op 0: <v_r| e^{-ip.x} |v_c>                                   (plain)
+ *   op 1: sum_j <D_j v_r| e^{-ip.x} |D_j v_c>                     (smeared)
+ *   op 2+j: <v_r| e^{-ip.x} |D_j v_c> - <D_j v_r| e^{-ip.x} |v_c>  (j = x, y, z)
+ * with <a|b> summed over the sites and colours of the slice, the phase
+ * e^{-i 2 pi (x p_x/nx + y p_y/ny + z p_z/nz)}, and the covariant derivative
+ * D_j v(x) = U_j(x) v(x + j) - U_j(x - j)^dag v(x - j), periodic.  (The reference
+ * takes the derivative from the gwu-qcd library, which it does not ship.)
+ * evec  : device [nt][nev][nz][ny][nx][3] complex128, eigenvector c of slice t
+ *         (site x + nx (y + ny z), colour fastest)
+ * links : device [nt][nz][ny][nx][3][3][3] complex128, U_j(x) of slice t
+ *         (direction j, row, column); may be NULL when nops == 1
+ * mom   : host [nmom][3] integer momenta
+ * nops  : 1 (op 0 only) or 5
+ * phi   : device [nmom][nops][nt][nev][nev] complex128: per momentum the layout
+ *         the drivers pass to calculateRho ([op][t][r][c])
+ * Scratch: the phase table and, for nops == 5, the derivatives of every
+ * eigenvector (3 x the size of evec). */
+int ctr_elementals(int nev, int nt, int nx, int ny, int nz, const double* evec, const double* links, int nmom,
+                   const int* mom, int nops, double* phi, void* stream);
+
 /* ------------------------------------------------ distillation-profile adjoint
  * The elementals enter the contractions as diag(f) Phi diag(f) for a real
  * per-eigenvector profile f (no counterpart in the reference, whose
