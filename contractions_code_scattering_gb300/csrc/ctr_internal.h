@@ -30,7 +30,8 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
     if (_rc != CTR_OK) return _rc; \
   } while (0)
 
-// Counts (and, when enabled, times with CUDA events) one kernel launch.
+// Counts (and, when enabled, times with CUDA events) one kernel launch, and
+// marks it with an NVTX range of the kernel's name for timeline profilers.
 class TimedLaunch {
  public:
   TimedLaunch(cudaStream_t s, const char* name);
@@ -39,6 +40,7 @@ class TimedLaunch {
  private:
   cudaStream_t stream_;
   int idx_;
+  bool ranged_ = false;
 };
 
 // --------------------------------------------------------------- tables

@@ -4,6 +4,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ctr_internal.h"
 
 namespace ctr {
@@ -336,6 +338,8 @@ TimedLaunch::TimedLaunch(cudaStream_t s, const char* name) : stream_(s), idx_(-1
     }
     return;
   }
+  nvtxRangePushA(name);
+  ranged_ = true;
   std::lock_guard<std::mutex> lk(g_tm_mutex);
   count_launch(name);
   if (!g_timing) return;
@@ -351,9 +355,11 @@ TimedLaunch::TimedLaunch(cudaStream_t s, const char* name) : stream_(s), idx_(-1
 }
 
 TimedLaunch::~TimedLaunch() {
-  if (idx_ < 0) return;
-  std::lock_guard<std::mutex> lk(g_tm_mutex);
-  cudaEventRecord(g_pool[idx_ + 1], stream_);
+  if (idx_ >= 0) {
+    std::lock_guard<std::mutex> lk(g_tm_mutex);
+    cudaEventRecord(g_pool[idx_ + 1], stream_);
+  }
+  if (ranged_) nvtxRangePop();
 }
 
 }  // namespace ctr
