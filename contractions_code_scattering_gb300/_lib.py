@@ -62,6 +62,7 @@ def lib(build_if_missing=True):
     L.ctr_timing_report.argtypes = [ctypes.c_char_p, i]
     L.ctr_zgemm_tasks.argtypes = [i, i, i, vp, vp]
     L.ctr_elementals.argtypes = [i, i, i, i, i, vp, vp, i, vp, i, vp, vp]
+    L.ctr_wait_probe.argtypes = [i, vp]
     L.ctr_split_set_refine.argtypes = [d]
     L.ctr_split_refined.restype = ctypes.c_longlong
     L.ctr_apply_profile.argtypes = [i, ctypes.c_longlong, vp, vp, vp, vp]

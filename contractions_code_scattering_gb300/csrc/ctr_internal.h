@@ -111,6 +111,8 @@ extern long long g_refined_last;
 
 // Reads (and clears) the device-side error flag of the split engine; syncs the stream.
 int split_error_check(cudaStream_t s);
+// Runs a bounded device wait that times out after timeout_ms and reports it (ctr_wait_probe).
+int wait_probe(int timeout_ms, cudaStream_t s);
 int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,
                         cudaStream_t stream);
 // A stage of FP64-engine GEMM tasks (struct ZTask, kernels.h) on the split

@@ -242,6 +242,12 @@ int ctr_source_average(int nt, int ncorr, const double* corr, double scale, doub
   return ctr::launch_source_average(nt, ncorr, (const double2*)corr, scale, (double2*)avg, (cudaStream_t)stream);
 }
 
+int ctr_wait_probe(int timeout_ms, void* stream) {
+  CTR_NO_CAPTURE("ctr_wait_probe");
+  if (timeout_ms < 1 || timeout_ms > 1000) return ctr::fail(CTR_ERR_ARG, "ctr_wait_probe: timeout %d ms not in [1, 1000]", timeout_ms);
+  return ctr::wait_probe(timeout_ms, (cudaStream_t)stream);
+}
+
 int ctr_sync(void* stream) {
   CTR_NO_CAPTURE("ctr_sync");
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);

@@ -56,13 +56,21 @@ int prepare_for_capture() {
   return split_kernels_prepare();
 }
 
+int wait_probe(int timeout_ms, cudaStream_t s) {
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  CTR_TRY(launch_wait_probe((unsigned long long)timeout_ms * 1000000ull, d_err, s));
+  return split_error_check(s);
+}
+
 int split_error_check(cudaStream_t s) {
   if (!g_err_dev) return CTR_OK;
   int h = 0;
   CTR_TRY(download(&h, g_err_dev, sizeof(int), s));
   if (h != 0) {
     CTR_CUDA(cudaMemsetAsync(g_err_dev, 0, sizeof(int), s));
-    return fail(CTR_ERR_TIMEOUT, "split GEMM pipeline wait timed out (stage %d)", h);
+    // 1-5: the split GEMM's pipeline, 6-7: the grouped traces, 9: ctr_wait_probe
+    return fail(CTR_ERR_TIMEOUT, "a bounded device wait timed out (code %d)", h);
   }
   return CTR_OK;
 }

@@ -1399,6 +1399,17 @@ __global__ void __launch_bounds__(TPB) trace_quads_kernel(const TraceGroup* __re
   }
 }
 
+// Failure detection check: one thread waits, through the same bounded wait as
+// the GEMM pipeline, on an mbarrier that nothing arrives at; the wait gives up
+// after timeout_ns and records error code 9.  Nothing hangs: the kernel returns.
+__global__ void wait_probe_kernel(unsigned long long timeout_ns, int* __restrict__ err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  if (!mbar_wait(&bar, 0, timeout_ns)) atomicExch(err, 9);
+}
+
 // --------------------------------------------------------------- launchers
 // Dynamic shared-memory limits are raised once per kernel (before any graph
 // capture, through split_kernels_prepare, or at the first launch).
@@ -1505,6 +1516,13 @@ int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, smem, g_attr_tr));
   TimedLaunch tl(s, "slice_task_right");
   slice_task_right_kernel<CfgHP><<<njobs * ntiles * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles, bexp);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_wait_probe(unsigned long long timeout_ns, int* d_err, cudaStream_t s) {
+  TimedLaunch tl(s, "wait_probe");
+  wait_probe_kernel<<<1, 32, 0, s>>>(timeout_ns, d_err);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

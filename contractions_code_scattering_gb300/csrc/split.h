@@ -177,6 +177,9 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s,
                        int form = 0);
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
+// A bounded wait that runs out (timeout_ns) on an mbarrier nothing arrives at,
+// recording error code 9 in *d_err (the failure-detection check).
+int launch_wait_probe(unsigned long long timeout_ns, int* d_err, cudaStream_t s);
 // Raises the shared-memory limits of the split kernels and caches the SM count.
 int split_kernels_prepare();
 // Closing traces over npair pairs: products of pair q at a_base[q] / b_base[q]

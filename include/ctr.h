@@ -164,6 +164,15 @@ typedef struct {
 } ctr_ztask;
 int ctr_zgemm_tasks(int engine, int nev, int ntask, const ctr_ztask* tasks /* host */, void* stream);
 
+/* Failure detection check (no counterpart in the reference, whose errors end
+ * the process): every device-side wait of the library is bounded; when one
+ * runs out, the kernel records an error code, finishes without hanging, and
+ * the next synchronising call returns CTR_ERR_TIMEOUT while the context stays
+ * usable.  This runs one such wait, on an mbarrier that nothing arrives at,
+ * with a limit of timeout_ms (1..1000), and returns what a caller would see:
+ * CTR_ERR_TIMEOUT.  Not recordable in a CUDA graph. */
+int ctr_wait_probe(int timeout_ms, void* stream);
+
 /* Diagnostics of the split engine: for one product x*y (nev x nev, device),
  * write the raw FP32 tensor-core accumulators before recombination, as
  * levels[8][nev][128] (Re levels 0, 1, 2, >=3, then Im; element (i,j) at

@@ -268,3 +268,26 @@ def test_fp64_gemm_tile_variants(cuda, n):
             assert np.abs(got - ref).max() / np.abs(ref).max() <= 1e-12, v
     finally:
         api.tune_force("zgemm_f64.tile", -1)
+
+
+@pytest.mark.gpu
+def test_bounded_wait_runs_out_and_the_context_stays_usable(cuda):
+    """Failure detection without a GPU fault: a device wait on an mbarrier that
+    nothing arrives at gives up after 50 ms, the call reports CTR_ERR_TIMEOUT,
+    and the next contraction on the same context is correct."""
+    import ctypes
+    import time
+    from contractions_code_scattering_gb300._lib import lib
+    s = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    rc = lib().ctr_wait_probe(50, ctypes.c_void_p(s.cuda_stream))
+    dt = time.perf_counter() - t0
+    assert rc == 5  # CTR_ERR_TIMEOUT
+    assert b"timed out" in lib().ctr_last_error()
+    assert 0.04 <= dt < 5.0
+    assert lib().ctr_wait_probe(0, ctypes.c_void_p(s.cuda_stream)) != 0  # limits are checked
+    nt, n = 3, 16
+    prop, mom5 = _rho_inputs(nt, n, seed=505)
+    ref = O.rho(prop, mom5)
+    got = api.run_contract_rho(torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda), engine="split")
+    assert np.abs(got.cpu().numpy() - ref).max() / np.abs(ref).max() <= 1e-9
