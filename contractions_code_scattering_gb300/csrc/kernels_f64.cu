@@ -486,15 +486,16 @@ int launch_zgemm_f64(const ZTask* d_tasks, int ntask, int N, cudaStream_t s, con
   for (int t = 0; exact && t < ntask; t++)
     for (int q = 0; q < h_tasks[t].nterm; q++)
       if (!exact_weight(h_tasks[t].wre[q], h_tasks[t].wim[q])) exact = false;
-  // default: a DMMA form where it covers Nev > 64, else the DFMA edge that pads
-  // Nev least (ties to the larger tile)
+  // default: the DFMA edge that pads Nev least (ties to the larger tile).  With
+  // the complex multiply-accumulate as four FMAs it beat the DMMA forms at every
+  // Nev measured on GB300 (Nev = 100: 89 ms against 117 ms per batch of the rho
+  // workload; Nev = 128: 112 ms against 127 ms); the DMMA forms stay candidates.
   int dflt = 0;
   long long best = -1;
   for (int v = 0; v < 3; v++) {
     const long long T = kTileEdge[v], cover = ((N + T - 1) / T) * T;
     if (best < 0 || cover < best) best = cover, dflt = v;
   }
-  if (exact && N > 64) dflt = dmma_fits(3, N) ? 3 : (dmma_fits(4, N) ? 4 : dflt);
   const int ncand = exact && N > 64 ? kTileVariants : 3;
   int v = dflt;
   CTR_TRY(tune_resolve("zgemm_f64.tile", "nev=" + std::to_string(N) + (exact ? ",exact" : ""), ncand, dflt, s,
