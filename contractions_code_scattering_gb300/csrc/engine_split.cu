@@ -75,6 +75,20 @@ int split_error_check(cudaStream_t s) {
   return CTR_OK;
 }
 
+// Scratch budget of a two-sided batch: 16 GB, or an eighth of the device's
+// memory where that is less (the tuner found the largest batch the fastest at
+// Nev = 100).  The memory size is queried once, outside any stream capture; a
+// call recorded before the first query uses 6 GB.  The batch size does not
+// change any pair's result.
+static size_t batch_budget() {
+  static size_t cached = 0;
+  if (cached == 0 && !capturing()) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) cached = std::min<size_t>((size_t)16 << 30, total_b / 8);
+  }
+  return cached ? cached : ((size_t)6 << 30);
+}
+
 // Slice Nt elementals stacked [op list] as left and right operands.
 struct PhiSlices {
   int nblk = 0, mtiles = 0, ntiles = 0;
@@ -181,7 +195,7 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
   const size_t b_b = align256((size_t)ntT * SPLIT_N * ldB * sizeof(float4));
   const size_t per_pair = tl_b + tr_b + tle_b + tre_b + a_b + b_b;
   const int npairs_total = (tf_end - tf_begin) * Nt;
-  const size_t budget = (size_t)6 << 30;
+  const size_t budget = batch_budget();
   int batch = (int)std::max<size_t>(1, budget / per_pair);
   batch = std::min(batch, npairs_total);
 
