@@ -547,7 +547,7 @@ def roofline(engine, report, steps, nt, nev, nmom):
     return {"kernel": "split_gemm", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at Nt=8, scaled "
-                              "by pairs per launch (profiles/split_gemm_rho_nt8.md)",
+                              "by pairs per launch (the split_gemm rho Nt=8 ncu summary under profiles/)",
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
             "fp64_equivalent_tflops": achieved / 15 / 1.12,
             "algorithmic": "15 bf16 slice-pair products x 8*Nev^3 flops (K padded 100->112) per block product"}
