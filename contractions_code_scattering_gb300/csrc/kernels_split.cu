@@ -78,24 +78,38 @@ __host__ __device__ constexpr uint64_t digit_offset(int nslice) {
 template <int NS = SPLIT_NSLICE>
 __device__ __forceinline__ uint64_t round_fixed(uint64_t U) { return U + digit_offset(NS); }
 
-__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t W, int s, bool neg) {
-  const int d = s == 0 ? (int)(W >> 55) : (int)((W >> slice_shift(s)) & 511u) - 256;
-  const float v = (float)d * __int_as_float((127 + slice_shift(s) - 63) << 23);  // d * 2^{-8-9s}, exact
-  return __float2bfloat16_rn(neg ? -v : v);
+// FP32 bits of digit s of W, d_s 2^{-8-9s} with its sign flipped when neg, built
+// without an integer conversion: the 9-bit field f of the digit becomes the top
+// of the significand of X = 2^q (1 + f/512), q = 1 - 9s, and X - 2^q (1 + o/512)
+// = (f - o) 2^{q-9} exactly (the operands are within a factor 2), with o = 0
+// for s = 0 (d_0 = f) and o = 256 otherwise (d_s = f - 256).  At most 9
+// significant bits, so the value is exact in BF16 and its BF16 encoding is the
+// high half of these bits.  A zero digit gives +0 (-0 when neg).
+__device__ __forceinline__ uint32_t slice_bits(uint64_t W, int s, bool neg) {
+  const int p = slice_shift(s);
+  const uint32_t w = p >= 14 ? (uint32_t)(W >> (p - 14)) : (uint32_t)W << (14 - p);
+  const uint32_t eb = (uint32_t)(128 - 9 * s) << 23;
+  const float v = __uint_as_float((w & (511u << 14)) | eb) - __uint_as_float(eb | (s ? (1u << 22) : 0u));
+  return __float_as_uint(v) ^ (neg ? 0x80000000u : 0u);
 }
 
-// The value of slice_bf16 before its rounding to BF16 (exact in BF16).
-__device__ __forceinline__ float slice_f32(uint64_t W, int s, bool neg) {
-  const int d = s == 0 ? (int)(W >> 55) : (int)((W >> slice_shift(s)) & 511u) - 256;
-  const float v = (float)d * __int_as_float((127 + slice_shift(s) - 63) << 23);
-  return neg ? -v : v;
+__device__ __forceinline__ __nv_bfloat16 slice_bf16(uint64_t W, int s, bool neg) {
+  return __ushort_as_bfloat16((unsigned short)(slice_bits(W, s, neg) >> 16));
 }
+
+// The value of slice_bf16 before its conversion to BF16 (exact in BF16).
+__device__ __forceinline__ float slice_f32(uint64_t W, int s, bool neg) { return __uint_as_float(slice_bits(W, s, neg)); }
 
 // Two slices of adjacent k as one packed BF16 pair (k in the low half).
 __device__ __forceinline__ uint32_t slice_pair(uint64_t W0, bool n0, uint64_t W1, bool n1, int s) {
-  const __nv_bfloat162 p = __floats2bfloat162_rn(slice_f32(W0, s, n0), slice_f32(W1, s, n1));
-  return *(const uint32_t*)&p;
+  return __byte_perm(slice_bits(W0, s, n0), slice_bits(W1, s, n1), 0x7632);
 }
+
+// BF16 bits of -x for BF16 bits x (one value, or a packed pair).
+__device__ __forceinline__ __nv_bfloat16 bf16_neg(__nv_bfloat16 x) {
+  return __ushort_as_bfloat16((unsigned short)(__bfloat16_as_ushort(x) ^ 0x8000u));
+}
+constexpr uint32_t BF16X2_SIGNS = 0x80008000u;
 
 // Byte offset of element (row, k) of one (slice, plane) sub-tile inside a
 // K-chunk stage: core matrices of 8 rows x 8 elements, K-adjacent at +128 B,
@@ -228,9 +242,10 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
 #pragma unroll
       for (int s = 0; s < SPLIT_NSLICE; s++) {
         // planes -im, re, im (packed complex MMAs)
-        *(__nv_bfloat16*)(stage + (s * 3 + 0) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, !ni);
+        const __nv_bfloat16 bi = slice_bf16(Ui, s, ni);
+        *(__nv_bfloat16*)(stage + (s * 3 + 0) * SPLIT_B_SUB + off) = bf16_neg(bi);
         *(__nv_bfloat16*)(stage + (s * 3 + 1) * SPLIT_B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 3 + 2) * SPLIT_B_SUB + off) = slice_bf16(Ui, s, ni);
+        *(__nv_bfloat16*)(stage + (s * 3 + 2) * SPLIT_B_SUB + off) = bi;
       }
     }
     __syncthreads();
@@ -384,9 +399,10 @@ __global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRigh
 #pragma unroll
     for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
       // planes -im, re, im (packed complex MMAs)
-      *(uint32_t*)(stage + (sl * 3 + 0) * 1024 + off) = slice_pair(Ui0, !ni0, Ui1, !ni1, sl);
+      const uint32_t pi = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+      *(uint32_t*)(stage + (sl * 3 + 0) * 1024 + off) = pi ^ BF16X2_SIGNS;
       *(uint32_t*)(stage + (sl * 3 + 1) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
-      *(uint32_t*)(stage + (sl * 3 + 2) * 1024 + off) = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+      *(uint32_t*)(stage + (sl * 3 + 2) * 1024 + off) = pi;
     }
     __syncthreads();
     uint8_t* d = dst_tile + (size_t)kc * SPLIT_B_STAGE;
@@ -592,9 +608,10 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
 #pragma unroll
     for (int s = 0; s < C::NS; s++) {
       if (C::PACK) {
-        *(__nv_bfloat16*)(stage + (s * 3 + 0) * C::B_SUB + off) = slice_bf16(Ui, s, !ni);
+        const __nv_bfloat16 bi = slice_bf16(Ui, s, ni);
+        *(__nv_bfloat16*)(stage + (s * 3 + 0) * C::B_SUB + off) = bf16_neg(bi);
         *(__nv_bfloat16*)(stage + (s * 3 + 1) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 3 + 2) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
+        *(__nv_bfloat16*)(stage + (s * 3 + 2) * C::B_SUB + off) = bi;
       } else {
         *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
         *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
