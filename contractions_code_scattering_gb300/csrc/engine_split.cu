@@ -309,13 +309,13 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
                           {gb.data(), gb.size() * sizeof(SplitGemmInst)}},
                          d4, stream));
     void *d_lj = d4[0], *d_rj = d4[1], *d_ga = d4[2], *d_gb = d4[3], *d_tt;
-    // slicer form (autotuned; both write the same bytes, so candidates re-run)
+    // slicer form (autotuned; all three write the same bytes, so candidates re-run)
     auto slice_tau = [&](int form) {
       CTR_TRY(launch_slice_left((const SliceLeftJob*)d_lj, np, N, nchunk, mtT, stream, form));
       return launch_slice_right((const SliceRightJob*)d_rj, np, N, nchunk, ntT, stream, form);
     };
-    int sform = 1;
-    CTR_TRY(tune_resolve("slice_tau", shape, 2, 1, stream, slice_tau, &sform));
+    int sform = 2;
+    CTR_TRY(tune_resolve("slice_tau", shape, 3, 2, stream, slice_tau, &sform));
     CTR_TRY(slice_tau(sform));
     // tile walk of each GEMM (autotuned; idempotent, so candidates re-run on the same data)
     SplitGemmBatch GA{(const SplitGemmInst*)d_ga, mtT, F.ntiles, nchunk, ncd * N, nL * N, ldA};

@@ -262,7 +262,11 @@ __global__ void __launch_bounds__(256) slice_right_kernel(const SliceRightJob* _
 // flight together), takes the scale exponents from there and slices every K
 // chunk from there, so the operand is read from memory once.  A quarter covers
 // 4 of the core-matrix row groups of each (slice, plane) sub-tile, i.e. 1 KB
-// contiguous in each.
+// contiguous in each.  DIRECT = false stages each K chunk's output in shared
+// memory and copies it out in 16-byte pieces; DIRECT = true stores every
+// thread's packed BF16 pairs straight to memory (a warp's store covers whole
+// 32-byte sectors: 4 rows x 16 contiguous bytes at two 128-byte-apart runs)
+// and needs no barrier after the exponents.
 constexpr int SLQ = 32;  // rows / columns of a quarter
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
@@ -274,12 +278,13 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // staged output chunk (planes x 1 KB) and the exponents
 inline size_t slice_staged_smem(int nev, int planes) { return (size_t)SLQ * nev * 16 + (size_t)planes * 1024 + 256; }
 
+template <bool DIRECT>
 __global__ void __launch_bounds__(256) slice_left_staged_kernel(const SliceLeftJob* __restrict__ jobs, int nev,
                                                                 int nchunk, int mtiles) {
   extern __shared__ __align__(128) uint8_t sm[];
   double2* data = (double2*)sm;  // [SLQ][nev]
   uint8_t* stage = sm + (size_t)SLQ * nev * 16;
-  int* sexp = (int*)(stage + SPLIT_NSLICE * 2 * 1024);
+  int* sexp = (int*)(stage + (DIRECT ? 0 : SPLIT_NSLICE * 2 * 1024));
   const int quarters = SPLIT_M / SLQ;
   const int job = blockIdx.x / (mtiles * quarters), rem = blockIdx.x - job * mtiles * quarters;
   const int mt = rem / quarters, qt = rem - mt * quarters;
@@ -324,27 +329,37 @@ __global__ void __launch_bounds__(256) slice_left_staged_kernel(const SliceLeftJ
     bool nr0, ni0, nr1, ni1;
     const uint64_t Ur0 = round_fixed(f64_fixed(v0.x, E, nr0)), Ui0 = round_fixed(f64_fixed(v0.y, E, ni0));
     const uint64_t Ur1 = round_fixed(f64_fixed(v1.x, E, nr1)), Ui1 = round_fixed(f64_fixed(v1.y, E, ni1));
+    if constexpr (DIRECT) {
+      uint8_t* d = dst_tile + (size_t)kc * SPLIT_A_STAGE + off;
 #pragma unroll
-    for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
-      *(uint32_t*)(stage + (sl * 2 + 0) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
-      *(uint32_t*)(stage + (sl * 2 + 1) * 1024 + off) = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+        *(uint32_t*)(d + (size_t)(sl * 2 + 0) * SPLIT_A_SUB) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
+        *(uint32_t*)(d + (size_t)(sl * 2 + 1) * SPLIT_A_SUB) = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+      }
+    } else {
+#pragma unroll
+      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+        *(uint32_t*)(stage + (sl * 2 + 0) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
+        *(uint32_t*)(stage + (sl * 2 + 1) * 1024 + off) = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+      }
+      __syncthreads();
+      uint8_t* d = dst_tile + (size_t)kc * SPLIT_A_STAGE;
+      for (int i = threadIdx.x; i < SPLIT_NSLICE * 2 * 64; i += 256) {
+        const int piece = i >> 6, w = i & 63;
+        ((int4*)(d + (size_t)piece * SPLIT_A_SUB))[w] = ((const int4*)(stage + piece * 1024))[w];
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    uint8_t* d = dst_tile + (size_t)kc * SPLIT_A_STAGE;
-    for (int i = threadIdx.x; i < SPLIT_NSLICE * 2 * 64; i += 256) {
-      const int piece = i >> 6, w = i & 63;
-      ((int4*)(d + (size_t)piece * SPLIT_A_SUB))[w] = ((const int4*)(stage + piece * 1024))[w];
-    }
-    __syncthreads();
   }
 }
 
+template <bool DIRECT>
 __global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRightJob* __restrict__ jobs, int nev,
                                                                  int nchunk, int ntiles) {
   extern __shared__ __align__(128) uint8_t sm[];
   double2* data = (double2*)sm;  // [nev][SLQ]
   uint8_t* stage = sm + (size_t)SLQ * nev * 16;
-  int* sexp = (int*)(stage + SPLIT_NSLICE * 3 * 1024);
+  int* sexp = (int*)(stage + (DIRECT ? 0 : SPLIT_NSLICE * 3 * 1024));
   __shared__ int part[256];
   const int quarters = SPLIT_N / SLQ;
   const int job = blockIdx.x / (ntiles * quarters), rem = blockIdx.x - job * ntiles * quarters;
@@ -386,7 +401,11 @@ __global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRigh
   __syncthreads();
   uint8_t* dst_tile = J.out + (size_t)nt * nchunk * SPLIT_B_STAGE + qt * 1024;
   static_assert(SLQ * SPLIT_K == 2 * 256, "two adjacent k per thread");
-  const int nn = threadIdx.x & 31, kk = (threadIdx.x >> 5) * 2;
+  // 8 consecutive lanes: 8 columns of one k pair (128 contiguous bytes of the
+  // quarter, and 8 core-matrix rows); a warp: 8 columns x 4 k pairs, whose
+  // packed pairs fill 128 contiguous output bytes
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nn = (warp & 3) * 8 + (lane & 7), kk = ((warp >> 2) * 4 + (lane >> 3)) * 2;
   const uint32_t off = core_offset(nn, kk);  // k and k + 1 are adjacent
   const int E = sexp[nn];
   for (int kc = 0; kc < nchunk; kc++) {
@@ -396,21 +415,32 @@ __global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRigh
     bool nr0, ni0, nr1, ni1;
     const uint64_t Ur0 = round_fixed(f64_fixed(v0.x, E, nr0)), Ui0 = round_fixed(f64_fixed(v0.y, E, ni0));
     const uint64_t Ur1 = round_fixed(f64_fixed(v1.x, E, nr1)), Ui1 = round_fixed(f64_fixed(v1.y, E, ni1));
+    if constexpr (DIRECT) {
+      uint8_t* d = dst_tile + (size_t)kc * SPLIT_B_STAGE + off;
 #pragma unroll
-    for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
-      // planes -im, re, im (packed complex MMAs)
-      const uint32_t pi = slice_pair(Ui0, ni0, Ui1, ni1, sl);
-      *(uint32_t*)(stage + (sl * 3 + 0) * 1024 + off) = pi ^ BF16X2_SIGNS;
-      *(uint32_t*)(stage + (sl * 3 + 1) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
-      *(uint32_t*)(stage + (sl * 3 + 2) * 1024 + off) = pi;
+      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+        const uint32_t pi = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+        *(uint32_t*)(d + (size_t)(sl * 3 + 0) * SPLIT_B_SUB) = pi ^ BF16X2_SIGNS;
+        *(uint32_t*)(d + (size_t)(sl * 3 + 1) * SPLIT_B_SUB) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
+        *(uint32_t*)(d + (size_t)(sl * 3 + 2) * SPLIT_B_SUB) = pi;
+      }
+    } else {
+#pragma unroll
+      for (int sl = 0; sl < SPLIT_NSLICE; sl++) {
+        // planes -im, re, im (packed complex MMAs)
+        const uint32_t pi = slice_pair(Ui0, ni0, Ui1, ni1, sl);
+        *(uint32_t*)(stage + (sl * 3 + 0) * 1024 + off) = pi ^ BF16X2_SIGNS;
+        *(uint32_t*)(stage + (sl * 3 + 1) * 1024 + off) = slice_pair(Ur0, nr0, Ur1, nr1, sl);
+        *(uint32_t*)(stage + (sl * 3 + 2) * 1024 + off) = pi;
+      }
+      __syncthreads();
+      uint8_t* d = dst_tile + (size_t)kc * SPLIT_B_STAGE;
+      for (int i = threadIdx.x; i < SPLIT_NSLICE * 3 * 64; i += 256) {
+        const int piece = i >> 6, w = i & 63;
+        ((int4*)(d + (size_t)piece * SPLIT_B_SUB))[w] = ((const int4*)(stage + piece * 1024))[w];
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    uint8_t* d = dst_tile + (size_t)kc * SPLIT_B_STAGE;
-    for (int i = threadIdx.x; i < SPLIT_NSLICE * 3 * 64; i += 256) {
-      const int piece = i >> 6, w = i & 63;
-      ((int4*)(d + (size_t)piece * SPLIT_B_SUB))[w] = ((const int4*)(stage + piece * 1024))[w];
-    }
-    __syncthreads();
   }
 }
 
@@ -1438,7 +1468,7 @@ static int ensure_smem(K kernel, size_t smem, bool& done) {
   }
   return CTR_OK;
 }
-static bool g_attr_sls = false, g_attr_srs = false, g_attr_tg = false;
+static bool g_attr_sls = false, g_attr_srs = false, g_attr_tg = false, g_attr_sld = false, g_attr_srd = false;
 static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr = false, g_attr_std = false,
             g_attr_hp = false;
 static int g_nsm = 0;
@@ -1465,8 +1495,10 @@ int split_kernels_prepare() {
   CTR_TRY(sm_count(&nsm));
   CTR_TRY(ensure_smem(slice_left_kernel, 512 + SPLIT_A_STAGE, g_attr_sl));
   CTR_TRY(ensure_smem(slice_right_kernel, 512 + SPLIT_B_STAGE, g_attr_sr));
-  CTR_TRY(ensure_smem(slice_left_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 2), g_attr_sls));
-  CTR_TRY(ensure_smem(slice_right_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 3), g_attr_srs));
+  CTR_TRY(ensure_smem(slice_left_staged_kernel<false>, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 2), g_attr_sls));
+  CTR_TRY(ensure_smem(slice_right_staged_kernel<false>, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 3), g_attr_srs));
+  CTR_TRY(ensure_smem(slice_left_staged_kernel<true>, slice_staged_smem(SPLIT_MAXK, 0), g_attr_sld));
+  CTR_TRY(ensure_smem(slice_right_staged_kernel<true>, slice_staged_smem(SPLIT_MAXK, 0), g_attr_srd));
   CTR_TRY(ensure_smem(trace_groups_kernel, trace_groups_max_smem(), g_attr_tg));
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
@@ -1478,12 +1510,18 @@ int split_kernels_prepare() {
 int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, cudaStream_t s,
                       int form) {
   if (njobs == 0) return CTR_OK;
-  if (form == 1) {
+  if (form == 1 || form == 2) {
     if (nev > SPLIT_MAXK) return fail(CTR_ERR_ARG, "slicer: Nev %d above %d", nev, SPLIT_MAXK);
-    const size_t smem = slice_staged_smem(nev, SPLIT_NSLICE * 2);
-    CTR_TRY(ensure_smem(slice_left_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 2), g_attr_sls));
+    const int grid = njobs * mtiles * (SPLIT_M / SLQ);
     TimedLaunch tl(s, "slice_left");
-    slice_left_staged_kernel<<<njobs * mtiles * (SPLIT_M / SLQ), 256, smem, s>>>(d_jobs, nev, nchunk, mtiles);
+    if (form == 2) {
+      CTR_TRY(ensure_smem(slice_left_staged_kernel<true>, slice_staged_smem(SPLIT_MAXK, 0), g_attr_sld));
+      slice_left_staged_kernel<true><<<grid, 256, slice_staged_smem(nev, 0), s>>>(d_jobs, nev, nchunk, mtiles);
+    } else {
+      CTR_TRY(ensure_smem(slice_left_staged_kernel<false>, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 2), g_attr_sls));
+      slice_left_staged_kernel<false>
+          <<<grid, 256, slice_staged_smem(nev, SPLIT_NSLICE * 2), s>>>(d_jobs, nev, nchunk, mtiles);
+    }
     CTR_CUDA(cudaGetLastError());
     return CTR_OK;
   }
@@ -1498,12 +1536,18 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s,
                        int form) {
   if (njobs == 0) return CTR_OK;
-  if (form == 1) {
+  if (form == 1 || form == 2) {
     if (nev > SPLIT_MAXK) return fail(CTR_ERR_ARG, "slicer: Nev %d above %d", nev, SPLIT_MAXK);
-    const size_t smem = slice_staged_smem(nev, SPLIT_NSLICE * 3);
-    CTR_TRY(ensure_smem(slice_right_staged_kernel, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 3), g_attr_srs));
+    const int grid = njobs * ntiles * (SPLIT_N / SLQ);
     TimedLaunch tl(s, "slice_right");
-    slice_right_staged_kernel<<<njobs * ntiles * (SPLIT_N / SLQ), 256, smem, s>>>(d_jobs, nev, nchunk, ntiles);
+    if (form == 2) {
+      CTR_TRY(ensure_smem(slice_right_staged_kernel<true>, slice_staged_smem(SPLIT_MAXK, 0), g_attr_srd));
+      slice_right_staged_kernel<true><<<grid, 256, slice_staged_smem(nev, 0), s>>>(d_jobs, nev, nchunk, ntiles);
+    } else {
+      CTR_TRY(ensure_smem(slice_right_staged_kernel<false>, slice_staged_smem(SPLIT_MAXK, SPLIT_NSLICE * 3), g_attr_srs));
+      slice_right_staged_kernel<false>
+          <<<grid, 256, slice_staged_smem(nev, SPLIT_NSLICE * 3), s>>>(d_jobs, nev, nchunk, ntiles);
+    }
     CTR_CUDA(cudaGetLastError());
     return CTR_OK;
   }

@@ -81,19 +81,21 @@ def test_grouped_traces_match_per_trace_kernel(cuda, n):
 @pytest.mark.parametrize("n", [9, 37, 100, 128])
 def test_staged_slicer_writes_the_same_bytes(cuda, n):
     """The staged perambulator slicers (slice_tau form 1: one read of the operand
-    through shared memory) write the same operand bytes as form 0, so the split
-    engine's rho values are bitwise identical."""
+    through shared memory; form 2: the same with direct stores of the digits)
+    write the same operand bytes as form 0, so the split engine's rho values are
+    bitwise identical."""
     nt = 2
     prop, mom5 = _inputs(nt, n, seed=500 + n)
     d_prop, d_mom = torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda)
     got = {}
     try:
-        for form in (0, 1):
+        for form in (0, 1, 2):
             api.tune_force("slice_tau", form)
             got[form] = api.run_contract_rho(d_prop, d_mom, engine="split").cpu().numpy()
     finally:
         api.tune_force("slice_tau", -1)
     assert np.array_equal(got[0], got[1])
+    assert np.array_equal(got[0], got[2])
     _close(got[1], O.rho(prop, mom5), TOL["split"])
 
 
