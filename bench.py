@@ -387,11 +387,19 @@ def main():
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
 
+        # copy-stream events around each step's input copy: how long the copies
+        # take while the previous step computes
+        copy_ev = []
+
         def load(b):
             with torch.cuda.stream(cs):
+                ca, cb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ca.record(cs)
                 buf_tau[b].copy_(h_tau, non_blocking=True)
                 buf_phi[b].copy_(h_phi, non_blocking=True)
                 copied[b].record(cs)
+                cb.record(cs)
+                copy_ev.append((ca, cb))
 
         graphs = None
         if args.graph:
@@ -447,7 +455,8 @@ def main():
                "pipelining": "inputs of step i+1 copied on a second stream while step i computes; step 0's "
                              "tau in 2-row chunks, each row range computed once its rows arrived", "steps": K,
                "graph": bool(args.graph), "bitwise_equal_to_value_step": e2e_same,
-               "h2d_tau_alone_ms": 1e3 * h2d_alone, "h2d_tau_alone_gbs": h_tau.numel() * 16 / h2d_alone / 1e9}
+               "h2d_tau_alone_ms": 1e3 * h2d_alone, "h2d_tau_alone_gbs": h_tau.numel() * 16 / h2d_alone / 1e9,
+               "h2d_overlapped_ms": [round(ca.elapsed_time(cb), 1) for ca, cb in copy_ev]}
         if graphs:
             for gb in graphs:
                 gb.close()
