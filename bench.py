@@ -47,11 +47,13 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time extent (default: the workload's; a smaller value "
                                                               "gives a small case of the same kernels, e.g. for ncu)")
     ap.add_argument("--nev", type=int, default=NEV)
-    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu", "elementals"],
+    ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu", "elementals",
+                             "fp64_peak"],
                     help="rho: the headline rho two-point (Nev=100, Lt=64); rho_small: Nev=32, Lt=16 FP64; "
                          "pipi: pi pi I=0 diagram set, 19 momentum pairs; mixed: rho-pipi / sigma-pipi / "
                          "sigma loops at Nev=128, Lt=48, 27 momenta; adjoint: profile objective and gradient; "
-                         "legacy_gpu: the reference's own rho kernel built for sm_103a beside both engines")
+                         "legacy_gpu: the reference's own rho kernel built for sm_103a beside both engines; "
+                         "fp64_peak: cuBLAS DGEMM/ZGEMM rates")
     return ap.parse_args()
 
 
@@ -224,36 +226,73 @@ def rows_to_out(vals, oi, nout):
 
 
 # -------------------------------------------------------------- reference
-def run_reference(args):
-    """--impl reference: the reference's contraction algorithm on the host cores
-    (the oracle's OpenMP FP64 restatement; the reference's own kernels are
-    GPU-only), on a bounded sample of the workload per step."""
-    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
-    if rank != 0:
-        return
+def oracle_rho_rows(nmom, ico=0):
+    """The workload's two-sided rows (op pair `ico`, one elemental per momentum,
+    out index = momentum*3 + polarisation) from the oracle's own restatement of
+    the reference tables (devTools/comb_rho.cpp), so that the reference arm
+    loads nothing of the product library."""
+    import numpy as np
+    from oracle import tables as TB
+    spin, _, coef = TB.rho_tables()
+    rows, cf, oi = [], [], []
+    for p in range(nmom):
+        for r in range(ico * 48, ico * 48 + 48):
+            s = spin[r]
+            rows.append((s[0], s[1], s[2], s[3], p, p))
+            cf.append(coef[r])
+            oi.append(p * 3 + (r % 48) // 16)
+    return np.array(rows, np.int16), np.array(cf, np.float32), np.array(oi, np.int32)
+
+
+def host_sink_row(nt, nev, seed, decay=0.35):
+    """tau(0, t) for t < nt on the host, with the workload's distribution: complex
+    Gaussian N(0,1/Nev) blocks times exp(-decay*t), the t = 0 block
+    gamma5-symmetrised.  [Nt, 4, 4, N, N] complex128."""
     import numpy as np
     from contractions_code_scattering_gb300 import synth
+    rng = np.random.default_rng(seed)
+    sd = np.sqrt(0.5 / nev)
+    row = np.empty((nt, 4, 4, nev, nev), np.complex128)
+    for t in range(nt):
+        x = rng.normal(0.0, sd, (4, 4, nev, nev)) + 1j * rng.normal(0.0, sd, (4, 4, nev, nev))
+        x *= np.exp(-decay * t)
+        if t == 0:
+            x = 0.5 * (x + synth._gamma5_adjoint_np(x))
+        row[t] = x
+    return row
+
+
+def run_reference(args):
+    """--impl reference: the reference's contraction algorithm on the host cores
+    (the oracle's OpenMP FP64 restatement in the reference's chain order; the
+    reference's own kernels are GPU-only).  Each step is one whole t_sink row of
+    the workload: t_sink = 0 against all Nt source times, every one of the 21
+    outputs (7 momenta x 3 polarisations), 16 spin rows each recomputing both of
+    its products, as lib/calculate_rho_core.h does."""
+    ws, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from contractions_code_scattering_gb300 import synth
     from oracle import pyoracle as O
-    moms, rows, coef, oi, nout = workload(args.nt, args.nev)
-    rng_seed = SEED
-    # Only t_sink = 0 is sampled: build tau(0, t) for t < k directly on the host.
-    k = 2
-    nev = args.nev
-    prop = synth.make_prop(k, nev, seed=rng_seed, decay=0.35)
-    phis = synth.make_phi_momenta(k, nev, moms, seed=rng_seed + 1)
-    phi = synth.mom_stack(phis, moms)
+    nt, nev = args.nt or NT, args.nev
+    moms = synth.momenta(MAXP2)
+    rows, coef, oi = oracle_rho_rows(len(moms))
+    nout = 3 * len(moms)
+    row = host_sink_row(nt, nev, SEED)
+    phi = synth.mom_stack(synth.make_phi_momenta(nt, nev, moms, seed=SEED + 1), moms)
     for _ in range(args.warmup):
-        O.twosided_rows(prop[0], phi, rows, coef, 0, 0, 1)
+        O.twosided_rows(row, phi, rows, coef, 0, 0, 1)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.twosided_rows(prop[0], phi, rows, coef, 0, 0, k)
+        O.twosided_rows(row, phi, rows, coef, 0, 0, nt)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * sum(times) / len(times)
-    diag = k * nout
+    diag = nt * nout
     val = diag / (ms / 1e3)
     cores = os.cpu_count() or 1
-    sample = "t_sink=0, t_src=0..%d of the workload, %d rows each (%d diagrams) per step" % (k - 1, len(rows), diag)
+    sample = ("t_sink=0 against all %d t_src, %d outputs x 16 spin rows each (%d diagrams) per step; the work is "
+              "uniform per t_sink row" % (nt, nout, diag))
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": val, "unit": "diagrams/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -924,7 +963,32 @@ def run_elementals(args):
     print(json.dumps(line))
 
 
-WORKLOADS = {"rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint,
+def run_fp64_peak(args):
+    """cuBLAS FP64 reference rates on this GPU (torch.matmul): DGEMM and ZGEMM at
+    4096^3, best of 3 after one untimed call; the FP64 engine's block GEMM is
+    compared with these."""
+    import torch
+    n = 4096
+    res = {}
+    for name, dt, fl in (("dgemm", torch.float64, 2.0), ("zgemm", torch.complex128, 8.0)):
+        a = torch.randn(n, n, dtype=dt, device="cuda")
+        b = torch.randn(n, n, dtype=dt, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        res[name] = {"tflops": fl * n ** 3 / best / 1e12, "ms": 1e3 * best}
+        del a, b
+    print(json.dumps({"workload": "fp64_peak", "n": n, **res}))
+
+
+WORKLOADS = {"fp64_peak": run_fp64_peak, "rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint,
              "legacy_gpu": run_legacy_gpu, "elementals": run_elementals}
 
 

@@ -6,12 +6,17 @@
 // synchronise the device (cudaMalloc/cudaFree can), or hosts whose allocator is
 // locked down.  ctr_rho_noalloc serves them: it computes the same correlators as
 // ctr_rho with the plain FP64 engine for one t_sink row, and its only scratch is
-// the file-scope device array below, of fixed size, reserved when the library
-// is loaded and held by every GPU that loads it until the process exits.  It
-// calls no cudaMalloc, cudaFree, cudaMallocHost or any allocating routine; its
-// host-side task lists live in fixed static arrays.
+// the file-scope device array below, of fixed size.  That array lives in this
+// file's device module: a device reserves it when the module is loaded there,
+// which under CUDA's default lazy module loading happens at the latest in the
+// first call on that device, and keeps it until the process exits.
+//
+// Nothing is allocated and nothing is copied from the host: the call's plan
+// (which blocks to multiply, which traces to take, how rows sum into outputs)
+// is built once, when the library is loaded, into a host struct that every
+// launch passes by value as a kernel parameter; a small kernel then writes the
+// per-source-time task lists into the scratch array.
 #include <cstring>
-#include <mutex>
 
 #include "kernels.h"
 
@@ -26,30 +31,73 @@ __global__ void rowsum_kernel(const double2* __restrict__ rows, int nrows, const
 namespace {
 
 constexpr size_t kScratchBytes = (size_t)32 << 20;  // 32 MiB: 160 products of Nev <= 114
-constexpr int kProducts = 160;                        // 80 source-side + 80 sink-side blocks of rho
+constexpr int kHalf = 80;                             // distinct source-side (and sink-side) blocks of rho
+constexpr int kProducts = 2 * kHalf;
 constexpr int kRows = 768;
 constexpr int kOut = 48;
-constexpr int kMaxDevices = 64;
 
 // The scratch.  In host code this name is only a stand-in for the device
 // symbol; its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// The diagram tables are built when the library is loaded, so that the entry
-// point itself never triggers their (host) construction.
-const Tables& g_tables_at_load = tables();
-
-// Fixed host-side staging of one t_source's task lists.
-struct HostTasks {
-  ZTask gemm[kProducts];
-  TraceTask trace[kRows];
-  int csr[kOut + 1 + kRows];
+// The rho table in the form the task kernel reads: product keys, the products
+// each row multiplies, its coefficient, and the rows of every output.  Output o
+// of the reference's host reduction is rows 16*o .. 16*o+15 (the row index is
+// (op pair*3 + direction)*16 + spin term, lib/contract_kernels_rho.cu:108-116),
+// the same rule ctr_rho uses.  About 11 kB, passed by value to every launch.
+struct Plan {
+  int16_t a_key[kHalf];  // source-side product k: tau(tf,ti)_{cd} Phi_L(ti), key cd*5 + L
+  int16_t b_key[kHalf];  // sink-side product k: Phi_R(tf) tau(tf,ti)_{ab}, key ab*5 + R
+  int16_t row_a[kRows], row_b[kRows];
+  float2 coef[kRows];
+  int32_t csr[kOut + 1 + kRows];
+  int nA, nB;
 };
-HostTasks g_host;
-std::mutex g_host_mutex;
+
+Plan make_plan(int* status) {
+  Plan P;
+  std::memset(&P, 0, sizeof(P));
+  const Tables& T = tables();
+  *status = CTR_OK;
+  for (int r = 0; r < kRows; r++) {
+    const int ka = (T.rho_spin[r][2] * 4 + T.rho_spin[r][3]) * 5 + T.rho_lprp[r][0];
+    const int kb = (T.rho_spin[r][0] * 4 + T.rho_spin[r][1]) * 5 + T.rho_lprp[r][1];
+    int ia = -1, ib = -1;
+    for (int k = 0; k < P.nA; k++)
+      if (P.a_key[k] == ka) ia = k;
+    for (int k = 0; k < P.nB; k++)
+      if (P.b_key[k] == kb) ib = k;
+    if ((ia < 0 && P.nA == kHalf) || (ib < 0 && P.nB == kHalf)) {
+      *status = CTR_ERR_UNSUPPORTED;
+      return P;
+    }
+    if (ia < 0) {
+      ia = P.nA;
+      P.a_key[P.nA++] = (int16_t)ka;
+    }
+    if (ib < 0) {
+      ib = P.nB;
+      P.b_key[P.nB++] = (int16_t)kb;
+    }
+    P.row_a[r] = (int16_t)ia;
+    P.row_b[r] = (int16_t)ib;
+    P.coef[r] = make_float2(T.rho_coef[r][0], T.rho_coef[r][1]);
+  }
+  // CSR of the outputs: counts by output index r / 16, then rows in ascending order
+  int cnt[kOut] = {};
+  for (int r = 0; r < kRows; r++) cnt[r / 16]++;
+  P.csr[0] = 0;
+  for (int o = 0; o < kOut; o++) P.csr[o + 1] = P.csr[o] + cnt[o];
+  int fill[kOut];
+  for (int o = 0; o < kOut; o++) fill[o] = P.csr[o];
+  for (int r = 0; r < kRows; r++) P.csr[kOut + 1 + fill[r / 16]++] = r;
+  return P;
+}
+
+// Built when the library is loaded, so that the entry point itself runs no
+// host-side construction (and no allocation) of its own.
+int g_plan_status = CTR_OK;
+const Plan g_plan = make_plan(&g_plan_status);
 
 // Byte layout of the scratch (all offsets 256-aligned).
 constexpr size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -59,18 +107,52 @@ constexpr size_t kOffCsr = align_up(kOffTrace + sizeof(TraceTask) * kRows);
 constexpr size_t kOffRows = align_up(kOffCsr + sizeof(int) * (kOut + 1 + kRows));
 constexpr size_t kOffProducts = align_up(kOffRows + sizeof(double2) * kRows);
 
-int scratch_address(void** out) {
-  int dev = 0;
-  CTR_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(CTR_ERR_UNSUPPORTED, "device index %d beyond %d", dev, kMaxDevices);
-  std::lock_guard<std::mutex> lk(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    CTR_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_addr[dev] = p;
+// Task lists of one (t_sink, t_source) pair, written into the scratch.
+__global__ void noalloc_tasks_kernel(const Plan P, int N, int tf, int ti, const double2* __restrict__ tau_row,
+                                     const double2* __restrict__ ph, unsigned char* __restrict__ S) {
+  ZTask* gemm = (ZTask*)(S + kOffGemm);
+  TraceTask* trace = (TraceTask*)(S + kOffTrace);
+  int* csr = (int*)(S + kOffCsr);
+  double2* rows = (double2*)(S + kOffRows);
+  double2* prod = (double2*)(S + kOffProducts);
+  const size_t N2 = (size_t)N * N;
+  const double2* tblk = tau_row + (size_t)ti * 16 * N2;
+  for (int i = threadIdx.x; i < P.nA + P.nB; i += blockDim.x) {
+    ZTask z;
+    for (int q = 0; q < 4; q++) {
+      z.A[q] = nullptr;
+      z.B[q] = nullptr;
+      z.wre[q] = 0.f;
+      z.wim[q] = 0.f;
+    }
+    if (i < P.nA) {  // tau_{cd} Phi_L(ti)
+      const int cd = P.a_key[i] / 5, L = P.a_key[i] % 5;
+      z.A[0] = tblk + (size_t)cd * N2;
+      z.B[0] = ph + ((size_t)ti * 5 + L) * N2;
+    } else {  // Phi_R(tf) tau_{ab}
+      const int ab = P.b_key[i - P.nA] / 5, R = P.b_key[i - P.nA] % 5;
+      z.A[0] = ph + ((size_t)tf * 5 + R) * N2;
+      z.B[0] = tblk + (size_t)ab * N2;
+    }
+    z.C = prod + (size_t)i * N2;
+    z.wre[0] = 1.f;
+    z.nterm = 1;
+    z.flags = 0;
+    gemm[i] = z;
   }
-  *out = g_scratch_addr[dev];
-  return CTR_OK;
+  for (int r = threadIdx.x; r < kRows; r += blockDim.x) {
+    TraceTask t;
+    t.X = prod + (size_t)P.row_a[r] * N2;
+    t.Y = prod + (size_t)(P.nA + P.row_b[r]) * N2;
+    t.out = rows + r;
+    t.absout = nullptr;
+    t.coef[0] = P.coef[r].x;
+    t.coef[1] = P.coef[r].y;
+    t.mode = 0;
+    t.pad = 0;
+    trace[r] = t;
+  }
+  for (int k = threadIdx.x; k < kOut + 1 + kRows; k += blockDim.x) csr[k] = P.csr[k];
 }
 
 }  // namespace
@@ -84,88 +166,24 @@ int rho_noalloc(int N, int Nt, int tf, const double* prop_row, const double* mom
   if (need > kScratchBytes)
     return fail(CTR_ERR_ARG, "ctr_rho_noalloc: Nev=%d needs %zu bytes of scratch, the fixed maximum is %zu (Nev <= 114)",
                 N, need, kScratchBytes);
-  void* base;
-  CTR_TRY(scratch_address(&base));
-  uint8_t* S = (uint8_t*)base;
-  ZTask* d_gemm = (ZTask*)(S + kOffGemm);
-  TraceTask* d_trace = (TraceTask*)(S + kOffTrace);
-  int* d_csr = (int*)(S + kOffCsr);
-  double2* d_rows = (double2*)(S + kOffRows);
-  double2* d_prod = (double2*)(S + kOffProducts);
-
-  // distinct source-side (s3,s4,lp) and sink-side (s1,s2,rp) blocks of the rho table
-  const Tables& T = tables();
-  int keyA[kRows], keyB[kRows];
-  int listA[kProducts / 2], listB[kProducts / 2];
-  int nA = 0, nB = 0;
-  for (int r = 0; r < kRows; r++) {
-    const int ka = (T.rho_spin[r][2] * 4 + T.rho_spin[r][3]) * 5 + T.rho_lprp[r][0];
-    const int kb = (T.rho_spin[r][0] * 4 + T.rho_spin[r][1]) * 5 + T.rho_lprp[r][1];
-    int ia = -1, ib = -1;
-    for (int k = 0; k < nA; k++)
-      if (listA[k] == ka) ia = k;
-    for (int k = 0; k < nB; k++)
-      if (listB[k] == kb) ib = k;
-    if (ia < 0) {
-      if (nA == kProducts / 2) return fail(CTR_ERR_ARG, "ctr_rho_noalloc: table has too many blocks");
-      ia = nA;
-      listA[nA++] = ka;
-    }
-    if (ib < 0) {
-      if (nB == kProducts / 2) return fail(CTR_ERR_ARG, "ctr_rho_noalloc: table has too many blocks");
-      ib = nB;
-      listB[nB++] = kb;
-    }
-    keyA[r] = ia;
-    keyB[r] = ib;
-  }
-
-  std::lock_guard<std::mutex> lk(g_host_mutex);
-  HostTasks& H = g_host;
-  for (int o = 0; o <= kOut; o++) H.csr[o] = 16 * o;  // rows of output o: 16*o .. 16*o+15 (table order)
-  for (int r = 0; r < kRows; r++) H.csr[kOut + 1 + r] = r;
-  CTR_CUDA(cudaMemcpyAsync(d_csr, H.csr, sizeof(H.csr), cudaMemcpyHostToDevice, stream));
-
+  if (g_plan_status != CTR_OK) return fail(g_plan_status, "ctr_rho_noalloc: the rho table has too many blocks");
+  // Looked up on every call: cheap once the module is loaded, and never stale
+  // after a cudaDeviceReset (which reloads the module elsewhere).
+  void* base = nullptr;
+  CTR_CUDA(cudaGetSymbolAddress(&base, g_noalloc_scratch));
+  unsigned char* S = (unsigned char*)base;
+  const ZTask* d_gemm = (const ZTask*)(S + kOffGemm);
+  const TraceTask* d_trace = (const TraceTask*)(S + kOffTrace);
+  const int* d_csr = (const int*)(S + kOffCsr);
+  const double2* d_rows = (const double2*)(S + kOffRows);
   const double2* tau = (const double2*)prop_row;
   const double2* ph = (const double2*)mom5;
+  const int nprod = g_plan.nA + g_plan.nB;
   const int tpd = (N + 31) / 32;
   for (int ti = 0; ti < Nt; ti++) {
-    const double2* tblk = tau + (size_t)ti * 16 * N2;
-    for (int k = 0; k < nA; k++) {
-      const int cd = listA[k] / 5, L = listA[k] % 5;
-      ZTask& z = H.gemm[k];
-      std::memset(&z, 0, sizeof(z));
-      z.A[0] = tblk + (size_t)cd * N2;
-      z.B[0] = ph + ((size_t)ti * 5 + L) * N2;
-      z.C = d_prod + (size_t)k * N2;
-      z.wre[0] = 1.f;
-      z.nterm = 1;
-    }
-    for (int k = 0; k < nB; k++) {
-      const int ab = listB[k] / 5, R = listB[k] % 5;
-      ZTask& z = H.gemm[nA + k];
-      std::memset(&z, 0, sizeof(z));
-      z.A[0] = ph + ((size_t)tf * 5 + R) * N2;
-      z.B[0] = tblk + (size_t)ab * N2;
-      z.C = d_prod + (size_t)(nA + k) * N2;
-      z.wre[0] = 1.f;
-      z.nterm = 1;
-    }
-    for (int r = 0; r < kRows; r++) {
-      TraceTask& t = H.trace[r];
-      std::memset(&t, 0, sizeof(t));
-      t.X = d_prod + (size_t)keyA[r] * N2;
-      t.Y = d_prod + (size_t)(nA + keyB[r]) * N2;
-      t.out = d_rows + r;
-      t.coef[0] = T.rho_coef[r][0];
-      t.coef[1] = T.rho_coef[r][1];
-      t.mode = 0;
-    }
-    // Pageable-source copies: the runtime stages the host data before returning,
-    // so the static host arrays can be refilled for the next t_source at once.
-    CTR_CUDA(cudaMemcpyAsync(d_gemm, H.gemm, sizeof(ZTask) * (nA + nB), cudaMemcpyHostToDevice, stream));
-    CTR_CUDA(cudaMemcpyAsync(d_trace, H.trace, sizeof(TraceTask) * kRows, cudaMemcpyHostToDevice, stream));
-    zgemm_f64_kernel<<<(nA + nB) * tpd * tpd, 256, 0, stream>>>(d_gemm, nA + nB, N, tpd);
+    noalloc_tasks_kernel<<<1, 256, 0, stream>>>(g_plan, N, tf, ti, tau, ph, S);
+    CTR_CUDA(cudaGetLastError());
+    zgemm_f64_kernel<<<nprod * tpd * tpd, 256, 0, stream>>>(d_gemm, nprod, N, tpd);
     CTR_CUDA(cudaGetLastError());
     trace_f64_kernel<<<kRows, 256, 0, stream>>>(d_trace, kRows, N);
     CTR_CUDA(cudaGetLastError());
@@ -180,7 +198,9 @@ int rho_noalloc(int N, int Nt, int tf, const double* prop_row, const double* mom
 
 extern "C" int ctr_rho_noalloc(int nev, int nt, int tf, const double* prop_row, const double* mom5, double* corr,
                                void* stream) {
-  CTR_NO_CAPTURE("ctr_rho_noalloc");
+  if (ctr::capturing())
+    return ctr::fail(CTR_ERR_UNSUPPORTED, "ctr_rho_noalloc is not available while this thread records with "
+                     "ctr_graph_begin/ctr_graph_end");
   if (nev < 1 || nt < 1 || tf < 0 || tf >= nt || !prop_row || !mom5 || !corr)
     return ctr::fail(CTR_ERR_ARG, "ctr_rho_noalloc: bad arguments");
   if (((uintptr_t)prop_row | (uintptr_t)mom5 | (uintptr_t)corr) & 15)

@@ -185,12 +185,18 @@ int ctr_split_levels(int nev, const double* x, const double* y, float* levels, v
  * budget is held by a fixed pool, or they must not trigger the device-wide
  * synchronisation of cudaMalloc/cudaFree).  This entry point has no
  * counterpart in the reference.  Its only scratch is a fixed 32 MiB device
- * array inside the library (enough for Nev <= 114), held by every GPU that
- * loads the library until the process exits; larger Nev are rejected with
- * CTR_ERR_ARG.  It calls no cudaMalloc/cudaFree or other allocating routine.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU (different streams, or threads) race.
+ * array inside the library (enough for Nev <= 114); larger Nev are rejected
+ * with CTR_ERR_ARG.  A device reserves the array when the library's module
+ * holding it is loaded there; with CUDA's default lazy module loading that is
+ * the first ctr_rho_noalloc call on that device, which also looks up the
+ * array's device address.  Make one such warm-up call at start-up, before any
+ * stream capture, so that later calls find the array in place; the device then
+ * holds it until the process exits.  Each call looks the address up again
+ * (cheap once loaded), so a cudaDeviceReset in between is safe.  It calls no
+ * cudaMalloc/cudaFree or other allocating routine and copies nothing from the
+ * host: its task lists are built on the device.  All calls share the array, and
+ * each call rewrites what it reads: calls whose work overlaps on the GPU
+ * (different streams, or threads) race.
  * prop_row: tau(tf, .) [Nt][4][4][N][N]; mom5 [Nt][5][N][N]; corr [Nt][16][3]. */
 int ctr_rho_noalloc(int nev, int nt, int tf, const double* prop_row, const double* mom5, double* corr,
                     void* stream);
@@ -318,9 +324,9 @@ int ctr_timing_report(char* buf, int buflen);
  * those steps between them, synchronising the stream there (as the eager call
  * does).  Recording needs a created stream (not the legacy default stream),
  * uses the autotuner's cached choices (it measures nothing), and rejects the
- * calls that read device data on the host to plan their work: the profile
- * adjoint entry points, ctr_rho_noalloc, the ctr_calculate_* host API and
- * ctr_sync.  A call that fails while recording makes ctr_graph_end fail (the
+ * calls that read device data on the host to plan their work (the profile
+ * adjoint entry points, the ctr_calculate_* host API and ctr_sync) as well as
+ * ctr_rho_noalloc, which keeps to its own fixed array.  A call that fails while recording makes ctr_graph_end fail (the
  * capture is closed and discarded).  Launch counts of replays are added to the
  * launch accounting; per-kernel event timing is not recorded for replays. */
 typedef struct ctr_graph ctr_graph;

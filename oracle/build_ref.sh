@@ -2,11 +2,13 @@
 # Compile the reference's device code, unmodified and from its own source files
 # (lib/contract_kernels_*.cu with the lib/calculate_*_core.h bodies), into
 # sm_103a cubins under oracle/_ref/.  Runs only where the reference tree is
-# mounted (default /root/reference, or $1).  The cubins are test infrastructure:
+# mounted, given as $1 or in $CTR_REFERENCE_ROOT (no default: without either it
+# stops with a message).  The cubins are test infrastructure:
 # oracle/refkernels.py launches them to record the reference's own outputs as
 # golden vectors.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$CTR_REFERENCE_ROOT}
+[ -n "$REF" ] || { echo "usage: build_ref.sh <reference tree> (or set CTR_REFERENCE_ROOT)" >&2; exit 1; }
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF/lib" ] || { echo "reference tree not found at $REF" >&2; exit 1; }

@@ -1,7 +1,7 @@
 """Generate ``tests/golden/tables_ref.json`` from the reference's shipped tables.
 
-Run in a checkout where the reference tree is mounted (default
-``/root/reference``; override with ``--ref``).  It parses every
+Run in a checkout where the reference tree is mounted, given by ``--ref`` or
+the ``CTR_REFERENCE_ROOT`` environment variable (no default).  It parses every
 ``include/constants_*.h`` of the reference and records, for each array, its
 declared shape and the SHA-256 of its value tokens exactly as printed in the
 header (``%d`` / ``%+3.2f``, signed zeros kept), joined by commas.  Only the
@@ -39,7 +39,7 @@ def digest(tokens):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CTR_REFERENCE_ROOT"), required="CTR_REFERENCE_ROOT" not in os.environ)
     ap.add_argument("--out", default=os.path.join(os.path.dirname(__file__), "tables_ref.json"))
     args = ap.parse_args()
     res = {}

@@ -50,9 +50,13 @@ def test_gamma5_is_chiral_diag():
         assert np.allclose(g @ g5, -g5 @ g)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/include"), reason="reference tree not mounted")
+REF_ROOT = os.environ.get("CTR_REFERENCE_ROOT", "")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "include")) if REF_ROOT else True,
+                    reason="reference tree not given (CTR_REFERENCE_ROOT)")
 def test_direct_against_reference_headers():
     import glob
-    for f in glob.glob("/root/reference/include/constants_*.h"):
+    for f in glob.glob(os.path.join(REF_ROOT, "include", "constants_*.h")):
         for name, t in parse_header(f).items():
             assert T.format_values(T.all_tables()[name]) == t["tokens"], name
