@@ -184,6 +184,76 @@ double flops_rows(double rows, double nprod, int N, int Nt) {
 
 }  // namespace
 
+bool contract_state(int* nev, int* nt) {
+  if (nev) *nev = g_nev;
+  if (nt) *nt = g_nt;
+  return g_on;
+}
+
+// lib/contract.cpp:633-638
+void dump_rho(FILE* f, const double* a, int nt) {
+  for (int iop = 0; iop < 16; iop++)
+    for (int it = 0; it < nt; it++) {
+      const double* c = &a[((size_t)it * 48 + iop * 3) * 2];
+      fprintf(f, "%d %d \t %+e %+e \t %+e %+e \t %+e %+e\n", iop, it, c[0], c[1], c[2], c[3], c[4], c[5]);
+    }
+  fprintf(f, "\n");
+  fflush(f);
+}
+
+// lib/contract.cpp:720-722 (printed x2; the label is the option parser's i_dir)
+void dump_rhopi(FILE* f, const double* a, int nt) {
+  for (int iop = 0; iop < 4; iop++)
+    for (int it = 0; it < nt; it++)
+      fprintf(f, "%d %d %d \t %+e %+e\n", iop, contract::i_dir, it, 2 * a[(it * 4 + iop) * 2], 2 * a[(it * 4 + iop) * 2 + 1]);
+  fprintf(f, "\n");
+  fflush(f);
+}
+
+// lib/contract.cpp:815-835
+void dump_pipi(FILE* f, const double* a, int nt, int isospin) {
+  const char* label[5] = {"Square", "DoubleTriangle", "Star", "Fish", "DoubleTriangle_Hor"};
+  for (int k = 0; k < (isospin == 0 ? 5 : 4); k++) {
+    for (int it = 0; it < nt; it++)
+      fprintf(f, "%s: %d \t %+e %+e\n", label[k], it, a[(it * 5 + k) * 2], a[(it * 5 + k) * 2 + 1]);
+    fprintf(f, "\n");
+  }
+  fflush(f);
+}
+
+// lib/contract.cpp:874-878
+void dump_loop(FILE* f, const double* l, int nt) {
+  for (int it = 0; it < nt; it++) fprintf(f, "loop: %d \t %+e %+e\n", it, l[it * 2], l[it * 2 + 1]);
+  fprintf(f, "\n");
+  fflush(f);
+}
+
+// lib/contract.cpp:940-944: printed as -C
+void dump_sigma(FILE* f, const double* a, int nt) {
+  for (int iop = 0; iop < 4; iop++)
+    for (int it = 0; it < nt; it++)
+      fprintf(f, "twop: %d %d \t %+e %+e\n", iop, it, -a[(it * 4 + iop) * 2], -a[(it * 4 + iop) * 2 + 1]);
+  fprintf(f, "\n");
+  fflush(f);
+}
+
+// lib/contract.cpp:1019-1025
+void dump_fish_hor(FILE* f, const double* hf, int nt) {
+  for (int it = 0; it < nt; it++) fprintf(f, "fish_hor: %d \t %+e %+e\n", it, hf[it * 2], hf[it * 2 + 1]);
+  fprintf(f, "\n");
+  fflush(f);
+}
+
+// lib/contract.cpp:1043-1048: scaled by -2/sqrt(6)
+void dump_triangle(FILE* f, const double* a, int nt) {
+  const double w = -2. / std::sqrt(6.);
+  for (int iop = 0; iop < 2; iop++)
+    for (int it = 0; it < nt; it++)
+      fprintf(f, "triangle: %d %d \t %+e %+e\n", iop, it, w * a[(it * 2 + iop) * 2], w * a[(it * 2 + iop) * 2 + 1]);
+  fprintf(f, "\n");
+  fflush(f);
+}
+
 // File payload (host, complex128, file order) -> host_out in the library layout,
 // transposed on the device.
 int reorder_prop_device(int N, int Nt, const double* file_payload, int single, void* host_out) {
@@ -230,6 +300,7 @@ int ctr_contract_destroy(void) {
   CTR_NO_CAPTURE("ctr_contract_destroy");
   if (!g_on) return fail(CTR_ERR_ARG, "cannot destroy contract library because is not on");
   ctr_release_workspace();
+  compat_release();
   g_on = false;
   return CTR_OK;
 }
@@ -320,14 +391,7 @@ int ctr_calculate_rho(int nev, int nt, const void* prop, const double* mom, int 
   CTR_TRY(ctr_sync(nullptr));
   std::vector<double> a;
   CTR_TRY(averaged(dc, nt, 48, a));
-  // lib/contract.cpp:633-638
-  for (int iop = 0; iop < 16; iop++)
-    for (int it = 0; it < nt; it++) {
-      const double* c = &a[((size_t)it * 48 + iop * 3) * 2];
-      fprintf(F.f, "%d %d \t %+e %+e \t %+e %+e \t %+e %+e\n", iop, it, c[0], c[1], c[2], c[3], c[4], c[5]);
-    }
-  fprintf(F.f, "\n");
-  fflush(F.f);
+  dump_rho(F.f, a.data(), nt);
   report(t0, flops_rows(768, 2, nev, nt), single);
   return CTR_OK;
 }
@@ -351,12 +415,7 @@ int ctr_calculate_rhopi(int idir, int nev, int nt, const void* prop, const doubl
   CTR_TRY(ctr_sync(nullptr));
   std::vector<double> a;
   CTR_TRY(averaged(dc, nt, 4, a));
-  // lib/contract.cpp:720-722 (the label is the option parser's i_dir)
-  for (int iop = 0; iop < 4; iop++)
-    for (int it = 0; it < nt; it++)
-      fprintf(F.f, "%d %d %d \t %+e %+e\n", iop, contract::i_dir, it, 2 * a[(it * 4 + iop) * 2], 2 * a[(it * 4 + iop) * 2 + 1]);
-  fprintf(F.f, "\n");
-  fflush(F.f);
+  dump_rhopi(F.f, a.data(), nt);
   report(t0, flops_rows(256, 4, nev, nt), single);
   return CTR_OK;
 }
@@ -380,14 +439,7 @@ int ctr_calculate_pipi(int nev, int nt, const void* prop, const double* p1, cons
   CTR_TRY(ctr_sync(nullptr));
   std::vector<double> a;
   CTR_TRY(averaged(dc, nt, 5, a));
-  // lib/contract.cpp:815-835
-  const char* label[5] = {"Square", "DoubleTriangle", "Star", "Fish", "DoubleTriangle_Hor"};
-  for (int k = 0; k < (isospin == 0 ? 5 : 4); k++) {
-    for (int it = 0; it < nt; it++)
-      fprintf(F.f, "%s: %d \t %+e %+e\n", label[k], it, a[(it * 5 + k) * 2], a[(it * 5 + k) * 2 + 1]);
-    fprintf(F.f, "\n");
-  }
-  fflush(F.f);
+  dump_pipi(F.f, a.data(), nt, isospin);
   const double n3 = 8.0 * nev * (double)nev * nev, n2 = 8.0 * nev * (double)nev;
   const double sq = 256 * (6 * n3 + n2), sf = 16 * (2 * n3 + n2);
   report(t0, (isospin == 0 ? 3 * sq + 2 * sf : 2 * sq + 2 * sf) * nt * (double)nt, single);
@@ -410,9 +462,7 @@ int ctr_calculate_sigma(int nev, int nt, const void* prop, const double* mom, in
     CTR_TRY(ctr_loop_unity(CTR_ENGINE_FP64, nev, nt, dd.d(), dm.d(), dl.d(), nullptr));
     std::vector<double> l((size_t)nt * 2);
     CTR_CUDA(cudaMemcpy(l.data(), dl.p, l.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int it = 0; it < nt; it++) fprintf(F.f, "loop: %d \t %+e %+e\n", it, l[it * 2], l[it * 2 + 1]);
-    fprintf(F.f, "\n");
-    fflush(F.f);
+    dump_loop(F.f, l.data(), nt);
     report(t0, 320000.0 * nt * (nev / 100.0) * (nev / 100.0), single);
   }
   const double t0 = now();
@@ -423,12 +473,7 @@ int ctr_calculate_sigma(int nev, int nt, const void* prop, const double* mom, in
   CTR_TRY(ctr_sync(nullptr));
   std::vector<double> a;
   CTR_TRY(averaged(dc, nt, 4, a));
-  // lib/contract.cpp:940-944: printed as -C
-  for (int iop = 0; iop < 4; iop++)
-    for (int it = 0; it < nt; it++)
-      fprintf(F.f, "twop: %d %d \t %+e %+e\n", iop, it, -a[(it * 4 + iop) * 2], -a[(it * 4 + iop) * 2 + 1]);
-  fprintf(F.f, "\n");
-  fflush(F.f);
+  dump_sigma(F.f, a.data(), nt);
   report(t0, flops_rows(64, 2, nev, nt), single);
   return CTR_OK;
 }
@@ -450,9 +495,7 @@ int ctr_calculate_sigmapi(int nev, int nt, const void* prop, const double* p1, c
     CTR_TRY(ctr_loop_unity(CTR_ENGINE_FP64, nev, nt, dd.d(), dm.d(), dl.d(), nullptr));
     std::vector<double> l((size_t)nt * 2);
     CTR_CUDA(cudaMemcpy(l.data(), dl.p, l.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int it = 0; it < nt; it++) fprintf(F.f, "loop: %d \t %+e %+e\n", it, l[it * 2], l[it * 2 + 1]);
-    fprintf(F.f, "\n");
-    fflush(F.f);
+    dump_loop(F.f, l.data(), nt);
     report(t0, 320000.0 * nt * (nev / 100.0) * (nev / 100.0), single);
   }
   const double t0 = now();
@@ -467,19 +510,10 @@ int ctr_calculate_sigmapi(int nev, int nt, const void* prop, const double* p1, c
   CTR_TRY(ctr_sync(nullptr));
   std::vector<double> hf((size_t)nt * 2);
   CTR_CUDA(cudaMemcpy(hf.data(), dhf.p, hf.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  // lib/contract.cpp:1019-1025
-  for (int it = 0; it < nt; it++) fprintf(F.f, "fish_hor: %d \t %+e %+e\n", it, hf[it * 2], hf[it * 2 + 1]);
-  fprintf(F.f, "\n");
-  fflush(F.f);
+  dump_fish_hor(F.f, hf.data(), nt);
   std::vector<double> a;
   CTR_TRY(averaged(dtr, nt, 2, a));
-  // lib/contract.cpp:1043-1048: scaled by -2/sqrt(6)
-  const double w = -2. / std::sqrt(6.);
-  for (int iop = 0; iop < 2; iop++)
-    for (int it = 0; it < nt; it++)
-      fprintf(F.f, "triangle: %d %d \t %+e %+e\n", iop, it, w * a[(it * 2 + iop) * 2], w * a[(it * 2 + iop) * 2 + 1]);
-  fprintf(F.f, "\n");
-  fflush(F.f);
+  dump_triangle(F.f, a.data(), nt);
   const double n3 = 8.0 * nev * (double)nev * nev, n2 = 8.0 * nev * (double)nev;
   report(t0, 16 * (2 * n3 + n2) * nt + 128 * (4 * n3 + n2) * nt * (double)nt, single);
   return CTR_OK;

@@ -185,4 +185,20 @@ int twosided_split(int nev, int nt, int tf_begin, int tf_end, const double* prop
 int chain_values(int N, int Nt, int nphi, const double* prop, const double* phi, const std::vector<ctr_factor>& factors,
                  const std::vector<int>& off, double* values, cudaStream_t s, int engine);
 
+// ------------------------------------------- reference-compatible C++ layer
+// State set by initContract (api.cu): false while the library is off.
+bool contract_state(int* nev, int* nt);
+// The reference's result text blocks (the dumpData bodies of lib/contract.cpp),
+// appended to f from source-averaged correlators [Nt][ncorr] complex (interleaved
+// re/im doubles); loop and fish_hor take the per-time values [Nt].
+void dump_rho(FILE* f, const double* avg, int nt);
+void dump_rhopi(FILE* f, const double* avg, int nt);
+void dump_pipi(FILE* f, const double* avg, int nt, int isospin);
+void dump_loop(FILE* f, const double* loop, int nt);
+void dump_sigma(FILE* f, const double* avg, int nt);
+void dump_fish_hor(FILE* f, const double* hf, int nt);
+void dump_triangle(FILE* f, const double* avg, int nt);
+// Frees the device staging buffers of the texture-object launchers (compat.cu).
+void compat_release();
+
 }  // namespace ctr

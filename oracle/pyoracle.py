@@ -137,13 +137,14 @@ def pipi(prop, p1, p2, p3, p4, iso):
     return np.stack([pipi_row(prop, p1, p2, p3, p4, tf, iso)["corr"] for tf in range(nt)])
 
 
-def loop_unity(prop, mom):
+def loop_unity(prop, mom, with_rows=False):
+    """loop [Nt] (and, with_rows, the per-spin traces [Nt, 4])."""
     nt, n = prop.shape[0], prop.shape[-1]
     diag = _c(prop_diag(prop))
     rows = np.zeros((nt, 4), np.complex128)
     loop = np.zeros((nt,), np.complex128)
     lib().oracle_loop_unity(n, nt, _p(diag), _p(_c(mom)), _p(rows), _p(loop))
-    return loop
+    return (loop, rows) if with_rows else loop
 
 
 def sigma_row(prop, mom2, tf):
@@ -162,7 +163,8 @@ def sigma(prop, mom2):
     return np.stack([sigma_row(prop, mom2, tf)[1] for tf in range(nt)])
 
 
-def sigmapi_hor_fish(prop, p1, p2):
+def sigmapi_hor_fish(prop, p1, p2, with_rows=False):
+    """hor_fish [Nt] (and, with_rows, the coefficient-weighted spin rows [Nt, 16])."""
     _tables()
     nt, n = prop.shape[0], prop.shape[-1]
     t = _SIGMAPI
@@ -171,7 +173,7 @@ def sigmapi_hor_fish(prop, p1, p2):
     lib().oracle_sigmapi_hor_fish(n, nt, _p(_c(prop_diag(prop))), _p(_c(p1)), _p(_c(p2)),
                                   _p(_i16(t["spinIndices_sigmapi_hor_fish"])), _p(_f32(t["coef_sigmapi_hor_fish"])),
                                   _p(rows), _p(corr))
-    return corr
+    return (corr, rows) if with_rows else corr
 
 
 def sigmapi_triangle_row(prop, p1, p2, mom2_p1p2, tf):

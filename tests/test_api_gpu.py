@@ -188,8 +188,9 @@ def test_cpp_driver_against_interface_h(cuda, tmp_path):
     src.write_text(CPP)
     exe = tmp_path / "driver"
     pkg = os.path.dirname(_build.LIB)
+    from tests.test_cpp_boundary import cuda_home
     subprocess.check_call(["g++", "-O1", "-o", str(exe), str(src), "-I", os.path.join(ROOT, "include"),
-                           "-L", pkg, "-lctr", "-Wl,-rpath," + pkg])
+                           "-I", os.path.join(cuda_home(), "include"), "-L", pkg, "-lctr", "-Wl,-rpath," + pkg])
     out = tmp_path / "rho.dat"
     r = subprocess.run([str(exe), str(n), str(nt), str(tmp_path / "prop.bin"), str(tmp_path / "mom.bin"), str(out)],
                        capture_output=True, text=True, timeout=300)

@@ -5,6 +5,8 @@ correlator entries), through properties that need no CPU oracle at this size:
 * every split-engine entry is within 1e-9 (relative, entry by entry) of the
   plain FP64 engine, whose parity with the oracle and the reference's own
   kernels is tested at smaller sizes;
+* a whole t_sink row (t_sink = 0: 64 source times x 21 outputs = 1 344 entries)
+  matches the oracle entry by entry on both engines;
 * scaling the perambulator by 2^3 scales every correlator by exactly 2^6, on
   both engines, bit for bit: the split engine's slice scales are powers of two,
   so its digits, products, error estimates and refinement decisions are the
@@ -14,6 +16,7 @@ import pytest
 import torch
 
 from contractions_code_scattering_gb300 import api, synth
+from tests import parity as P
 
 pytestmark = pytest.mark.gpu
 
@@ -52,3 +55,21 @@ def test_power_of_two_scaling_is_exact(workload):
         b = _run(workload, engine, tau=tau8)
         assert np.array_equal(b, a * 64.0), engine
     del tau8
+
+
+def test_sink_row_matches_oracle_per_entry(workload):
+    """t_sink = 0 of the production workload against the oracle (the reference's
+    chain order: every spin row recomputes both of its products)."""
+    from oracle import pyoracle as O
+    tau, phi, rows, coef, oi, nout = workload
+    vals = O.twosided_rows(tau[0].cpu().numpy(), phi.cpu().numpy(), rows, coef, 0, 0, tau.shape[0])
+    ref = np.zeros((tau.shape[0], nout), np.complex128)
+    ab = np.zeros((tau.shape[0], nout))
+    for r, o in enumerate(oi):
+        ref[:, o] += vals[:, r]
+        ab[:, o] += np.abs(vals[:, r])
+    for engine, tol in (("fp64", 1e-12), ("split", 1e-9)):
+        got = _run(workload, engine)[0]
+        st = P.entrywise(got, ref, tol, ab, "t_sink 0, %s engine" % engine)
+        print("full-size t_sink 0, %s: worst per-entry rel %.2e, %d entries needed the floor"
+              % (engine, st["max_rel"], st["needed_floor"]))

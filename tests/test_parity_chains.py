@@ -1,7 +1,12 @@
 """GPU parity of the chain diagrams (rho->pipi, pipi I=1/I=0, loop-unity,
-sigma->pipi) on the plain FP64 engine: against the reference's own kernel
-outputs (golden vectors, Nev=100) and against the oracle at other sizes.
-Tolerance 1e-12 relative to the largest |entry| of each compared array."""
+sigma->pipi) on both engines: against the reference's own kernel outputs
+(golden vectors, Nev=100) and against the oracle at other sizes and at the
+shapes of the benchmark configurations.
+
+Every entry is gated on its own (tests/parity.py): |err| <= tol |ref| plus the
+FP64 rounding floor 2^-44 x (sum of the magnitudes of the entry's spin rows),
+which matters only where the rows cancel.  tol = 1e-12 for the plain FP64
+engine and 1e-9 for the split engine (1e-10 on the small random data)."""
 import os
 
 import numpy as np
@@ -10,21 +15,50 @@ import torch
 
 from contractions_code_scattering_gb300 import api, synth
 from oracle import pyoracle as O
+from tests import parity as P
 
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+SPLIT_TOL = 1e-10
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_outputs.npz")
 
 
-def _close(got, ref, tol=TOL):
-    got = got.cpu().numpy() if hasattr(got, "cpu") else got
-    err = np.abs(got - ref).max() / np.abs(ref).max()
-    assert err <= tol, "error %.3e relative to max |entry| (tolerance %.1e)" % (err, tol)
+def _np(x):
+    return x.cpu().numpy() if hasattr(x, "cpu") else np.asarray(x)
 
 
 def _dev(a, cuda):
     return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+# ---- oracle references with their per-entry row magnitudes
+def ref_pipi(prop, ph, iso, tfs=None):
+    tfs = range(prop.shape[0]) if tfs is None else tfs
+    ds = [O.pipi_row(prop, *ph, tf, iso) for tf in tfs]
+    return np.stack([d["corr"] for d in ds]), np.stack([P.pipi_rows_abs(d, iso) for d in ds])
+
+
+def ref_rhopi(prop, p1, p2, mom5, idir, tfs=None):
+    tfs = range(prop.shape[0]) if tfs is None else tfs
+    rc = [O.rhopi_row(prop, p1, p2, mom5, tf, idir) for tf in tfs]
+    return np.stack([c for _, c in rc]), np.stack([P.rhopi_rows_abs(r) for r, _ in rc])
+
+
+def ref_triangle(prop, p1, p2, mom2, tfs=None):
+    tfs = range(prop.shape[0]) if tfs is None else tfs
+    rc = [O.sigmapi_triangle_row(prop, p1, p2, mom2, tf) for tf in tfs]
+    return np.stack([c for _, c in rc]), np.stack([P.triangle_rows_abs(r) for r, _ in rc])
+
+
+def ref_hor_fish(prop, p1, p2):
+    c, r = O.sigmapi_hor_fish(prop, p1, p2, with_rows=True)
+    return c, P.sum_rows_abs(r)
+
+
+def ref_loop(prop, mom):
+    c, r = O.loop_unity(prop, mom, with_rows=True)
+    return c, P.sum_rows_abs(r)
 
 
 @pytest.fixture(scope="module")
@@ -42,102 +76,164 @@ def small(cuda):
     return d, t
 
 
+@pytest.mark.parametrize("engine,tol", [("fp64", TOL), ("split", SPLIT_TOL)])
 @pytest.mark.parametrize("iso", [1, 0])
-def test_pipi_vs_oracle(small, iso):
+def test_pipi_vs_oracle(small, iso, engine, tol):
     d, t = small
-    ref = O.pipi(d["prop"], *d["ph"], iso)
-    got = api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], iso)
-    _close(got, ref)
+    ref, ab = ref_pipi(d["prop"], d["ph"], iso)
+    got = api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], iso, engine=engine)
+    P.entrywise(_np(got), ref, tol, ab, "pipi I%d %s" % (iso, engine))
 
 
+@pytest.mark.parametrize("engine,tol", [("fp64", TOL), ("split", SPLIT_TOL)])
 @pytest.mark.parametrize("idir", [0, 1, 2])
-def test_rhopi_vs_oracle(small, idir):
+def test_rhopi_vs_oracle(small, idir, engine, tol):
     d, t = small
-    ref = O.rhopi(d["prop"], d["ph"][0], d["ph"][1], d["mom5"], idir)
-    got = api.run_contract_rhopi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom5"], idir)
-    _close(got, ref)
+    ref, ab = ref_rhopi(d["prop"], d["ph"][0], d["ph"][1], d["mom5"], idir)
+    got = api.run_contract_rhopi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom5"], idir, engine=engine)
+    P.entrywise(_np(got), ref, tol, ab, "rhopi idir %d %s" % (idir, engine))
 
 
-def test_sigmapi_and_loop_vs_oracle(small):
+@pytest.mark.parametrize("engine,tol", [("fp64", TOL), ("split", SPLIT_TOL)])
+def test_sigmapi_and_loop_vs_oracle(small, engine, tol):
     d, t = small
-    hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"])
-    _close(hf, O.sigmapi_hor_fish(d["prop"], d["ph"][0], d["ph"][1]))
-    _close(tri, O.sigmapi_triangle(d["prop"], d["ph"][0], d["ph"][1], d["mom2"]))
-    _close(api.run_contract_loop_unity(t["diag"], t["ph"][2]), O.loop_unity(d["prop"], d["ph"][2]))
+    hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"], engine=engine)
+    ref, ab = ref_hor_fish(d["prop"], d["ph"][0], d["ph"][1])
+    P.entrywise(_np(hf), ref, tol, ab, "hor fish %s" % engine)
+    ref, ab = ref_triangle(d["prop"], d["ph"][0], d["ph"][1], d["mom2"])
+    P.entrywise(_np(tri), ref, tol, ab, "triangle %s" % engine)
+    ref, ab = ref_loop(d["prop"], d["ph"][2])
+    P.entrywise(_np(api.run_contract_loop_unity(t["diag"], t["ph"][2], engine=engine)), ref, tol, ab, "loop")
 
 
 def test_row_range(small):
     """A single t_sink row held on the device, as the reference stages it."""
     d, t = small
-    ref = O.pipi(d["prop"], *d["ph"], 0)
+    ref, ab = ref_pipi(d["prop"], d["ph"], 0)
     for tf in range(d["prop"].shape[0]):
         row = t["prop"][tf:tf + 1].contiguous()
         got = api.run_contract_pipi(row, t["diag"], *t["ph"], 0, tf_range=(tf, tf + 1))
-        _close(got[0], ref[tf])
+        P.entrywise(_np(got[0]), ref[tf], TOL, ab[tf], "pipi row %d" % tf)
+
+
+# ---- golden vectors: the reference's own kernels at Nev = 100
+def _gold_abs(gold):
+    out = {}
+    for idir in range(3):
+        out["rhopi%d" % idir] = P.rhopi_rows_abs(gold["rhopi%d_rows" % idir])
+    for iso in (0, 1):
+        g = {k: gold["pipi_I%d_%s" % (iso, k)] for k in ("square", "dtri", "dtri_hor")}
+        g["star"] = np.moveaxis(gold["pipi_I%d_star" % iso], 2, 0)  # [2][tf][ti][16]
+        g["fish"] = np.moveaxis(gold["pipi_I%d_fish" % iso], 2, 0)
+        out["pipi%d" % iso] = P.pipi_rows_abs(g, iso)
+    out["hor_fish"] = P.sum_rows_abs(gold["sigmapi_hor_fish_rows"])
+    out["triangle"] = P.triangle_rows_abs(gold["sigmapi_triangle_rows"])
+    out["loop"] = P.sum_rows_abs(gold["loop_rows"])
+    return out
 
 
 @pytest.mark.skipif(not os.path.exists(GOLD), reason="reference golden vectors not recorded")
-def test_chains_vs_reference_kernels(cuda):
+@pytest.mark.parametrize("engine,tol", [("fp64", TOL), ("split", 1e-9)])
+def test_chains_vs_reference_kernels(cuda, engine, tol):
+    """Nev = 100; on the split engine the chains' four-term block products have
+    K = 400 (leading digit halved)."""
     from tests.golden.make_ref_fixtures import inputs
     gold = dict(np.load(GOLD))
+    ab = _gold_abs(gold)
     d = inputs()
     prop = _dev(d["prop"], cuda)
     diag = api.prop_diag(prop)
     p = [_dev(d[k], cuda) for k in ("p1", "p2", "p3", "p4")]
     mom5, mom2 = _dev(d["mom5"], cuda), _dev(d["mom2"], cuda)
     for idir in range(3):
-        _close(api.run_contract_rhopi(prop, diag, p[0], p[1], mom5, idir), gold["rhopi%d_corr" % idir])
+        got = api.run_contract_rhopi(prop, diag, p[0], p[1], mom5, idir, engine=engine)
+        P.entrywise(_np(got), gold["rhopi%d_corr" % idir], tol, ab["rhopi%d" % idir], "rhopi%d" % idir)
     for iso in (0, 1):
-        _close(api.run_contract_pipi(prop, diag, *p, iso), gold["pipi_I%d_corr" % iso])
-    hf, tri = api.run_contract_sigmapi(prop, diag, p[0], p[1], mom2)
-    _close(hf, gold["sigmapi_hor_fish"])
-    _close(tri, gold["sigmapi_triangle"])
-    _close(api.run_contract_loop_unity(diag, p[0]), gold["loop"])
+        got = api.run_contract_pipi(prop, diag, *p, iso, engine=engine)
+        P.entrywise(_np(got), gold["pipi_I%d_corr" % iso], tol, ab["pipi%d" % iso], "pipi I%d" % iso)
+    hf, tri = api.run_contract_sigmapi(prop, diag, p[0], p[1], mom2, engine=engine)
+    P.entrywise(_np(hf), gold["sigmapi_hor_fish"], tol, ab["hor_fish"], "hor fish")
+    P.entrywise(_np(tri), gold["sigmapi_triangle"], tol, ab["triangle"], "triangle")
+    P.entrywise(_np(api.run_contract_loop_unity(diag, p[0], engine=engine)), gold["loop"], tol, ab["loop"], "loop")
 
 
-# ---- split engine: every block product of the chains on the tensor cores
-SPLIT_TOL = 1e-10
+# ---- the chain shapes of the benchmark configurations
+def test_mixed_config_shape_split(cuda):
+    """The mixed cross-correlator configuration's chain shape on the split engine:
+    Nev = 128, so the four-term gamma_5 tasks have K = 4 x 128 = 512, the bound up to
+    which the split engine's leading level stays exact; perambulator decay 0.25,
+    momentum elementals Phi(+-p) for p = (1,1,1) and random rho / sigma operators.
+    rho -> pi pi (3 polarisations), sigma -> pi pi (triangle and horizontal fish) and
+    the sigma loops, per entry against the oracle on t_sink rows 0 and 2."""
+    nt, n = 3, 128
+    prop = synth.make_prop(nt, n, seed=900, decay=0.25)
+    moms = [(1, 1, 1), (-1, -1, -1)]
+    phis = synth.make_phi_momenta(nt, n, moms, seed=901)
+    p1, p2 = phis[moms[0]], phis[moms[1]]
+    rng = np.random.default_rng(902)
+    sd = np.sqrt(0.5 / n)
+    mom5 = np.ascontiguousarray(rng.normal(0, sd, (nt, 5, n, n)) + 1j * rng.normal(0, sd, (nt, 5, n, n)))
+    mom2 = np.ascontiguousarray(mom5[:, :2])
+    tp, dp1, dp2, d5, d2 = (_dev(x, cuda) for x in (prop, p1, p2, mom5, mom2))
+    diag = api.prop_diag(tp)
+    rows = [0, 2]
+    tol = 1e-9
+    for idir in range(3):
+        got = _np(api.run_contract_rhopi(tp, diag, dp1, dp2, d5, idir, engine="split"))[rows]
+        ref, ab = ref_rhopi(prop, p1, p2, mom5, idir, rows)
+        P.entrywise(got, ref, tol, ab, "rhopi idir %d" % idir)
+    hf, tri = api.run_contract_sigmapi(tp, diag, dp1, dp2, d2, engine="split")
+    ref, ab = ref_triangle(prop, p1, p2, mom2, rows)
+    P.entrywise(_np(tri)[rows], ref, tol, ab, "sigma-pipi triangle")
+    ref, ab = ref_hor_fish(prop, p1, p2)
+    P.entrywise(_np(hf), ref, tol, ab, "hor fish")
+    for k in range(2):
+        got = _np(api.run_contract_loop_unity(diag, d2[:, k].contiguous(), engine="split"))
+        ref, ab = ref_loop(prop, mom2[:, k])
+        P.entrywise(got, ref, tol, ab, "sigma loop %d" % k)
 
 
-@pytest.mark.parametrize("iso", [1, 0])
-def test_pipi_split_vs_oracle(small, iso):
-    d, t = small
-    ref = O.pipi(d["prop"], *d["ph"], iso)
-    got = api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], iso, engine="split")
-    _close(got, ref, SPLIT_TOL)
+@pytest.fixture(scope="module")
+def pipi19(cuda):
+    """The pi pi configuration's 19 momentum pairs (p, -p), |p|^2 <= 2, at Nev = 100
+    (Nt = 4, t_sink row 1 sampled), with the oracle's I=0 rows for every pair; the
+    I=1 weights are applied to the same rows."""
+    nt, n, tf = 4, 100, 1
+    prop = synth.make_prop(nt, n, seed=1200, decay=0.35)
+    moms = synth.momenta(2)
+    phis = synth.make_phi_momenta(nt, n, moms, seed=1201)
+    pairs = [(p, tuple(-c for c in p)) for p in moms]
+    refs = {}
+    for a, b in pairs:
+        d = O.pipi_row(prop, phis[a], phis[b], phis[a], phis[b], tf, 0)
+        refs[(a, b)] = d
+    dev = {"prop": _dev(prop, cuda), "phi": {p: _dev(phis[p], cuda) for p in moms}}
+    dev["diag"] = api.prop_diag(dev["prop"])
+    return dict(nt=nt, tf=tf, pairs=pairs, refs=refs, dev=dev)
 
 
-@pytest.mark.parametrize("idir", [0, 2])
-def test_rhopi_split_vs_oracle(small, idir):
-    d, t = small
-    ref = O.rhopi(d["prop"], d["ph"][0], d["ph"][1], d["mom5"], idir)
-    got = api.run_contract_rhopi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom5"], idir, engine="split")
-    _close(got, ref, SPLIT_TOL)
+def _i1_from_i0_rows(d):
+    sq, dt = d["square"].sum(-1), d["dtri"].sum(-1)
+    star = d["star"][0].sum(-1) * d["star"][1].sum(-1)
+    fish = d["fish"][0].sum(-1) * d["fish"][1].sum(-1)
+    return np.stack([-2 * sq, 2 * dt, -star, fish, 0 * sq], axis=-1)
 
 
-def test_sigmapi_split_vs_oracle(small):
-    d, t = small
-    hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"], engine="split")
-    _close(hf, O.sigmapi_hor_fish(d["prop"], d["ph"][0], d["ph"][1]), SPLIT_TOL)
-    _close(tri, O.sigmapi_triangle(d["prop"], d["ph"][0], d["ph"][1], d["mom2"]), SPLIT_TOL)
-
-
-@pytest.mark.skipif(not os.path.exists(GOLD), reason="reference golden vectors not recorded")
-def test_split_chains_vs_reference_kernels(cuda):
-    """Nev = 100: four-term block products (K = 400, leading digit halved) on the split engine."""
-    from tests.golden.make_ref_fixtures import inputs
-    gold = dict(np.load(GOLD))
-    d = inputs()
-    prop = _dev(d["prop"], cuda)
-    diag = api.prop_diag(prop)
-    p = [_dev(d[k], cuda) for k in ("p1", "p2", "p3", "p4")]
-    mom5, mom2 = _dev(d["mom5"], cuda), _dev(d["mom2"], cuda)
-    _close(api.run_contract_rhopi(prop, diag, p[0], p[1], mom5, 1, engine="split"), gold["rhopi1_corr"], SPLIT_TOL)
-    for iso in (0, 1):
-        _close(api.run_contract_pipi(prop, diag, *p, iso, engine="split"), gold["pipi_I%d_corr" % iso], SPLIT_TOL)
-    hf, tri = api.run_contract_sigmapi(prop, diag, p[0], p[1], mom2, engine="split")
-    _close(hf, gold["sigmapi_hor_fish"], SPLIT_TOL)
-    _close(tri, gold["sigmapi_triangle"], SPLIT_TOL)
+@pytest.mark.parametrize("engine,tol", [("fp64", TOL), ("split", 1e-9)])
+@pytest.mark.parametrize("iso", [0, 1])
+def test_pipi_19_pair_set(pipi19, engine, iso, tol):
+    c = pipi19
+    dv, tf = c["dev"], c["tf"]
+    row = dv["prop"][tf:tf + 1].contiguous()
+    stats = []
+    for a, b in c["pairs"]:
+        d = c["refs"][(a, b)]
+        ref = d["corr"] if iso == 0 else _i1_from_i0_rows(d)
+        pa, pb = dv["phi"][a], dv["phi"][b]
+        got = _np(api.run_contract_pipi(row, dv["diag"], pa, pb, pa, pb, iso, engine=engine, tf_range=(tf, tf + 1)))
+        stats.append(P.entrywise(got[0], ref, tol, P.pipi_rows_abs(d, iso), "pair %s I%d %s" % (a, iso, engine)))
+    print("pipi 19 pairs I%d %s: worst per-entry rel %.2e, %d entries needed the floor"
+          % (iso, engine, max(s["max_rel"] for s in stats), sum(s["needed_floor"] for s in stats)))
 
 
 def test_block_product_tasks_split_vs_fp64(cuda):
@@ -174,32 +270,32 @@ def _refine(tol):
 
 def test_split_chain_refinement(small):
     """Per-entry accuracy of the split chain engine: with the tolerance below the
-    engine's error every pair is recomputed by the FP64 engine (results equal to
-    FP64 rounding); with 1e-9 every entry meets 1e-9 relative to itself."""
+    engine's error every pair is recomputed by the FP64 engine (results at the FP64
+    engine's per-entry tolerance); with 1e-9 every entry meets 1e-9 relative to itself."""
     from contractions_code_scattering_gb300._lib import lib
     d, t = small
     nt = d["prop"].shape[0]
-    ref_pp = O.pipi(d["prop"], *d["ph"], 0)
-    ref_rp = O.rhopi(d["prop"], d["ph"][0], d["ph"][1], d["mom5"], 1)
-    ref_hf = O.sigmapi_hor_fish(d["prop"], d["ph"][0], d["ph"][1])
-    ref_tr = O.sigmapi_triangle(d["prop"], d["ph"][0], d["ph"][1], d["mom2"])
-
-    def rel(got, ref):
-        got = got.cpu().numpy()
-        return (np.abs(got - ref) / np.abs(ref)).max()
+    ref_pp = ref_pipi(d["prop"], d["ph"], 0)
+    ref_rp = ref_rhopi(d["prop"], d["ph"][0], d["ph"][1], d["mom5"], 1)
+    ref_hf = ref_hor_fish(d["prop"], d["ph"][0], d["ph"][1])
+    ref_tr = ref_triangle(d["prop"], d["ph"][0], d["ph"][1], d["mom2"])
     try:
         _refine(1e-15)
-        assert rel(api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], 0, engine="split"), ref_pp) < 1e-12
+        P.entrywise(_np(api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], 0, engine="split")), ref_pp[0],
+                    TOL, ref_pp[1], "pipi refined")
         assert lib().ctr_split_refined() == nt * nt * 5
-        assert rel(api.run_contract_rhopi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom5"], 1,
-                                          engine="split"), ref_rp) < 1e-12
+        P.entrywise(_np(api.run_contract_rhopi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom5"], 1,
+                                               engine="split")), ref_rp[0], TOL, ref_rp[1], "rhopi refined")
         assert lib().ctr_split_refined() == nt * nt * 4
         hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"], engine="split")
-        assert rel(hf, ref_hf) < 1e-12 and rel(tri, ref_tr) < 1e-12
+        P.entrywise(_np(hf), ref_hf[0], TOL, ref_hf[1], "hor fish refined")
+        P.entrywise(_np(tri), ref_tr[0], TOL, ref_tr[1], "triangle refined")
         assert lib().ctr_split_refined() == nt + nt * nt * 2
         _refine(1e-9)
-        assert rel(api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], 0, engine="split"), ref_pp) <= 1e-9
+        P.entrywise(_np(api.run_contract_pipi(t["prop"], t["diag"], *t["ph"], 0, engine="split")), ref_pp[0], 1e-9,
+                    ref_pp[1], "pipi at 1e-9")
         hf, tri = api.run_contract_sigmapi(t["prop"], t["diag"], t["ph"][0], t["ph"][1], t["mom2"], engine="split")
-        assert rel(hf, ref_hf) <= 1e-9 and rel(tri, ref_tr) <= 1e-9
+        P.entrywise(_np(hf), ref_hf[0], 1e-9, ref_hf[1], "hor fish at 1e-9")
+        P.entrywise(_np(tri), ref_tr[0], 1e-9, ref_tr[1], "triangle at 1e-9")
     finally:
         _refine(1e-9)

@@ -60,3 +60,42 @@ def test_direct_against_reference_headers():
     for f in glob.glob(os.path.join(REF_ROOT, "include", "constants_*.h")):
         for name, t in parse_header(f).items():
             assert T.format_values(T.all_tables()[name]) == t["tokens"], name
+
+
+HEADERS = ["constants_rho.h", "constants_rhopi.h", "constants_pipi.h", "constants_sigma.h", "constants_sigmapi.h"]
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+
+def test_shipped_headers_are_the_generated_ones():
+    """include/constants_*.h are exactly what the generator renders from the
+    library's own tables (contractions_code_scattering_gb300/constants_headers.py)."""
+    from contractions_code_scattering_gb300 import constants_headers as CH
+    files = CH.render(CH.library_tables())
+    for f in HEADERS + ["constants.h"]:
+        assert open(os.path.join(INCLUDE, f)).read() == files[f], f
+
+
+def test_shipped_headers_match_reference_digests():
+    """Every array of the shipped headers has the reference header's name, type,
+    shape and token digest (tests/golden/tables_ref.json)."""
+    seen = set()
+    for f in HEADERS:
+        for name, t in parse_header(os.path.join(INCLUDE, f)).items():
+            assert REF[name]["header"] == "include/" + f, name
+            assert t["shape"] == REF[name]["shape"] and t["type"] == REF[name]["type"], name
+            assert digest(t["tokens"]) == REF[name]["sha256"], name
+            seen.add(name)
+    assert seen == set(REF)
+
+
+@pytest.mark.skipif(__import__("shutil").which("g++") is None, reason="no C++ compiler")
+def test_shipped_headers_compile(tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text('#include <constants.h>\n#include <cstdio>\nint main() { printf("%d %+3.2f %d\\n", '
+                   'spinIndices_rho[1][3], coef_rho[8][1], ip_sigmapi_triangle[127]); return 0; }\n')
+    import subprocess
+    subprocess.check_call(["g++", "-o", str(tmp_path / "t"), str(src), "-I", INCLUDE])
+    out = subprocess.check_output([str(tmp_path / "t")], text=True).split()
+    tabs = T.all_tables()
+    assert out == ["%d" % tabs["spinIndices_rho"][1][3], "%+3.2f" % tabs["coef_rho"][8][1],
+                   "%d" % tabs["ip_sigmapi_triangle"][127]]
