@@ -47,6 +47,12 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time extent (default: the workload's; a smaller value "
                                                               "gives a small case of the same kernels, e.g. for ncu)")
     ap.add_argument("--nev", type=int, default=NEV)
+    ap.add_argument("--configs", type=int, default=1, help="append one timed step of the pi pi (19 pairs), mixed "
+                    "(Nev=128) and reference-kernel workloads to the headline line (0 = skip)")
+    ap.add_argument("--mixed-form", default="sets", choices=["sets", "pairs"],
+                    help="mixed workload: one ctr_rhopi_sigmapi_sets call for the 27 pairs, or calls per pair")
+    ap.add_argument("--pipi-form", default="sets", choices=["sets", "pairs"],
+                    help="pi pi workload: one ctr_pipi_sets call for the 19 momentum sets, or one ctr_pipi per pair")
     ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu", "elementals",
                              "fp64_peak"],
                     help="rho: the headline rho two-point (Nev=100, Lt=64); rho_small: Nev=32, Lt=16 FP64; "
@@ -380,6 +386,7 @@ def main():
         elapsed, launches = timed(lambda: g.launch(stream), args.steps)
         graph_info = {"segments": nseg, "kernels_per_replay": nker, "device_bytes": nbytes,
                       "speedup_vs_eager": t_eager / elapsed}
+        g.close()
     else:
         elapsed, launches = t_eager, launches_eager
     refined = int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
@@ -553,6 +560,17 @@ def main():
         "fp64_engine": fp64, "parity_vs_oracle_sample": parity,
         "split_refined_entries_per_step": refined,
     }
+    if args.configs and ws == 1:
+        # the other chain configurations, each one timed step of its full workload
+        del tau, phi, out
+        torch.cuda.synchronize()
+        line["configs"] = {}
+        for name, fn in (("pipi", pipi_block), ("mixed", mixed_block), ("legacy_gpu", legacy_block)):
+            try:
+                line["configs"][name] = fn(args)
+            except Exception as e:  # recorded, so that the headline line still prints
+                line["configs"][name] = {"error": "%s: %s" % (type(e).__name__, str(e)[:300])}
+            torch.cuda.set_stream(stream)
     print(json.dumps(line))
 
 
@@ -613,17 +631,42 @@ def _timed(fn, steps, warmup):
         fn()
     torch.cuda.synchronize()
     _lib.timing_enable(True)
+    _lib.split_flops(reset=True)
     n0 = _lib.launch_count()
+    stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
+    e0.record(stream)
     for _ in range(steps):
         fn()
-    e1.record()
+    e1.record(stream)
     torch.cuda.synchronize()
     launches = _lib.launch_count() - n0
     rep = _lib.timing_report()
     _lib.timing_enable(False)
-    return e0.elapsed_time(e1) / 1e3 / steps, launches, {k: {"launches": v[0], "ms": v[2]} for k, v in rep.items()}
+    kern = {k: {"launches": v[0], "ms": v[2]} for k, v in rep.items()}
+    mma, prods = _lib.split_flops()
+    kern["_split_work"] = {"mma_flops": mma / steps, "block_products": prods / steps, "steps": steps}
+    return e0.elapsed_time(e1) / 1e3 / steps, launches, kern
+
+
+def chain_roofline(kern, nev):
+    """split_gemm_hp (the chain engine's block GEMMs) against the measured BF16 peak:
+    executed BF16 MMA flops (the library's count, padding included) and the
+    FP64-equivalent rate of the block products (8 Nev^3 each), per step."""
+    w = kern.get("_split_work", {})
+    g = kern.get("split_gemm_hp")
+    if not g or not w.get("mma_flops"):
+        return None
+    t = g["ms"] / 1e3 / max(1, w.get("steps", 1))
+    pk = measured_peaks()
+    peak = pk.get("bf16_tflops", 1924.8)
+    achieved = w["mma_flops"] / t / 1e12
+    return {"kernel": "split_gemm_hp", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "fp64_equivalent_tflops": w["block_products"] * 8.0 * nev ** 3 / t / 1e12,
+            "gemm_ms_per_step": 1e3 * t, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
+            "algorithmic": "executed: 21 bf16 slice-pair products x 8 M N K per tile (the library's launch count); "
+                           "FP64-equivalent: 8 Nev^3 per complex block product"}
 
 
 def _errs(a, b):
@@ -689,7 +732,37 @@ def run_rho_small(args):
 
 def run_pipi(args):
     """pi pi I=0 diagram set (square, double triangle, horizontal double triangle, star,
-    fish) for the 19 momentum pairs (p, -p), |p|^2 <= 2, all 64 x 64 pairs, Nev=100."""
+    fish) for the 19 momentum pairs (p, -p), |p|^2 <= 2, all 64 x 64 pairs, Nev=100.
+    --pipi-form sets (default): all 19 sets in one ctr_pipi_sets call per step;
+    pairs: one ctr_pipi call per momentum pair."""
+    print(json.dumps(pipi_block(args, full=True)))
+
+
+def _entry_gate(got, ref, rows_abs, tol):
+    """Per-entry errors of got against ref, and how many entries miss
+    |err| <= tol |ref| + 2^-44 (sum of the magnitudes of the entry's rows)."""
+    import numpy as np
+    err = np.abs(got - ref)
+    rel = err / np.maximum(np.abs(ref), 1e-300)
+    bound = tol * np.abs(ref) + 2.0 ** -44 * rows_abs
+    return {"entries": int(ref.size), "max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+            "outside_gate": int(np.count_nonzero(err > bound)), "gate": "%.0e |ref| + 2^-44 rows_abs" % tol}
+
+
+def _pipi_rows_abs(d):
+    """Row magnitudes of the oracle's I=0 pi pi entries (weights of lib/contract_kernels_pipi.cu:463-478)."""
+    import numpy as np
+    a = lambda x: np.abs(x).sum(-1)
+    return np.stack([a(d["square"]) / 3, a(d["dtri"]) / 3, a(d["star"][0]) * a(d["star"][1]),
+                     a(d["fish"][0]) * a(d["fish"][1]), 5 * a(d["dtri_hor"]) / 3], axis=-1)
+
+
+def pipi_block(args, full=False):
+    """The pi pi I=0 set over 19 momentum pairs at Nev=100, Lt=64 (one ctr_pipi_sets call
+    per step, or one ctr_pipi call per pair with --pipi-form pairs): eager step with
+    per-kernel times, the step recorded as a CUDA graph and replayed, the block GEMM's
+    roofline, the FP64 engine on a subset, and an oracle sample that is also the CPU
+    baseline of this configuration."""
     import numpy as np
     import torch
     from contractions_code_scattering_gb300 import _lib, api, synth
@@ -699,47 +772,103 @@ def run_pipi(args):
     idx = {p: k for k, p in enumerate(moms)}
     tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
     diag = api.prop_diag(tau)
-    phis = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
-    P = {p: phis[:, idx[p]].contiguous() for p in moms}
-    del phis
+    phi_all = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1).contiguous()
+    P = {p: phi_all[:, idx[p]].contiguous() for p in moms}
     pairs = [(p, _neg(p)) for p in moms]
-
+    sets = [(idx[a], idx[b], idx[a], idx[b]) for a, b in pairs]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    form = args.pipi_form
     refined = [0]
 
-    def step(engine, rows=None, plist=pairs):
+    def step(engine, rows=None, plist=None, out=None):
         tr = rows if rows is not None else (0, nt)
         tb = tau[tr[0]:tr[1]]
-        out = []
         refined[0] = 0
-        for a, b in plist:
-            out.append(api.run_contract_pipi(tb, diag, P[a], P[b], P[a], P[b], 0, engine=engine, tf_range=tr))
+        if form == "sets":
+            sl = sets if plist is None else [sets[pairs.index(p)] for p in plist]
+            o = api.run_contract_pipi_sets(tb, diag, phi_all, sl, 0, engine=engine, tf_range=tr, out=out)
             refined[0] += int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
-        return out
+            return o
+        res = []
+        for a, b in (pairs if plist is None else plist):
+            res.append(api.run_contract_pipi(tb, diag, P[a], P[b], P[a], P[b], 0, engine=engine, tf_range=tr))
+            refined[0] += int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
+        return torch.stack(res)
 
-    t, launches, kern = _timed(lambda: step("split"), args.steps, args.warmup)
+    steps, warm = (args.steps, args.warmup) if full else (1, 1)
+    out = torch.empty((len(sets), nt, nt, 5), dtype=torch.complex128, device="cuda")
+    t, launches, kern = _timed(lambda: step("split", out=out if form == "sets" else None), steps, warm)
     refined_step = refined[0]
     diagrams = nt * nt * len(pairs) * 5
+    res = {"workload": "pipi I=0 set, Nev=100, Lt=64, 19 momentum pairs (p,-p) |p|^2<=2, all 64x64 (t_src,t_sink)",
+           "metric": "diagrams/s @Nev=100,Lt=64: pi pi I=0 set, 19 momentum pairs, split-TC",
+           "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t, "steps": steps, "warmup": warm,
+           "form": form, "diagrams_per_step": diagrams, "gpu_launches": launches,
+           "split_refined_entries_per_step": refined_step, "roofline": chain_roofline(kern, nev),
+           "kernels": {k: v for k, v in kern.items() if not k.startswith("_")}}
+    got = (out if form == "sets" else step("split")).cpu().numpy()
+    if form == "sets":
+        # the same step recorded once as a CUDA graph and replayed
+        with api.Graph(stream) as g:
+            step("split", out=out)
+        g.launch(stream)
+        torch.cuda.synchronize()
+        nseg, nker, nbytes = g.info()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.launch(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tg = e0.elapsed_time(e1) / 1e3
+        same = bool(np.array_equal(out.cpu().numpy(), got))
+        g.close()
+        res["graph"] = {"value": diagrams / tg, "ms_per_step": 1e3 * tg, "segments": nseg, "kernels_per_replay": nker,
+                        "device_bytes": nbytes, "speedup_vs_eager": t / tg, "bitwise_equal_to_eager": same}
+    # the plain FP64 engine and per-entry errors on a subset: one momentum pair, t_sink 0..3
     sub_pairs, sub_rows = [((1, 0, 0), (-1, 0, 0))], (0, 4)
     sub_diag = (sub_rows[1] - sub_rows[0]) * nt * len(sub_pairs) * 5
-    t64, _, k64 = _timed(lambda: step("fp64", sub_rows, sub_pairs), 1, 1)
-    ts, _, _ = _timed(lambda: step("split", sub_rows, sub_pairs), 1, 1)
-    a = step("split", sub_rows, sub_pairs)[0].cpu().numpy()
-    b = step("fp64", sub_rows, sub_pairs)[0].cpu().numpy()
-    line = {"workload": "pipi", "metric": "diagrams/s @Nev=100,Lt=64: pi pi I=0 set, 19 momentum pairs, split-TC",
-            "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t, "steps": args.steps,
-            "warmup": args.warmup, "diagrams_per_step": diagrams, "gpu_launches": launches, "kernels": kern,
-            "split_refined_entries_per_step": refined_step,
-            "fp64_subset": {"sample": "momentum pair (1,0,0)/(-1,0,0), t_sink 0..3, all t_src (%d diagrams)" % sub_diag,
-                            "fp64_diagrams_per_s": sub_diag / t64, "split_diagrams_per_s": sub_diag / ts,
-                            "split_speedup": t64 / ts, "split_vs_fp64_rel_err": _errs(a, b), "fp64_kernels": k64}}
-    print(json.dumps(line))
+    t64, _, _ = _timed(lambda: step("fp64", sub_rows, plist=sub_pairs), 1, 1)
+    b = step("fp64", sub_rows, plist=sub_pairs).cpu().numpy()[0]
+    a = got[sets.index(sets[pairs.index(sub_pairs[0])])][sub_rows[0]:sub_rows[1]]
+    res["fp64_subset"] = {"sample": "momentum pair (1,0,0)/(-1,0,0), t_sink 0..3, all t_src (%d diagrams)" % sub_diag,
+                          "fp64_diagrams_per_s": sub_diag / t64,
+                          "split_speedup": (sub_diag / t64) and (diagrams / t) / (sub_diag / t64),
+                          "split_vs_fp64_rel_err": _errs(a, b)}
+    # oracle sample (also this configuration's CPU baseline): the same pair, t_sink 0, t_src 0..7;
+    # these entries involve only time slices below 8, so the oracle runs on that sub-lattice
+    try:
+        from oracle import pyoracle as O
+        k8 = min(8, nt)
+        p1, p2 = sub_pairs[0]
+        sub_prop = tau[:k8, :k8].cpu().numpy()
+        ph = {p: P[p][:k8].cpu().numpy() for p in (p1, p2)}
+        t0 = time.perf_counter()
+        d = O.pipi_row(sub_prop, ph[p1], ph[p2], ph[p1], ph[p2], 0, 0)
+        tcpu = time.perf_counter() - t0
+        k = pairs.index(sub_pairs[0])
+        res["vs_oracle"] = {"sample": "pair (1,0,0)/(-1,0,0), t_sink 0, t_src 0..%d" % (k8 - 1),
+                            "split": _entry_gate(got[k][0, :k8], d["corr"], _pipi_rows_abs(d), 1e-9),
+                            "fp64": _entry_gate(b[0, :k8], d["corr"], _pipi_rows_abs(d), 1e-12)}
+        res["cpu_baseline"] = {"value": k8 * 5 / tcpu, "unit": "diagrams/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "the oracle sample above (%d entries, reference chain order)" % (k8 * 5)}
+    except Exception as e:  # the oracle library is not built
+        res["vs_oracle"] = {"unavailable": str(e)[:200]}
+    del tau, diag, phi_all, P, out
+    torch.cuda.synchronize()
+    return res
 
 
 def run_mixed(args):
     """Mixed cross-correlator batch at Nev=128, Lt=48, decay 0.25: for each of the 27
     momenta |p|^2 <= 3, rho -> pi pi (3 polarisations x 4 operators) and sigma -> pi pi
     (triangle x 2 operators, horizontal fish) with the pion pair (p, -p), plus the
-    sigma one-fish loops; split engine."""
+    sigma one-fish loops; split engine.  --mixed-form sets (default): one
+    ctr_rhopi_sigmapi_sets call for the 27 pairs; pairs: per-pair ctr_rhopi / ctr_sigmapi."""
+    print(json.dumps(mixed_block(args, full=True)))
+
+
+def mixed_block(args, full=False):
     import numpy as np
     import torch
     from contractions_code_scattering_gb300 import _lib, api, synth
@@ -749,9 +878,8 @@ def run_mixed(args):
     idx = {p: k for k, p in enumerate(moms)}
     tau = synth.make_prop(nt, nev, seed=SEED, decay=0.25, backend="torch")
     diag = api.prop_diag(tau)
-    phis = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1)
-    P = {p: phis[:, idx[p]].contiguous() for p in moms}
-    del phis
+    phi_all = synth.make_phi_momenta_torch(nt, nev, moms, seed=SEED + 1).contiguous()
+    P = {p: phi_all[:, idx[p]].contiguous() for p in moms}
     g = torch.Generator(device="cuda")
     g.manual_seed(SEED + 2)
     sd = float(np.sqrt(0.5 / nev))
@@ -759,46 +887,106 @@ def run_mixed(args):
                         torch.randn((nt, 5, nev, nev), generator=g, device="cuda", dtype=torch.float64) * sd)
     mom5 = ops.contiguous()
     mom2 = ops[:, :2].contiguous()
-
+    sets = [(idx[p], idx[_neg(p)]) for p in moms]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    form = args.mixed_form
     refined = [0]
 
-    def count():
-        refined[0] += int(_lib.lib().ctr_split_refined())
-
     def step(engine, plist=moms, rows=None):
+        """[rhopi (set, idir, rows, Nt, 4), triangle (set, rows, Nt, 2), hor_fish (set, Nt)], loops (2, Nt)"""
         tr = rows if rows is not None else (0, nt)
         tb = tau[tr[0]:tr[1]]
-        out = []
         refined[0] = 0
-        for p in plist:
-            for idir in range(3):
-                out.append(api.run_contract_rhopi(tb, diag, P[p], P[_neg(p)], mom5, idir, engine=engine, tf_range=tr))
-                count()
-            hf, tri = api.run_contract_sigmapi(tb, diag, P[p], P[_neg(p)], mom2, engine=engine, tf_range=tr)
-            count()
-            out += [tri, hf]
-        for k in range(2):
-            out.append(api.run_contract_loop_unity(diag, mom2[:, k].contiguous(), engine=engine))
-        return out
+        if form == "sets":
+            sl = [sets[moms.index(p)] for p in plist]
+            o = api.run_contract_rhopi_sigmapi_sets(tb, diag, phi_all, sl, mom5, mom2, engine=engine, tf_range=tr)
+            refined[0] += int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
+            res = [o["rhopi"], o["triangle"], o["hor_fish"]]
+        else:
+            rp, tri, hf = [], [], []
+            for p in plist:
+                rp.append(torch.stack([api.run_contract_rhopi(tb, diag, P[p], P[_neg(p)], mom5, idir, engine=engine,
+                                                              tf_range=tr) for idir in range(3)]))
+                refined[0] += int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
+                h, t = api.run_contract_sigmapi(tb, diag, P[p], P[_neg(p)], mom2, engine=engine, tf_range=tr)
+                refined[0] += int(_lib.lib().ctr_split_refined()) if engine == "split" else 0
+                tri.append(t)
+                hf.append(h)
+            res = [torch.stack(rp), torch.stack(tri), torch.stack(hf)]
+        loops = torch.stack([api.run_contract_loop_unity(diag, mom2[:, k].contiguous(), engine=engine)
+                             for k in range(2)])
+        return res + [loops]
 
-    t, launches, kern = _timed(lambda: step("split"), args.steps, args.warmup)
+    steps, warm = (args.steps, args.warmup) if full else (1, 1)
+    holder = {}
+    t, launches, kern = _timed(lambda: holder.__setitem__("r", step("split")), steps, warm)
     refined_step = refined[0]
     diagrams = nt * nt * len(moms) * (12 + 2) + nt * len(moms) + 2 * nt
-    sub = [(1, 1, 1)]
-    rows = (0, 4)
-    t64, _, _ = _timed(lambda: step("fp64", sub, rows), 1, 1)
-    ts, _, _ = _timed(lambda: step("split", sub, rows), 1, 1)
-    a = np.concatenate([x.cpu().numpy().ravel() for x in step("split", sub, rows)])
-    b = np.concatenate([x.cpu().numpy().ravel() for x in step("fp64", sub, rows)])
+    res = {"workload": "mixed: rho->pipi (3 polarisations x 4 operators) + sigma->pipi (triangle x 2, horizontal "
+                       "fish) for 27 pion pairs (p,-p) |p|^2<=3, + 2 sigma loops; Nev=128, Lt=48",
+           "metric": "diagrams/s @Nev=128,Lt=48: rho-pipi + sigma-pipi + sigma loops, 27 momenta, split-TC",
+           "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t, "steps": steps, "warmup": warm,
+           "form": form, "diagrams_per_step": diagrams, "gpu_launches": launches,
+           "split_refined_entries_per_step": refined_step, "roofline": chain_roofline(kern, nev),
+           "kernels": {k: v for k, v in kern.items() if not k.startswith("_")}}
+    got = [x.cpu().numpy() for x in holder["r"]]
+    if form == "sets":
+        with api.Graph(stream) as gr:
+            holder["g"] = step("split")
+        gr.launch(stream)
+        torch.cuda.synchronize()
+        nseg, nker, nbytes = gr.info()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        gr.launch(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tg = e0.elapsed_time(e1) / 1e3
+        same = all(np.array_equal(a.cpu().numpy(), b) for a, b in zip(holder["g"], got))
+        gr.close()
+        res["graph"] = {"value": diagrams / tg, "ms_per_step": 1e3 * tg, "segments": nseg, "kernels_per_replay": nker,
+                        "device_bytes": nbytes, "speedup_vs_eager": t / tg, "bitwise_equal_to_eager": same}
+    # FP64 engine on a subset: momentum (1,1,1), t_sink 0..3, all t_src
+    sub, rows = [(1, 1, 1)], (0, 4)
+    k1 = moms.index(sub[0])
     sub_diag = (rows[1] - rows[0]) * nt * 14 + nt + 2 * nt
-    line = {"workload": "mixed", "metric": "diagrams/s @Nev=128,Lt=48: rho-pipi + sigma-pipi + sigma loops, "
-            "27 momenta, split-TC", "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t,
-            "steps": args.steps, "warmup": args.warmup, "diagrams_per_step": diagrams, "gpu_launches": launches,
-            "kernels": kern, "split_refined_entries_per_step": refined_step,
-            "fp64_subset": {"sample": "momentum (1,1,1), t_sink 0..3, all t_src (%d diagrams)" % sub_diag,
-                            "fp64_diagrams_per_s": sub_diag / t64, "split_diagrams_per_s": sub_diag / ts,
-                            "split_speedup": t64 / ts, "split_vs_fp64_rel_err": _errs(a, b)}}
-    print(json.dumps(line))
+    t64, _, _ = _timed(lambda: holder.__setitem__("f", step("fp64", sub, rows)), 1, 1)
+    f = [x.cpu().numpy() for x in holder["f"]]
+    a = np.concatenate([got[0][k1][:, rows[0]:rows[1]].ravel(), got[1][k1][rows[0]:rows[1]].ravel(),
+                        got[2][k1].ravel(), got[3].ravel()])
+    b = np.concatenate([f[0][0].ravel(), f[1][0].ravel(), f[2][0].ravel(), f[3].ravel()])
+    res["fp64_subset"] = {"sample": "momentum (1,1,1), t_sink 0..3, all t_src (%d diagrams)" % sub_diag,
+                          "fp64_diagrams_per_s": sub_diag / t64,
+                          "split_speedup": (diagrams / t) / (sub_diag / t64), "split_vs_fp64_rel_err": _errs(a, b)}
+    # oracle sample (also this configuration's CPU baseline): rho -> pi pi idir 0 and the
+    # triangle for (1,1,1), t_sink 0, t_src 0..3 (sub-lattice t < 4)
+    try:
+        from oracle import pyoracle as O
+        k4 = min(4, nt)
+        p1, p2 = P[sub[0]][:k4].cpu().numpy(), P[_neg(sub[0])][:k4].cpu().numpy()
+        sp = tau[:k4, :k4].cpu().numpy()
+        m5, m2 = mom5[:k4].cpu().numpy(), mom2[:k4].cpu().numpy()
+        t0 = time.perf_counter()
+        r1, c1 = O.rhopi_row(sp, p1, p2, m5, 0, 0)
+        r2, c2 = O.sigmapi_triangle_row(sp, p1, p2, m2, 0)
+        tcpu = time.perf_counter() - t0
+        ab1 = np.abs(r1).reshape(k4, 4, 64).sum(-1)
+        ab2 = np.abs(r2).reshape(k4, 2, 64).sum(-1)
+        res["vs_oracle"] = {"sample": "(1,1,1): rho->pipi idir 0 and triangle, t_sink 0, t_src 0..%d" % (k4 - 1),
+                            "split": _entry_gate(np.concatenate([got[0][k1][0, 0, :k4].ravel(), got[1][k1][0, :k4].ravel()]),
+                                                 np.concatenate([c1.ravel(), c2.ravel()]),
+                                                 np.concatenate([ab1.ravel(), ab2.ravel()]), 1e-9),
+                            "fp64": _entry_gate(np.concatenate([f[0][0][0, 0, :k4].ravel(), f[1][0][0, :k4].ravel()]),
+                                                np.concatenate([c1.ravel(), c2.ravel()]),
+                                                np.concatenate([ab1.ravel(), ab2.ravel()]), 1e-12)}
+        res["cpu_baseline"] = {"value": k4 * 6 / tcpu, "unit": "diagrams/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "the oracle sample above (%d entries, reference chain order)" % (k4 * 6)}
+    except Exception as e:
+        res["vs_oracle"] = {"unavailable": str(e)[:200]}
+    del tau, diag, phi_all, P, ops, mom5, mom2, holder
+    torch.cuda.synchronize()
+    return res
 
 
 def run_adjoint(args):
@@ -856,6 +1044,10 @@ def run_adjoint(args):
 
 
 def run_legacy_gpu(args):
+    print(json.dumps(legacy_block(args)))
+
+
+def legacy_block(args):
     """The reference's own rho kernel (lib/contract_kernels_rho.cu built unmodified for
     sm_103a: CUDA-core FP64, 25x25 tiles, one launch of 768 spin-row blocks per
     (t_sink, t_src)) against both engines on the same workload: Nev=100, Lt=64, one
@@ -867,8 +1059,7 @@ def run_legacy_gpu(args):
     from oracle import refkernels as RK
     from oracle import tables as TB
     if not os.path.exists(RK.cubin("rho")):
-        print(json.dumps({"workload": "legacy_gpu", "unavailable": "reference cubins not built (oracle/build_ref.sh)"}))
-        return
+        return {"workload": "legacy_gpu", "unavailable": "reference cubins not built (oracle/build_ref.sh)"}
     api.device_init(0)
     nt, nev = 64, 100
     tau = synth.make_prop(nt, nev, seed=SEED, decay=0.35, backend="torch")
@@ -915,7 +1106,9 @@ def run_legacy_gpu(args):
             "fp64_engine": res["fp64"], "split_engine": res["split"],
             "split_vs_reference_kernel": res["split"]["diagrams_per_s"] / ref_rate,
             "fp64_vs_reference_kernel": res["fp64"]["diagrams_per_s"] / ref_rate}
-    print(json.dumps(line))
+    del tau, mom5, tmp1, tmp2, out
+    torch.cuda.synchronize()
+    return line
 
 
 def run_elementals(args):

@@ -52,6 +52,8 @@ def lib(build_if_missing=True):
     L.ctr_split_levels.argtypes = [i, vp, vp, vp, vp]
     L.ctr_rhopi.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp]
     L.ctr_pipi.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.ctr_pipi_sets.argtypes = [i, i, i, i, i, i, vp, vp, vp, i, i, vp, vp, vp]
+    L.ctr_rhopi_sigmapi_sets.argtypes = [i, i, i, i, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, vp, vp]
     L.ctr_loop_unity.argtypes = [i, i, i, vp, vp, vp, vp]
     L.ctr_sigmapi.argtypes = [i, i, i, i, i, vp, vp, vp, vp, vp, vp, vp, vp]
     L.ctr_split_available.restype = i
@@ -65,6 +67,7 @@ def lib(build_if_missing=True):
     L.ctr_wait_probe.argtypes = [i, vp]
     L.ctr_split_set_refine.argtypes = [d]
     L.ctr_split_refined.restype = ctypes.c_longlong
+    L.ctr_split_flops.argtypes = [ctypes.POINTER(d), ctypes.POINTER(d), i]
     L.ctr_apply_profile.argtypes = [i, ctypes.c_longlong, vp, vp, vp, vp]
     L.ctr_chain_adjoint.argtypes = [i, i, i, i, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]
     L.ctr_rho_profile_vjp.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp, vp]
@@ -124,3 +127,11 @@ def timing_report():
     buf = ctypes.create_string_buffer(1 << 16)
     check(lib().ctr_timing_report(buf, len(buf)))
     return {k: tuple(v) for k, v in json.loads(buf.value.decode()).items()}
+
+
+def split_flops(reset=False):
+    """(executed BF16 MMA flops, complex block products) of the split engine's eager
+    launches since the last reset (include/ctr.h: ctr_split_flops)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(lib().ctr_split_flops(ctypes.byref(a), ctypes.byref(b), 1 if reset else 0))
+    return a.value, b.value

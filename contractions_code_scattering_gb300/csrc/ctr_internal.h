@@ -108,6 +108,11 @@ int reorder_prop_device(int N, int Nt, const double* file_payload, int single, v
 // tolerance (0 = off) and the number of entries the last split call recomputed.
 extern double g_refine_tol;
 extern long long g_refined_last;
+// Work of the split engine's launches since the last reset (ctr_split_flops): BF16
+// MMA flops the tensor cores executed (padding included) and the Nev x Nev complex
+// block products they computed (8 Nev^3 FP64-equivalent flops each).  Counted by
+// eager launches; replays of recorded graphs are not counted.
+extern double g_split_mma_flops, g_split_products;
 
 // Reads (and clears) the device-side error flag of the split engine; syncs the stream.
 int split_error_check(cudaStream_t s);
@@ -119,6 +124,21 @@ int zgemm_split_batched(int N, int nb, const double* const* x, const double* con
 // engine: C = sum_q w_q op(A_q) op(B_q) with real power-of-two weights.
 struct ZTask;
 int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream);
+
+// A grid of block products that share their right side:
+//   C(s, j) = sum_{q < nterm} w_q op(A[s * nterm + q]) op(B[j][q]),  s < nslab, j < nb <= 8,
+// written at C0[j] + s * Nev^2 (the slabs' outputs of one right block are
+// consecutive blocks).  op: conjugate transpose where bit q of adag / bit 4j+q of
+// bdag is set.  On the split engine the slabs stack along M, so that 128-row
+// tiles carry no padding rows between them; weights must be real powers of two.
+struct GridTask {
+  std::vector<const double2*> A;
+  const double2* B[8][4];
+  double2* C0[8];
+  float w[4];
+  int nslab, nb, nterm, adag, bdag;
+};
+int zgemm_split_grids(int N, const std::vector<GridTask>& grids, cudaStream_t stream);
 
 // ------------------------------------------------------------ graph capture
 // A host step that reads device results (e.g. the split engine's refinement

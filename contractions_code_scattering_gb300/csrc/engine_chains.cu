@@ -19,6 +19,8 @@
 // the batched FP64 GEMM (up to 4 accumulated terms with the gamma_5 signs).
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <utility>
 
 #include "kernels.h"
 
@@ -60,6 +62,29 @@ int run_traces(const Ctx& c, const std::vector<TraceTask>& t) {
   void* d;
   CTR_TRY(upload(WS_ROWTASKS, t.data(), t.size() * sizeof(TraceTask), &d, c.s));
   return launch_trace_f64((const TraceTask*)d, (int)t.size(), c.N, c.s);
+}
+
+// A stage of block grids: the split engine stacks each grid's slabs along M; the
+// FP64 engine runs them as plain tasks.
+int run_grids(const Ctx& c, const std::vector<GridTask>& g, int slot) {
+  if (g.empty()) return CTR_OK;
+  if (c.engine == CTR_ENGINE_SPLIT) return zgemm_split_grids(c.N, g, c.s);
+  std::vector<ZTask> t;
+  for (const GridTask& G : g)
+    for (int sl = 0; sl < G.nslab; sl++)
+      for (int j = 0; j < G.nb; j++) {
+        ZTask z{};
+        for (int q = 0; q < G.nterm; q++) {
+          z.A[q] = G.A[(size_t)sl * G.nterm + q];
+          z.B[q] = G.B[j][q];
+          z.wre[q] = G.w[q];
+        }
+        z.nterm = G.nterm;
+        z.flags = G.adag | (((G.bdag >> (4 * j)) & 0xF) << 4);
+        z.C = G.C0[j] + (size_t)sl * c.N2;
+        t.push_back(z);
+      }
+  return run_stage(c, t, slot);
 }
 
 inline TraceTask tr(const double2* X, const double2* Y, double2* out, float cre, float cim, int mode) {
@@ -229,9 +254,11 @@ int batch_pairs(size_t per_pair, int npairs) {
 }  // namespace
 
 // ------------------------------------------------------------------ pi pi
+// pstride: elementals of consecutive time slices are pstride blocks apart (1 for
+// [Nt][N][N] arrays; nphi for one momentum of a [Nt][nphi][N][N] array).
 int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* prop_rows, const double* prop_diag,
               const double* p1, const double* p2, const double* p3, const double* p4, double* corr, cudaStream_t s,
-              int engine, const std::vector<int>* plist) {
+              int engine, const std::vector<int>* plist, size_t pstride = 1) {
   Ctx c{N, Nt, (size_t)N * N, s, engine};
   if (engine == CTR_ENGINE_SPLIT && !plist) g_refined_last = 0;
   const size_t N2 = c.N2, blk16 = 16 * N2;
@@ -249,9 +276,9 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
   void* pt;
   CTR_TRY(workspace(WS_PHI).get(4 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *L = (double2*)pt, *Rsq = L + Nt * blk16, *Rdt = Rsq + Nt * blk16, *tmp = Rdt + Nt * blk16;
-  CTR_TRY(per_t_chain(c, diag, P3, N2, P4, N2, tmp, L, &need_tf));
-  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, Rsq, &need_ti));
-  CTR_TRY(per_t_chain(c, diag, P1, N2, P2, N2, tmp, Rdt, &need_ti));
+  CTR_TRY(per_t_chain(c, diag, P3, pstride * N2, P4, pstride * N2, tmp, L, &need_tf));
+  CTR_TRY(per_t_chain(c, diag, P2, pstride * N2, P1, pstride * N2, tmp, Rsq, &need_ti));
+  CTR_TRY(per_t_chain(c, diag, P1, pstride * N2, P2, pstride * N2, tmp, Rdt, &need_ti));
 
   // per pair: X, Ysq, Ydt, V1, Pm, V2, Qm, F, G (16 blocks each), U3, U4, W1, W2
   const int nbuf = 13;
@@ -283,13 +310,13 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
       for (int b = 0; b < 16; b++) {
         const double2* tb = T + b * N2;
         if (iso == 0) {
-          st1.push_back(zt(tb, P1 + ti * N2, V1 + b * N2));  // V1 = T Phi1
-          st1.push_back(zt(tb, P2 + ti * N2, V2 + b * N2));  // V2 = T Phi2
+          st1.push_back(zt(tb, P1 + ti * pstride * N2, V1 + b * N2));  // V1 = T Phi1
+          st1.push_back(zt(tb, P2 + ti * pstride * N2, V2 + b * N2));  // V2 = T Phi2
         }
-        st1.push_back(zt(P3 + tf * N2, tb, U3 + b * N2));       // U3 = Phi3 tau_b
-        st1.push_back(zt(P4 + tf * N2, tb, U4 + b * N2));       // U4 = Phi4 tau_b
-        st1.push_back(zt(P1 + ti * N2, tb, W1 + b * N2, 1 << 4));  // W1 = Phi1 tau_b^dag
-        st1.push_back(zt(P2 + ti * N2, tb, W2 + b * N2, 1 << 4));  // W2 = Phi2 tau_b^dag
+        st1.push_back(zt(P3 + tf * pstride * N2, tb, U3 + b * N2));       // U3 = Phi3 tau_b
+        st1.push_back(zt(P4 + tf * pstride * N2, tb, U4 + b * N2));       // U4 = Phi4 tau_b
+        st1.push_back(zt(P1 + ti * pstride * N2, tb, W1 + b * N2, 1 << 4));  // W1 = Phi1 tau_b^dag
+        st1.push_back(zt(P2 + ti * pstride * N2, tb, W2 + b * N2, 1 << 4));  // W2 = Phi2 tau_b^dag
       }
       block_gemm_g5(c, X, Rs, Ysq, st2);  // Ysq = X G Rsq
       block_gemm_g5(c, X, Rd, Ydt, st2);  // Ydt = X G Rdt
@@ -313,8 +340,8 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
             st2.push_back(zq);
           }
         for (int b = 0; b < 16; b++) {
-          st3.push_back(zt(P3 + tf * N2, Pm + b * N2, F + b * N2));   // F = Phi3 P
-          st3.push_back(zt(P4 + tf * N2, Qm + b * N2, Gm + b * N2));  // G = Phi4 Q
+          st3.push_back(zt(P3 + tf * pstride * N2, Pm + b * N2, F + b * N2));   // F = Phi3 P
+          st3.push_back(zt(P4 + tf * pstride * N2, Qm + b * N2, Gm + b * N2));  // G = Phi4 Q
         }
       }
       double2* o = TR + (size_t)q * ntr;
@@ -348,7 +375,538 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
   return refine_end(c, rf, 5, WS_REFINE, (double2*)corr,
                     [=](const std::vector<int>& pairs, double2* out, cudaStream_t ls) {
                       return pipi_chain(N, Nt, tf_begin, tf_end, iso, prop_rows, prop_diag, p1, p2, p3, p4,
-                                        (double*)out, ls, CTR_ENGINE_FP64, &pairs);
+                                        (double*)out, ls, CTR_ENGINE_FP64, &pairs, pstride);
+                    });
+}
+
+// ------------------------------------------------ pi pi over momentum sets
+// One call for many momentum sets (P1..P4 chosen from one elemental array).
+// The per-time-slice products Phi_a taud Phi_b are computed once per (a, b) the
+// sets use.  Per batch of (t_sink, t_src) pairs, source time major, every
+// product is planned once: those several sets share -- Phi(q) tau_b,
+// Phi(q) tau_b^dag, tau_b Phi(q), tau Phi(q) tau^dag, Phi(q') tau Phi(q) tau^dag
+// and the star / fish twin traces, which the sets (p, -p) and (-p, p) have in
+// common -- are keyed by elemental index.  Each stage is a list of block grids
+// (GridTask): products with the same right operand -- Phi(q) for every q
+// against tau_b, every row block of X for all pairs of one t_src against R(t_src)
+// -- form the slabs of one grid, which the split engine stacks along M.
+
+namespace {
+
+// Bump allocation of Nev x Nev product blocks inside one workspace buffer; with
+// no buffer it only counts (a dry run that sizes the batches).
+struct Arena {
+  double2* base = nullptr;
+  size_t used = 0, cap = 0, N2 = 0;
+  double2* block() {
+    const size_t o = used;
+    used += N2;
+    if (!base) return (double2*)(uintptr_t)(sizeof(double2) * (o + 1));  // stand-in address, same spacing
+    return o + N2 <= cap ? base + o : nullptr;
+  }
+};
+
+struct TaskKey {
+  const double2* a[4];
+  const double2* b[4];
+  float wre[4], wim[4];
+  int nterm, flags;
+  bool operator<(const TaskKey& o) const { return std::memcmp(this, &o, sizeof(TaskKey)) < 0; }
+};
+
+// Stages of block products with hash-consing: an identical task (operands,
+// weights, transposes) returns the block computed by its first occurrence.
+struct Planner {
+  Arena ar;
+  std::vector<ZTask> st[4];
+  std::map<TaskKey, double2*> memo;
+  bool overflow = false;
+  double2* task(int stage, const ZTask& z) {
+    TaskKey k;
+    std::memset(&k, 0, sizeof(k));
+    for (int q = 0; q < z.nterm; q++) {
+      k.a[q] = z.A[q];
+      k.b[q] = z.B[q];
+      k.wre[q] = z.wre[q];
+      k.wim[q] = z.wim[q];
+    }
+    k.nterm = z.nterm;
+    k.flags = z.flags;
+    auto it = memo.find(k);
+    if (it != memo.end()) return it->second;
+    double2* c = ar.block();
+    if (!c) {
+      overflow = true;
+      return nullptr;
+    }
+    ZTask t = z;
+    t.C = c;
+    st[stage].push_back(t);
+    memo.emplace(k, c);
+    return c;
+  }
+};
+
+// Closing traces of a batch; add() returns the slot of the value.
+struct TracePlan {
+  std::vector<TraceTask> tt;
+  int add(const double2* x, const double2* y, float cre, float cim, int mode) {
+    tt.push_back(tr(x, y, nullptr, cre, cim, mode));
+    return (int)tt.size() - 1;
+  }
+};
+
+// (set, pair) item of a pi pi batch: 112 trace slots in the layout of
+// pipi_combine_kernel, combined into corr[ent * 5 ..].
+__global__ void pipi_combine_sets_kernel(const double2* __restrict__ trv, const double* __restrict__ trabs,
+                                         const int* __restrict__ slots, const int* __restrict__ ent, int nitem, int iso,
+                                         double2* __restrict__ corr, double eps_over_tol, int* __restrict__ count,
+                                         int* __restrict__ list) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= nitem) return;
+  const int* sl = slots + (size_t)it * 112;
+  double2 sum[7];
+  double ab[7];
+  for (int g = 0; g < 7; g++) {
+    double re = 0, im = 0, a = 0;
+    for (int k = 0; k < 16; k++) {
+      const int j = sl[g * 16 + k];
+      if (j < 0) continue;
+      re += trv[j].x;
+      im += trv[j].y;
+      if (trabs) a += trabs[j];
+    }
+    sum[g] = make_double2(re, im);
+    ab[g] = a;
+  }
+  const double2 star = cmul(sum[3], sum[4]);
+  const double2 fish = cmul(sum[5], sum[6]);
+  double2* o = corr + (size_t)ent[it] * 5;
+  if (iso == 1) {  // lib/contract_kernels_pipi.cu:288-303
+    o[0] = make_double2(-2. * sum[0].x, -2. * sum[0].y);
+    o[1] = make_double2(2. * sum[1].x, 2. * sum[1].y);
+    o[2] = make_double2(-star.x, -star.y);
+    o[3] = fish;
+    o[4] = make_double2(0., 0.);
+  } else {  // lib/contract_kernels_pipi.cu:463-478
+    o[0] = make_double2((-1. / 3.) * sum[0].x, (-1. / 3.) * sum[0].y);
+    o[1] = make_double2(-(1. / 3.) * sum[1].x, -(1. / 3.) * sum[1].y);
+    o[2] = star;
+    o[3] = fish;
+    o[4] = make_double2(-(5. / 3.) * sum[2].x, -(5. / 3.) * sum[2].y);
+  }
+  if (trabs && eps_over_tol > 0.0) {
+    auto mag = [](double2 v) { return sqrt(v.x * v.x + v.y * v.y); };
+    const double w[3] = {iso == 1 ? 2.0 : 1.0 / 3.0, iso == 1 ? 2.0 : 1.0 / 3.0, iso == 1 ? 0.0 : 5.0 / 3.0};
+    const double scale[5] = {w[0] * ab[0], w[1] * ab[1], mag(sum[3]) * ab[4] + mag(sum[4]) * ab[3],
+                             mag(sum[5]) * ab[6] + mag(sum[6]) * ab[5], w[2] * ab[2]};
+    for (int k = 0; k < 5; k++)
+      if (!(scale[k] * eps_over_tol <= mag(o[k])) || (scale[k] == 0.0 && mag(o[k]) > 0.0)) {
+        list[atomicAdd(count, 1)] = ent[it] * 5 + k;
+        break;
+      }
+  }
+}
+
+// Scratch budget of a set batch: 16 GB, or an eighth of the device's memory where less.
+size_t sets_budget() {
+  static size_t b = 0;
+  if (!b && !capturing()) {
+    size_t fr = 0, tot = 0;
+    b = cudaMemGetInfo(&fr, &tot) == cudaSuccess ? std::min<size_t>((size_t)16 << 30, tot / 8) : ((size_t)6 << 30);
+  }
+  return b ? b : ((size_t)6 << 30);
+}
+
+}  // namespace
+
+// Per time slice: M(a, b, t) = Phi_a(t) taud(t) Phi_b(t), 16 consecutive blocks at
+// M[combo * Nt + t], for the (a, b) combos and the t flagged in need; Phi_a(t)
+// taud(t)_blk is computed once for all combos with the same a.  phi [Nt][nphi][N][N].
+int per_t_sets(const Ctx& c, const double2* diag, const double2* ph, int nphi,
+               const std::vector<std::pair<int, int>>& combos, const std::vector<std::vector<char>>& need,
+               std::vector<const double2*>& M) {
+  const int Nt = c.Nt;
+  const size_t N2 = c.N2, blk16 = 16 * N2;
+  auto P = [&](int q, int t) { return ph + ((size_t)t * nphi + q) * N2; };
+  M.assign(combos.size() * Nt, nullptr);
+  size_t nblk = 0;
+  for (int pass = 0; pass < 2; pass++) {  // a dry run for the size, then the plan
+    Planner pl;
+    pl.ar.N2 = N2;
+    if (pass == 1) {
+      void* mem;
+      CTR_TRY(workspace(WS_PHI).get(nblk * N2 * sizeof(double2), &mem));
+      pl.ar.base = (double2*)mem;
+      pl.ar.cap = nblk * N2;
+    }
+    std::vector<const double2*> tmp(combos.size() * Nt * 16, nullptr);
+    for (size_t ci = 0; ci < combos.size(); ci++)
+      for (int t = 0; t < Nt; t++)
+        if (need[ci][t])
+          for (int b = 0; b < 16; b++)
+            tmp[(ci * Nt + t) * 16 + b] =
+                pl.task(0, zt(P(combos[ci].first, t), diag + (size_t)t * blk16 + b * N2, nullptr));
+    for (size_t ci = 0; ci < combos.size(); ci++)
+      for (int t = 0; t < Nt; t++) {
+        if (!need[ci][t]) continue;
+        double2* first = nullptr;
+        for (int b = 0; b < 16; b++) {
+          double2* out = pl.task(1, zt(tmp[(ci * Nt + t) * 16 + b], P(combos[ci].second, t), nullptr));
+          if (b == 0) first = out;
+          if (!pl.overflow && out != first + b * N2)
+            return fail(CTR_ERR_ARG, "per-time-slice products not consecutive");
+        }
+        M[ci * Nt + t] = first;
+      }
+    if (pl.overflow) return fail(CTR_ERR_ALLOC, "per-time-slice arena overflow");
+    if (pass == 0) {
+      nblk = pl.ar.used / N2;
+      continue;
+    }
+    CTR_TRY(run_stage(c, pl.st[0], WS_TASKS));
+    CTR_TRY(run_stage(c, pl.st[1], WS_TASKS2));
+  }
+  return CTR_OK;
+}
+
+int pipi_sets(int N, int Nt, int tf_begin, int tf_end, int iso, const double* prop_rows, const double* prop_diag,
+              const double* phi_all, int nphi, int nset, const int32_t* sets, double* corr, cudaStream_t s,
+              int engine) {
+  Ctx c{N, Nt, (size_t)N * N, s, engine};
+  if (engine == CTR_ENGINE_SPLIT) g_refined_last = 0;
+  const size_t N2 = c.N2, blk16 = 16 * N2;
+  const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag,
+                *ph = (const double2*)phi_all;
+  const int rows = tf_end - tf_begin, npairs = rows * Nt;
+  auto P = [&](int q, int t) { return ph + ((size_t)t * nphi + q) * N2; };
+  for (int k = 0; k < 4 * nset; k++)
+    if (sets[k] < 0 || sets[k] >= nphi) return fail(CTR_ERR_ARG, "ctr_pipi_sets: elemental index %d not in [0,%d)",
+                                                    sets[k], nphi);
+  // ---- per time slice: M(a, b, t) = Phi_a(t) taud(t) Phi_b(t) for the (a, b) the sets use:
+  // L = (P3, P4) at the sink times, Rsq = (P2, P1) and Rdt = (P1, P2) at every source time
+  std::map<std::pair<int, int>, int> combo;
+  std::vector<std::pair<int, int>> combos;
+  std::vector<std::vector<char>> need;
+  auto use = [&](int a, int b, int t0, int t1) {
+    auto it = combo.find({a, b});
+    if (it == combo.end()) {
+      it = combo.emplace(std::make_pair(a, b), (int)combos.size()).first;
+      combos.push_back({a, b});
+      need.emplace_back(Nt, 0);
+    }
+    for (int t = t0; t < t1; t++) need[it->second][t] = 1;
+    return it->second;
+  };
+  std::vector<int> cL(nset), cSq(nset), cDt(nset);
+  for (int k = 0; k < nset; k++) {
+    const int* q = sets + 4 * k;
+    cL[k] = use(q[2], q[3], tf_begin, tf_end);
+    cSq[k] = use(q[1], q[0], 0, Nt);
+    cDt[k] = use(q[0], q[1], 0, Nt);
+  }
+  std::vector<const double2*> M;
+  CTR_TRY(per_t_sets(c, diag, ph, nphi, combos, need, M));
+  // ---- pair batches, source time major: the pairs of one t_src share right
+  // operands (Rsq, Rdt, Phi(t_src)), so their products stack along M.  Each stage
+  // is a list of block grids whose outputs the plan places so that the slabs of
+  // one right block are consecutive blocks.
+  std::vector<int> order(npairs);
+  for (int ti = 0, k = 0; ti < Nt; ti++)
+    for (int tfl = 0; tfl < rows; tfl++) order[k++] = tfl * Nt + ti;
+  auto index_of = [&](std::vector<int>& v, int n) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    std::vector<int> ix(n, -1);
+    for (size_t a = 0; a < v.size(); a++) ix[v[a]] = (int)a;
+    return ix;
+  };
+  // elementals on the sink side of U (P3, P4) and on the source side (P1, P2: W, V, Pm)
+  std::vector<int> Qu, Qw;
+  for (int k = 0; k < nset; k++) {
+    Qu.push_back(sets[4 * k + 2]);
+    Qu.push_back(sets[4 * k + 3]);
+    Qw.push_back(sets[4 * k]);
+    Qw.push_back(sets[4 * k + 1]);
+  }
+  const std::vector<int> iu = index_of(Qu, nphi), iw = index_of(Qw, nphi);
+  const int nU = (int)Qu.size(), nW = (int)Qw.size();
+  std::vector<int> CL(cL.begin(), cL.end());
+  const std::vector<int> icl = index_of(CL, (int)combos.size());
+  const int nCL = (int)CL.size();
+  // Y families (left L combo, right combo): Ysq and Ydt of every set
+  std::map<std::pair<int, int>, int> yfam;
+  std::vector<std::pair<int, int>> YF;
+  std::vector<int> ysq(nset), ydt(nset);
+  auto fam = [&](int cl, int cr) {
+    auto it = yfam.find({cl, cr});
+    if (it == yfam.end()) {
+      it = yfam.emplace(std::make_pair(cl, cr), (int)YF.size()).first;
+      YF.push_back({cl, cr});
+    }
+    return it->second;
+  };
+  for (int k = 0; k < nset; k++) {
+    ysq[k] = fam(cL[k], cSq[k]);
+    ydt[k] = fam(cL[k], cDt[k]);
+  }
+  const int nYF = (int)YF.size();
+  // F = Phi_qf(tf) Pm(qp): per Pm index, the elementals it is multiplied by
+  std::vector<std::vector<int>> FK(nW);
+  std::vector<int> fpos(nset * 2);
+  if (iso == 0)
+    for (int k = 0; k < nset; k++)
+      for (int h = 0; h < 2; h++) {
+        const int qf = sets[4 * k + 2 + h], qp = iw[sets[4 * k + h]];
+        auto& v = FK[qp];
+        auto it = std::find(v.begin(), v.end(), qf);
+        if (it == v.end()) it = v.insert(v.end(), qf);
+        fpos[2 * k + h] = (int)(it - v.begin());
+      }
+  int nF = 0;
+  for (auto& v : FK) nF += (int)v.size();
+  // star / fish twin traces Tr[U(qu) W(qw)]: (U4, W1), (U3, W2), (U3, W1), (U4, W2) of every set
+  std::map<std::pair<int, int>, int> twk;
+  std::vector<std::pair<int, int>> TW;
+  std::vector<int> twin(4 * nset);
+  for (int k = 0; k < nset; k++) {
+    const int* q = sets + 4 * k;
+    const std::pair<int, int> key[4] = {{q[3], q[0]}, {q[2], q[1]}, {q[2], q[0]}, {q[3], q[1]}};
+    for (int h = 0; h < 4; h++) {
+      auto it = twk.find(key[h]);
+      if (it == twk.end()) {
+        it = twk.emplace(key[h], (int)TW.size()).first;
+        TW.push_back(key[h]);
+      }
+      twin[4 * k + h] = it->second;
+    }
+  }
+  const int nTW = (int)TW.size();
+  const size_t blk_pair = 16 * (size_t)(nU + nW + nCL + nYF + (iso == 0 ? 2 * nW + nF : 0));
+  const size_t tr_pair = (size_t)nset * (iso == 0 ? 48 : 32) + 16 * (size_t)nTW;
+  const size_t per_pair = blk_pair * N2 * sizeof(double2) + tr_pair * (sizeof(double2) + sizeof(double));
+  const int batch = std::max(1, std::min(npairs, (int)(sets_budget() / std::max<size_t>(per_pair, 1))));
+  Refine rf;
+  CTR_TRY(refine_begin(c, (size_t)nset * npairs * 5, WS_REFINE, rf));
+  const float g5w[4] = {(float)G5[0], (float)G5[1], (float)G5[2], (float)G5[3]};
+  for (int p0 = 0; p0 < npairs; p0 += batch) {
+    const int np = std::min(batch, npairs - p0);
+    void* mem;
+    CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * per_pair, &mem));
+    double2* base = (double2*)mem;
+    size_t used = 0;
+    auto alloc = [&](size_t nblk) {
+      double2* p = base + used;
+      used += nblk * N2;
+      return p;
+    };
+    std::vector<int> tfv(np), tiv(np), gof(np), pos(np);
+    std::vector<const double2*> Tv(np);
+    std::vector<std::pair<int, int>> grp;  // (first pair, count) of each t_src run
+    for (int i = 0; i < np; i++) {
+      const int pair = order[p0 + i], tfl = pair / Nt;
+      tfv[i] = tf_begin + tfl;
+      tiv[i] = pair % Nt;
+      Tv[i] = tau + ((size_t)tfl * Nt + tiv[i]) * blk16;
+      if (i == 0 || tiv[i] != tiv[i - 1]) grp.push_back({i, 0});
+      gof[i] = (int)grp.size() - 1;
+      pos[i] = grp.back().second++;
+    }
+    const int ng = (int)grp.size();
+    std::vector<double2*> bU(np), bW(np), bX(np), bP(np, nullptr), bV(ng, nullptr), bY((size_t)ng * nYF);
+    std::vector<std::vector<double2*>> bF(np, std::vector<double2*>(nW, nullptr));
+    for (int i = 0; i < np; i++) {
+      bU[i] = alloc(16 * (size_t)nU);
+      bW[i] = alloc(16 * (size_t)nW);
+      bX[i] = alloc(16 * (size_t)nCL);
+      if (iso == 0) {
+        bP[i] = alloc(16 * (size_t)nW);
+        for (int qp = 0; qp < nW; qp++)
+          if (!FK[qp].empty()) bF[i][qp] = alloc(16 * FK[qp].size());
+      }
+    }
+    for (int g = 0; g < ng; g++) {
+      const size_t m = grp[g].second;
+      if (iso == 0) bV[g] = alloc(16 * (size_t)nW * m);
+      for (int f = 0; f < nYF; f++) bY[(size_t)g * nYF + f] = alloc(16 * m);
+    }
+    auto grid = [](int nslab, int nb, int nterm, const float* w, int adag, int bdag) {
+      GridTask G;
+      std::memset(G.B, 0, sizeof(G.B));
+      std::memset(G.C0, 0, sizeof(G.C0));
+      for (int q = 0; q < 4; q++) G.w[q] = q < nterm ? w[q] : 0.f;
+      G.nslab = nslab;
+      G.nb = nb;
+      G.nterm = nterm;
+      G.adag = adag;
+      G.bdag = bdag;
+      G.A.resize((size_t)nslab * nterm);
+      return G;
+    };
+    const float one[4] = {1.f, 1.f, 1.f, 1.f};
+    std::vector<GridTask> g0, g1, g2;
+    for (int i = 0; i < np; i++) {
+      const double2* T = Tv[i];
+      for (int jb = 0; jb < 2; jb++) {
+        // U(q)_b = Phi_q(tf) tau_b, W(q)_b = Phi_q(ti) tau_b^dag; slab q, right block b
+        GridTask gu = grid(nU, 8, 1, one, 0, 0), gw = grid(nW, 8, 1, one, 0, 0x11111111);
+        for (int sl = 0; sl < nU; sl++) gu.A[sl] = P(Qu[sl], tfv[i]);
+        for (int sl = 0; sl < nW; sl++) gw.A[sl] = P(Qw[sl], tiv[i]);
+        for (int j = 0; j < 8; j++) {
+          const int b = 8 * jb + j;
+          gu.B[j][0] = gw.B[j][0] = T + b * N2;
+          gu.C0[j] = bU[i] + (size_t)b * nU * N2;
+          gw.C0[j] = bW[i] + (size_t)b * nW * N2;
+        }
+        g0.push_back(std::move(gu));
+        g0.push_back(std::move(gw));
+      }
+      // X = L G T: slab (L combo, row block a), right block b
+      GridTask gx = grid(4 * nCL, 4, 4, g5w, 0, 0);
+      for (int ci = 0; ci < nCL; ci++)
+        for (int a = 0; a < 4; a++)
+          for (int kk = 0; kk < 4; kk++)
+            gx.A[(size_t)(ci * 4 + a) * 4 + kk] = M[(size_t)CL[ci] * Nt + tfv[i]] + (size_t)(a * 4 + kk) * N2;
+      for (int j = 0; j < 4; j++) {
+        for (int kk = 0; kk < 4; kk++) gx.B[j][kk] = T + (kk * 4 + j) * N2;
+        gx.C0[j] = bX[i] + (size_t)j * 4 * nCL * N2;
+      }
+      g0.push_back(std::move(gx));
+    }
+    auto Xblk = [&](int cl, int i, int a, int b) { return bX[i] + ((size_t)b * 4 * nCL + icl[cl] * 4 + a) * N2; };
+    auto Vblk = [&](int qi, int i, int a, int b) {
+      return bV[gof[i]] + ((size_t)qi * 16 * grp[gof[i]].second + pos[i] * 16 + a * 4 + b) * N2;
+    };
+    auto Yblk = [&](int f, int i, int a, int c2) {
+      return bY[(size_t)gof[i] * nYF + f] + ((size_t)c2 * 4 * grp[gof[i]].second + pos[i] * 4 + a) * N2;
+    };
+    auto Pblk = [&](int qi, int i, int a, int c2) { return bP[i] + ((size_t)c2 * 4 * nW + qi * 4 + a) * N2; };
+    for (int g = 0; g < ng; g++) {
+      const int i0 = grp[g].first, m = grp[g].second, ti = tiv[i0];
+      if (iso == 0)  // V(q) = tau_b Phi_q(ti): slab (pair, block b), right block q
+        for (int q0 = 0; q0 < nW; q0 += 8) {
+          GridTask gv = grid(16 * m, std::min(8, nW - q0), 1, one, 0, 0);
+          for (int pp = 0; pp < m; pp++)
+            for (int b = 0; b < 16; b++) gv.A[pp * 16 + b] = Tv[i0 + pp] + b * N2;
+          for (int j = 0; j < gv.nb; j++) {
+            gv.B[j][0] = P(Qw[q0 + j], ti);
+            gv.C0[j] = bV[g] + (size_t)(q0 + j) * 16 * m * N2;
+          }
+          g0.push_back(std::move(gv));
+        }
+      // Ysq / Ydt = X G R: slab (pair, row block a), right block b of R(t_src)
+      for (int f = 0; f < nYF; f++) {
+        GridTask gy = grid(4 * m, 4, 4, g5w, 0, 0);
+        for (int pp = 0; pp < m; pp++)
+          for (int a = 0; a < 4; a++)
+            for (int kk = 0; kk < 4; kk++) gy.A[(size_t)(pp * 4 + a) * 4 + kk] = Xblk(YF[f].first, i0 + pp, a, kk);
+        for (int j = 0; j < 4; j++) {
+          for (int kk = 0; kk < 4; kk++) gy.B[j][kk] = M[(size_t)YF[f].second * Nt + ti] + (size_t)(kk * 4 + j) * N2;
+          gy.C0[j] = bY[(size_t)g * nYF + f] + (size_t)j * 4 * m * N2;
+        }
+        g1.push_back(std::move(gy));
+      }
+    }
+    if (iso == 0)
+      for (int i = 0; i < np; i++) {
+        // Pm(q) = V(q) T^dag: block (a, c) = sum_k V_ak tau_ck^dag; slab (q, a), right block c
+        GridTask gp = grid(4 * nW, 4, 4, one, 0, 0xFFFF);
+        for (int qi = 0; qi < nW; qi++)
+          for (int a = 0; a < 4; a++)
+            for (int kk = 0; kk < 4; kk++) gp.A[(size_t)(qi * 4 + a) * 4 + kk] = Vblk(qi, i, a, kk);
+        for (int j = 0; j < 4; j++) {
+          for (int kk = 0; kk < 4; kk++) gp.B[j][kk] = Tv[i] + (j * 4 + kk) * N2;
+          gp.C0[j] = bP[i] + (size_t)j * 4 * nW * N2;
+        }
+        g1.push_back(std::move(gp));
+        // F(qf, qp)_b = Phi_qf(tf) Pm(qp)_b: slab qf, right block b
+        for (int qp = 0; qp < nW; qp++) {
+          const int nf = (int)FK[qp].size();
+          if (!nf) continue;
+          for (int jb = 0; jb < 2; jb++) {
+            GridTask gf = grid(nf, 8, 1, one, 0, 0);
+            for (int sl = 0; sl < nf; sl++) gf.A[sl] = P(FK[qp][sl], tfv[i]);
+            for (int j = 0; j < 8; j++) {
+              const int b = 8 * jb + j;
+              gf.B[j][0] = Pblk(qp, i, b / 4, b % 4);
+              gf.C0[j] = bF[i][qp] + (size_t)b * nf * N2;
+            }
+            g2.push_back(std::move(gf));
+          }
+        }
+      }
+    // traces: values (and error scales) after the products in the same buffer
+    const size_t ntr = (size_t)np * tr_pair;
+    double2* trv = base + used;
+    double* tra = rf.on ? (double*)(trv + ntr) : nullptr;
+    if ((used * sizeof(double2) + ntr * (sizeof(double2) + sizeof(double))) > (size_t)np * per_pair)
+      return fail(CTR_ERR_ALLOC, "ctr_pipi_sets: batch arena overflow");
+    TracePlan tp;
+    std::vector<int> slots, ent, tws(16 * (size_t)nTW);
+    for (int i = 0; i < np; i++) {
+      const double2* T = Tv[i];
+      for (int t = 0; t < nTW; t++)
+        for (int b = 0; b < 16; b++)
+          tws[t * 16 + b] = tp.add(bU[i] + ((size_t)b * nU + iu[TW[t].first]) * N2,
+                                   bW[i] + ((size_t)b * nW + iw[TW[t].second]) * N2, 1.f, 0.f, 1);
+      for (int k = 0; k < nset; k++) {
+        const int* q = sets + 4 * k;
+        for (int b = 0; b < 16; b++) slots.push_back(tp.add(Yblk(ysq[k], i, b / 4, b % 4), T + b * N2, 1.f, 0.f, 0));
+        for (int b = 0; b < 16; b++) slots.push_back(tp.add(Yblk(ydt[k], i, b / 4, b % 4), T + b * N2, 1.f, 0.f, 0));
+        for (int b = 0; b < 16; b++) {
+          if (iso != 0) {
+            slots.push_back(-1);
+            continue;
+          }
+          // Tr[F_{s1 s3} G_{s3 s1}], F = Phi3 Pm(P1), G = Phi4 Pm(P2)
+          const int s1 = b / 4, s3 = b % 4, qf1 = iw[q[0]], qf2 = iw[q[1]];
+          const double2* Fb = bF[i][qf1] + ((size_t)b * FK[qf1].size() + fpos[2 * k]) * N2;
+          const double2* Gb = bF[i][qf2] + ((size_t)(s3 * 4 + s1) * FK[qf2].size() + fpos[2 * k + 1]) * N2;
+          slots.push_back(tp.add(Fb, Gb, 1.f, 0.f, 1));
+        }
+        for (int h = 0; h < 4; h++)
+          for (int b = 0; b < 16; b++) slots.push_back(tws[twin[4 * k + h] * 16 + b]);
+        ent.push_back(k * npairs + order[p0 + i]);
+      }
+    }
+    for (size_t k = 0; k < tp.tt.size(); k++) {
+      tp.tt[k].out = trv + k;
+      if (tra) tp.tt[k].absout = tra + k;
+    }
+    CTR_TRY(run_grids(c, g0, WS_TASKS));
+    CTR_TRY(run_grids(c, g1, WS_TASKS2));
+    CTR_TRY(run_grids(c, g2, WS_GEMM_A));
+    CTR_TRY(run_traces(c, tp.tt));
+    void* d[2];
+    CTR_TRY(upload_group(WS_MISC, {{slots.data(), slots.size() * sizeof(int)}, {ent.data(), ent.size() * sizeof(int)}},
+                         d, s));
+    {
+      TimedLaunch tl(s, "pipi_combine");
+      const int nitem = (int)ent.size();
+      pipi_combine_sets_kernel<<<(nitem + 127) / 128, 128, 0, s>>>(trv, tra, (const int*)d[0], (const int*)d[1], nitem,
+                                                                   iso, (double2*)corr, rf.eps_over_tol, rf.count,
+                                                                   rf.list);
+      CTR_CUDA(cudaGetLastError());
+    }
+  }
+  std::vector<int32_t> set_copy(sets, sets + 4 * nset);
+  return refine_end(c, rf, 5, WS_REFINE, (double2*)corr,
+                    [=](const std::vector<int>& units, double2* out, cudaStream_t ls) -> int {
+                      // units = set * npairs + pair, ascending: one FP64 rerun per set
+                      size_t u0 = 0;
+                      while (u0 < units.size()) {
+                        const int k = units[u0] / npairs;
+                        size_t u1 = u0;
+                        std::vector<int> pl;
+                        while (u1 < units.size() && units[u1] / npairs == k) pl.push_back(units[u1++] % npairs);
+                        const int* q = set_copy.data() + 4 * k;
+                        auto Pq = [&](int qq) { return (const double*)(ph + (size_t)qq * N2); };
+                        CTR_TRY(pipi_chain(N, Nt, tf_begin, tf_end, iso, prop_rows, prop_diag, Pq(q[0]), Pq(q[1]),
+                                           Pq(q[2]), Pq(q[3]), (double*)(out + u0 * 5), ls, CTR_ENGINE_FP64, &pl,
+                                           (size_t)nphi));
+                        u0 = u1;
+                      }
+                      return CTR_OK;
                     });
 }
 
@@ -358,7 +916,7 @@ int pipi_chain(int N, int Nt, int tf_begin, int tf_end, int iso, const double* p
 // coef = c(iop, s3, s5) * g5(s1), so the sum over s1 is (T G R)_{s5 s2}.
 int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double* prop_rows, const double* prop_diag,
                 const double* mp1, const double* mp2, const double* mom5, double* corr, cudaStream_t s, int engine,
-                const std::vector<int>* plist) {
+                const std::vector<int>* plist, size_t pstride = 1) {
   if (idir < 0 || idir > 2) return fail(CTR_ERR_ARG, "idir %d not in {0,1,2}", idir);
   Ctx c{N, Nt, (size_t)N * N, s, engine};
   if (engine == CTR_ENGINE_SPLIT && !plist) g_refined_last = 0;
@@ -372,7 +930,7 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
   void* pt;
   CTR_TRY(workspace(WS_PHI).get(2 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *R = (double2*)pt, *tmp = R + Nt * blk16;
-  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need_ti));  // R = Phi_P2 taud Phi_P1
+  CTR_TRY(per_t_chain(c, diag, P2, pstride * N2, P1, pstride * N2, tmp, R, &need_ti));  // R = Phi_P2 taud Phi_P1
 
   // groups (iop, s2, s3): s5 from the table, c = coef * g5(s1); the 4 rows s1=0..3 share a group
   const Tables& Tb = tables();
@@ -453,7 +1011,7 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
   return refine_end(c, rf, 4, WS_REFINE, (double2*)corr,
                     [=](const std::vector<int>& pairs, double2* out, cudaStream_t ls) {
                       return rhopi_chain(N, Nt, tf_begin, tf_end, idir, prop_rows, prop_diag, mp1, mp2, mom5,
-                                         (double*)out, ls, CTR_ENGINE_FP64, &pairs);
+                                         (double*)out, ls, CTR_ENGINE_FP64, &pairs, pstride);
                     });
 }
 
@@ -464,7 +1022,8 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
 // coef = g5(s1) g5(s3): sum_s3 g5(s3) tau_{s1s3} R_{s3s5} = (T G R)_{s1 s5}.
 int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* prop_diag,
                   const double* mp1, const double* mp2, const double* mom2, double* hor_fish, double* tri,
-                  cudaStream_t s, int engine, const std::vector<int>* plist, const std::vector<int>* tlist) {
+                  cudaStream_t s, int engine, const std::vector<int>* plist, const std::vector<int>* tlist,
+                  size_t pstride = 1) {
   Ctx c{N, Nt, (size_t)N * N, s, engine};
   if (engine == CTR_ENGINE_SPLIT && !plist && !tlist) g_refined_last = 0;
   const size_t N2 = c.N2, blk16 = 16 * N2;
@@ -482,7 +1041,7 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
   // a recomputation (plist / tlist) keeps its own R, so that the caller's stays valid
   CTR_TRY(workspace((plist || tlist) ? WS_RPHI : WS_PHI).get(2 * (size_t)Nt * blk16 * sizeof(double2), &pt));
   double2 *R = (double2*)pt, *tmp = R + Nt * blk16;
-  CTR_TRY(per_t_chain(c, diag, P2, N2, P1, N2, tmp, R, &need));
+  CTR_TRY(per_t_chain(c, diag, P2, pstride * N2, P1, pstride * N2, tmp, R, &need));
   if (hor_fish) {
     // lib/calculate_sigmapi_hor_fish_core.h: sum_ab coef * sum R_ab (.) conj taud_ab, per time slice
     Refine rf;
@@ -517,7 +1076,7 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
     CTR_TRY(refine_end(c, rf, 1, WS_REFINE, (double2*)hor_fish,
                        [=](const std::vector<int>& ts, double2* out, cudaStream_t ls) {
                          return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2,
-                                              (double*)out, nullptr, ls, CTR_ENGINE_FP64, nullptr, &ts);
+                                              (double*)out, nullptr, ls, CTR_ENGINE_FP64, nullptr, &ts, pstride);
                        }));
   }
   if (!tri) return CTR_OK;
@@ -570,8 +1129,388 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
   return refine_end(c, rf, 2, WS_REFINE, (double2*)tri,
                     [=](const std::vector<int>& pairs, double2* out, cudaStream_t ls) {
                       return sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, mp1, mp2, mom2, nullptr,
-                                           (double*)out, ls, CTR_ENGINE_FP64, &pairs, nullptr);
+                                           (double*)out, ls, CTR_ENGINE_FP64, &pairs, nullptr, pstride);
                     });
+}
+
+// --------------------------------------- rho -> pi pi and sigma -> pi pi over sets
+// Both families contract X = T G R, R(t) = Phi_P2(t) taud(t) Phi_P1(t), with the
+// sink operators: rho -> pi pi (lib/calculate_rhopi_core.h) takes Phi^{P1P2}_ip(tf)
+// X_{s5 s2} for ip in {0, 1, 2 + idir}, the sigma -> pi pi triangle
+// (lib/calculate_sigmapi_triangle_core.h) Phi^{x2}_ik(tf) X_b for ik in {0, 1}.
+// Per set and pair, X is computed once and multiplied by all the sink operators
+// the requested outputs need in one grid (slab = operator, right block = X
+// block); the horizontal fish (lib/calculate_sigmapi_hor_fish_core.h) traces R
+// against taud per time slice.
+
+namespace {
+
+// Row sums of batch items whose rows' trace values sit anywhere: row r of item it
+// is trace slot rowslot[it * nrows + r]; output o sums rows idx[off[o] .. off[o+1])
+// in that order into out[ent[it] * nout + o]; with trabs, entries whose error
+// estimate exceeds the tolerance append ent * nout + o to the refinement list.
+__global__ void rowsum_items_kernel(const double2* __restrict__ trv, const double* __restrict__ trabs,
+                                    const int* __restrict__ rowslot, int nrows, const int* __restrict__ off,
+                                    const int* __restrict__ idx, int nout, const int* __restrict__ ent, int nitem,
+                                    double2* __restrict__ out, double eps_over_tol, int* __restrict__ count,
+                                    int* __restrict__ list) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nitem * nout) return;
+  const int it = g / nout, o = g % nout;
+  double re = 0.0, im = 0.0, sc = 0.0;
+  for (int k = off[o]; k < off[o + 1]; k++) {
+    const int j = rowslot[(size_t)it * nrows + idx[k]];
+    re += trv[j].x;
+    im += trv[j].y;
+    if (trabs) sc += trabs[j];
+  }
+  const size_t e = (size_t)ent[it] * nout + o;
+  out[e] = make_double2(re, im);
+  const double mag = sqrt(re * re + im * im);
+  if (trabs && eps_over_tol > 0.0 && (!(sc * eps_over_tol <= mag) || (sc == 0.0 && mag > 0.0)))
+    list[atomicAdd(count, 1)] = (int)e;
+}
+
+// Item tables of one row-sum launch (host), and their device copies.
+struct RowItems {
+  std::vector<int> slot, csr, ent;
+  int nrows = 0, nout = 0;
+  const int *d_slot = nullptr, *d_csr = nullptr, *d_ent = nullptr;
+};
+
+// Uploads the tables of several row-sum launches in one staging copy.
+int upload_items(const Ctx& c, std::vector<RowItems*> items) {
+  std::vector<std::pair<const void*, size_t>> parts;
+  for (RowItems* r : items) {
+    parts.push_back({r->slot.data(), r->slot.size() * sizeof(int)});
+    parts.push_back({r->csr.data(), r->csr.size() * sizeof(int)});
+    parts.push_back({r->ent.data(), r->ent.size() * sizeof(int)});
+  }
+  std::vector<void*> d(parts.size());
+  CTR_TRY(upload_group(WS_MISC, parts, d.data(), c.s));
+  for (size_t i = 0; i < items.size(); i++) {
+    items[i]->d_slot = (const int*)d[3 * i];
+    items[i]->d_csr = (const int*)d[3 * i + 1];
+    items[i]->d_ent = (const int*)d[3 * i + 2];
+  }
+  return CTR_OK;
+}
+
+int rowsum_items(const Ctx& c, const double2* trv, const double* tra, const RowItems& r, double2* out,
+                 const Refine& rf) {
+  if (r.ent.empty()) return CTR_OK;
+  TimedLaunch tl(c.s, "rowsum_items");
+  const int n = (int)r.ent.size() * r.nout;
+  rowsum_items_kernel<<<(n + 127) / 128, 128, 0, c.s>>>(trv, rf.on ? tra : nullptr, r.d_slot, r.nrows, r.d_csr,
+                                                        r.d_csr + r.nout + 1, r.nout, r.d_ent, (int)r.ent.size(), out,
+                                                        rf.eps_over_tol, rf.count, rf.list);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+}  // namespace
+
+int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* prop_rows, const double* prop_diag,
+                       const double* phi_all, int nphi, const double* mom5, const double* mom2, int nset,
+                       const int32_t* sets, double* rhopi, double* tri, double* hor_fish, cudaStream_t s,
+                       int engine) {
+  Ctx c{N, Nt, (size_t)N * N, s, engine};
+  if (engine == CTR_ENGINE_SPLIT) g_refined_last = 0;
+  const size_t N2 = c.N2, blk16 = 16 * N2;
+  const double2 *tau = (const double2*)prop_rows, *diag = (const double2*)prop_diag,
+                *ph = (const double2*)phi_all, *P5 = (const double2*)mom5, *P2x = (const double2*)mom2;
+  const int rows = tf_end - tf_begin, npairs = rows * Nt;
+  const Tables& Tb = tables();
+  for (int k = 0; k < 2 * nset; k++)
+    if (sets[k] < 0 || sets[k] >= nphi)
+      return fail(CTR_ERR_ARG, "ctr_rhopi_sigmapi_sets: elemental index %d not in [0,%d)", sets[k], nphi);
+  // R(t) = Phi_P2 taud Phi_P1 for every set's (P2, P1), at every time slice
+  std::map<std::pair<int, int>, int> combo;
+  std::vector<std::pair<int, int>> combos;
+  std::vector<int> cR(nset);
+  for (int k = 0; k < nset; k++) {
+    auto key = std::make_pair(sets[2 * k + 1], sets[2 * k]);
+    auto it = combo.find(key);
+    if (it == combo.end()) {
+      it = combo.emplace(key, (int)combos.size()).first;
+      combos.push_back(key);
+    }
+    cR[k] = it->second;
+  }
+  const int nC = (int)combos.size();
+  std::vector<std::vector<char>> need(nC, std::vector<char>(Nt, 1));
+  std::vector<const double2*> M;
+  CTR_TRY(per_t_sets(c, diag, ph, nphi, combos, need, M));
+
+  // ---- horizontal fish: per set and time slice, sum_ab coef * Tr-Had(R_ab, taud_ab)
+  if (hor_fish) {
+    Refine rf;
+    CTR_TRY(refine_begin(c, (size_t)nset * Nt, WS_REFINE, rf));
+    const size_t ntr = (size_t)nset * Nt * 16;
+    void *trm, *tra = nullptr;
+    CTR_TRY(workspace(WS_ROWS).get(ntr * sizeof(double2), &trm));
+    if (rf.on) CTR_TRY(workspace(WS_ROWABS).get(ntr * sizeof(double), &tra));
+    std::vector<TraceTask> tt;
+    RowItems ri;
+    ri.nrows = 16;
+    ri.nout = 1;
+    for (int k = 0; k < nset; k++)
+      for (int t = 0; t < Nt; t++) {
+        for (int b = 0; b < 16; b++) {
+          const int ab = Tb.hf_spin[b][0] * 4 + Tb.hf_spin[b][1];
+          tt.push_back(tr(M[(size_t)cR[k] * Nt + t] + ab * N2, diag + t * blk16 + ab * N2,
+                          (double2*)trm + tt.size(), Tb.hf_coef[b][0], Tb.hf_coef[b][1], 0));
+          if (tra) tt.back().absout = (double*)tra + (tt.size() - 1);
+          ri.slot.push_back((int)tt.size() - 1);
+        }
+        ri.ent.push_back(k * Nt + t);
+      }
+    ri.csr = {0, 16};
+    for (int b = 0; b < 16; b++) ri.csr.push_back(b);
+    CTR_TRY(run_traces(c, tt));
+    CTR_TRY(upload_items(c, {&ri}));
+    CTR_TRY(rowsum_items(c, (double2*)trm, (double*)tra, ri, (double2*)hor_fish, rf));
+    std::vector<int32_t> sc(sets, sets + 2 * nset);
+    CTR_TRY(refine_end(c, rf, 1, WS_REFINE, (double2*)hor_fish,
+                       [=](const std::vector<int>& units, double2* out, cudaStream_t ls) -> int {
+                         size_t u0 = 0;
+                         while (u0 < units.size()) {  // units = set * Nt + t: one FP64 rerun per set
+                           const int k = units[u0] / Nt;
+                           std::vector<int> tl;
+                           size_t u1 = u0;
+                           while (u1 < units.size() && units[u1] / Nt == k) tl.push_back(units[u1++] % Nt);
+                           CTR_TRY(sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag,
+                                                 (const double*)(ph + (size_t)sc[2 * k] * N2),
+                                                 (const double*)(ph + (size_t)sc[2 * k + 1] * N2), mom2,
+                                                 (double*)(out + u0), nullptr, ls, CTR_ENGINE_FP64, nullptr, &tl,
+                                                 (size_t)nphi));
+                           u0 = u1;
+                         }
+                         return CTR_OK;
+                       }));
+  }
+  if (!rhopi && !tri) return CTR_OK;
+
+  // ---- sink operators of the grid: the rho operators the three polarisations use, then sigma's two
+  struct Grp {
+    int iop, s2, s3, s5, slab;
+    float cre, cim;
+  };
+  std::vector<int> ops;  // slab -> operator: 0..4 rho (mom5), 5..6 sigma (mom2)
+  std::vector<int> slab_of(7, -1);
+  std::vector<Grp> grp[3];
+  std::vector<int> csr_rp[3];
+  if (rhopi)
+    for (int idir = 0; idir < 3; idir++) {
+      for (int bx = 0; bx < 256; bx++) {
+        const int r = idir * 256 + bx;
+        const int16_t* sp = Tb.rhopi_spin[r];
+        const int s1 = sp[0];
+        if (sp[5] != s1 || sp[3] != sp[2])
+          return fail(CTR_ERR_ARG, "rho-pipi table row %d not gamma_5-diagonal", r);
+        if (s1 != 0) continue;  // one representative per group (coef x g5(s1) sums over s1)
+        const int ip = Tb.rhopi_ip[r];
+        if (slab_of[ip] < 0) {
+          slab_of[ip] = (int)ops.size();
+          ops.push_back(ip);
+        }
+        grp[idir].push_back(Grp{bx / 64, sp[1], sp[2], sp[4], slab_of[ip], Tb.rhopi_coef[r][0] * G5[s1],
+                                Tb.rhopi_coef[r][1] * G5[s1]});
+      }
+      // CSR of the 4 operators over the groups, in group order (as rhopi_chain)
+      std::vector<int> off(5, 0), idx(grp[idir].size());
+      for (auto& g : grp[idir]) off[g.iop + 1]++;
+      for (int o = 0; o < 4; o++) off[o + 1] += off[o];
+      std::vector<int> fill(off.begin(), off.end() - 1);
+      for (size_t g = 0; g < grp[idir].size(); g++) idx[fill[grp[idir][g].iop]++] = (int)g;
+      csr_rp[idir] = off;
+      csr_rp[idir].insert(csr_rp[idir].end(), idx.begin(), idx.end());
+    }
+  if (tri)
+    for (int ik = 0; ik < 2; ik++) {
+      slab_of[5 + ik] = (int)ops.size();
+      ops.push_back(5 + ik);
+    }
+  const int nops = (int)ops.size();
+  std::vector<int> csr_tr = {0, 16, 32};
+  for (int k = 0; k < 32; k++) csr_tr.push_back(k);
+
+  std::vector<int> order(npairs);
+  for (int ti = 0, k = 0; ti < Nt; ti++)
+    for (int tfl = 0; tfl < rows; tfl++) order[k++] = tfl * Nt + ti;
+  const int ngr = rhopi ? (int)grp[0].size() : 0;
+  const size_t blk_pair = 16 * (size_t)nC * (1 + nops);
+  const size_t tr_pair = (size_t)nset * ((rhopi ? 3 * ngr : 0) + (tri ? 32 : 0));
+  const size_t per_pair = blk_pair * N2 * sizeof(double2) + tr_pair * (sizeof(double2) + sizeof(double));
+  const int batch = std::max(1, std::min(npairs, (int)(sets_budget() / std::max<size_t>(per_pair, 1))));
+  Refine rf_rp, rf_tr;
+  if (rhopi) CTR_TRY(refine_begin(c, (size_t)nset * 3 * npairs * 4, WS_REFINE, rf_rp));
+  if (tri) CTR_TRY(refine_begin(c, (size_t)nset * npairs * 2, WS_SPLITJOBS3, rf_tr));
+  const float g5w[4] = {(float)G5[0], (float)G5[1], (float)G5[2], (float)G5[3]};
+  const float one[4] = {1.f, 1.f, 1.f, 1.f};
+  for (int p0 = 0; p0 < npairs; p0 += batch) {
+    const int np = std::min(batch, npairs - p0);
+    void* mem;
+    CTR_TRY(workspace(WS_SCRATCH).get((size_t)np * per_pair, &mem));
+    double2* base = (double2*)mem;
+    size_t used = 0;
+    auto alloc = [&](size_t nblk) {
+      double2* p = base + used;
+      used += nblk * N2;
+      return p;
+    };
+    std::vector<int> tfv(np), tiv(np), gof(np), pos(np);
+    std::vector<const double2*> Tv(np);
+    std::vector<std::pair<int, int>> gr;
+    for (int i = 0; i < np; i++) {
+      const int pair = order[p0 + i], tfl = pair / Nt;
+      tfv[i] = tf_begin + tfl;
+      tiv[i] = pair % Nt;
+      Tv[i] = tau + ((size_t)tfl * Nt + tiv[i]) * blk16;
+      if (i == 0 || tiv[i] != tiv[i - 1]) gr.push_back({i, 0});
+      gof[i] = (int)gr.size() - 1;
+      pos[i] = gr.back().second++;
+    }
+    const int ng = (int)gr.size();
+    std::vector<double2*> bX((size_t)ng * nC), bY((size_t)np * nC);
+    for (int g = 0; g < ng; g++)
+      for (int ci = 0; ci < nC; ci++) bX[(size_t)g * nC + ci] = alloc(16 * (size_t)gr[g].second);
+    for (int i = 0; i < np; i++)
+      for (int ci = 0; ci < nC; ci++) bY[(size_t)i * nC + ci] = alloc(16 * (size_t)nops);
+    // X(ci, i)_{a b} and Y(op slab, ci, i)_b
+    auto Xblk = [&](int ci, int i, int a, int b) {
+      return bX[(size_t)gof[i] * nC + ci] + ((size_t)b * 4 * gr[gof[i]].second + pos[i] * 4 + a) * N2;
+    };
+    auto Yblk = [&](int sl, int ci, int i, int b) { return bY[(size_t)i * nC + ci] + ((size_t)b * nops + sl) * N2; };
+    std::vector<GridTask> g0, g1;
+    for (int g = 0; g < ng; g++) {
+      const int i0 = gr[g].first, m = gr[g].second, ti = tiv[i0];
+      for (int ci = 0; ci < nC; ci++) {
+        // X = T G R: slab (pair, row block a), right block b of R(t_src)
+        GridTask gx;
+        std::memset(gx.B, 0, sizeof(gx.B));
+        std::memset(gx.C0, 0, sizeof(gx.C0));
+        std::copy(g5w, g5w + 4, gx.w);
+        gx.nslab = 4 * m;
+        gx.nb = 4;
+        gx.nterm = 4;
+        gx.adag = gx.bdag = 0;
+        gx.A.resize((size_t)16 * m);
+        for (int pp = 0; pp < m; pp++)
+          for (int a = 0; a < 4; a++)
+            for (int kk = 0; kk < 4; kk++) gx.A[(size_t)(pp * 4 + a) * 4 + kk] = Tv[i0 + pp] + (a * 4 + kk) * N2;
+        for (int j = 0; j < 4; j++) {
+          for (int kk = 0; kk < 4; kk++) gx.B[j][kk] = M[(size_t)ci * Nt + ti] + (size_t)(kk * 4 + j) * N2;
+          gx.C0[j] = bX[(size_t)g * nC + ci] + (size_t)j * 4 * m * N2;
+        }
+        g0.push_back(std::move(gx));
+      }
+    }
+    for (int i = 0; i < np; i++)
+      for (int ci = 0; ci < nC; ci++)
+        for (int jb = 0; jb < 2; jb++) {
+          // Y = Op(tf) X_b: slab = sink operator, right block b of X
+          GridTask gy;
+          std::memset(gy.B, 0, sizeof(gy.B));
+          std::memset(gy.C0, 0, sizeof(gy.C0));
+          std::copy(one, one + 4, gy.w);
+          gy.nslab = nops;
+          gy.nb = 8;
+          gy.nterm = 1;
+          gy.adag = gy.bdag = 0;
+          gy.A.resize(nops);
+          for (int sl = 0; sl < nops; sl++)
+            gy.A[sl] = ops[sl] < 5 ? P5 + ((size_t)tfv[i] * 5 + ops[sl]) * N2 : P2x + ((size_t)tfv[i] * 2 + ops[sl] - 5) * N2;
+          for (int j = 0; j < 8; j++) {
+            const int b = 8 * jb + j;
+            gy.B[j][0] = Xblk(ci, i, b / 4, b % 4);
+            gy.C0[j] = bY[(size_t)i * nC + ci] + (size_t)b * nops * N2;
+          }
+          g1.push_back(std::move(gy));
+        }
+    // traces
+    const size_t ntr = (size_t)np * tr_pair;
+    double2* trv = base + used;
+    double* tra = (rf_rp.on || rf_tr.on) ? (double*)(trv + ntr) : nullptr;
+    if (used * sizeof(double2) + ntr * (sizeof(double2) + sizeof(double)) > (size_t)np * per_pair)
+      return fail(CTR_ERR_ALLOC, "ctr_rhopi_sigmapi_sets: batch arena overflow");
+    TracePlan tp;
+    RowItems it_rp[3], it_tr;
+    for (int idir = 0; idir < 3; idir++) {
+      it_rp[idir].nrows = ngr;
+      it_rp[idir].nout = 4;
+      it_rp[idir].csr = csr_rp[idir];
+    }
+    it_tr.nrows = 32;
+    it_tr.nout = 2;
+    it_tr.csr = csr_tr;
+    for (int i = 0; i < np; i++) {
+      const double2* T = Tv[i];
+      const int pair = order[p0 + i];
+      for (int k = 0; k < nset; k++) {
+        const int ci = cR[k];
+        if (rhopi)
+          for (int idir = 0; idir < 3; idir++) {
+            for (const Grp& g : grp[idir])
+              it_rp[idir].slot.push_back(tp.add(Yblk(g.slab, ci, i, g.s5 * 4 + g.s2), T + (g.s3 * 4 + g.s2) * N2,
+                                                g.cre, g.cim, 0));
+            it_rp[idir].ent.push_back((k * 3 + idir) * npairs + pair);
+          }
+        if (tri) {
+          for (int ik = 0; ik < 2; ik++)
+            for (int b = 0; b < 16; b++)
+              it_tr.slot.push_back(tp.add(Yblk(slab_of[5 + ik], ci, i, b), T + b * N2, (float)G5[b / 4], 0.f, 0));
+          it_tr.ent.push_back(k * npairs + pair);
+        }
+      }
+    }
+    for (size_t k = 0; k < tp.tt.size(); k++) {
+      tp.tt[k].out = trv + k;
+      if (tra) tp.tt[k].absout = tra + k;
+    }
+    CTR_TRY(run_grids(c, g0, WS_TASKS));
+    CTR_TRY(run_grids(c, g1, WS_TASKS2));
+    CTR_TRY(run_traces(c, tp.tt));
+    CTR_TRY(upload_items(c, {&it_rp[0], &it_rp[1], &it_rp[2], &it_tr}));
+    for (int idir = 0; idir < 3 && rhopi; idir++)
+      CTR_TRY(rowsum_items(c, trv, tra, it_rp[idir], (double2*)rhopi, rf_rp));
+    if (tri) CTR_TRY(rowsum_items(c, trv, tra, it_tr, (double2*)tri, rf_tr));
+  }
+  std::vector<int32_t> sc(sets, sets + 2 * nset);
+  auto Pq = [=](int q) { return (const double*)(ph + (size_t)q * N2); };
+  if (rhopi)
+    CTR_TRY(refine_end(c, rf_rp, 4, WS_REFINE, (double2*)rhopi,
+                       [=](const std::vector<int>& units, double2* out, cudaStream_t ls) -> int {
+                         size_t u0 = 0;  // units = (set * 3 + idir) * npairs + pair
+                         while (u0 < units.size()) {
+                           const int kd = units[u0] / npairs, k = kd / 3, idir = kd % 3;
+                           std::vector<int> pl;
+                           size_t u1 = u0;
+                           while (u1 < units.size() && units[u1] / npairs == kd) pl.push_back(units[u1++] % npairs);
+                           CTR_TRY(rhopi_chain(N, Nt, tf_begin, tf_end, idir, prop_rows, prop_diag, Pq(sc[2 * k]),
+                                               Pq(sc[2 * k + 1]), mom5, (double*)(out + u0 * 4), ls, CTR_ENGINE_FP64,
+                                               &pl, (size_t)nphi));
+                           u0 = u1;
+                         }
+                         return CTR_OK;
+                       }));
+  if (tri)
+    CTR_TRY(refine_end(c, rf_tr, 2, WS_SPLITJOBS3, (double2*)tri,
+                       [=](const std::vector<int>& units, double2* out, cudaStream_t ls) -> int {
+                         size_t u0 = 0;  // units = set * npairs + pair
+                         while (u0 < units.size()) {
+                           const int k = units[u0] / npairs;
+                           std::vector<int> pl;
+                           size_t u1 = u0;
+                           while (u1 < units.size() && units[u1] / npairs == k) pl.push_back(units[u1++] % npairs);
+                           CTR_TRY(sigmapi_chain(N, Nt, tf_begin, tf_end, prop_rows, prop_diag, Pq(sc[2 * k]),
+                                                 Pq(sc[2 * k + 1]), mom2, nullptr, (double*)(out + u0 * 2), ls,
+                                                 CTR_ENGINE_FP64, &pl, nullptr, (size_t)nphi));
+                           u0 = u1;
+                         }
+                         return CTR_OK;
+                       }));
+  return CTR_OK;
 }
 
 // -------------------------------------------------------------- loop unity
@@ -631,6 +1570,33 @@ int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin,
     return ctr::fail(CTR_ERR_ARG, "ctr_pipi: null or misaligned pointer");
   return ctr::pipi_chain(nev, nt, tf_begin, tf_end, isospin, prop_rows, prop_diag, p1, p2, p3, p4, corr,
                          (cudaStream_t)stream, engine, nullptr);
+}
+
+int ctr_pipi_sets(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin, const double* prop_rows,
+                  const double* prop_diag, const double* phi, int nphi, int nset, const int32_t* sets, double* corr,
+                  void* stream) {
+  CTR_TRY(chain_args(engine, nev, nt, tf_begin, tf_end));
+  if (isospin != 0 && isospin != 1) return ctr::fail(CTR_ERR_ARG, "isospin must be 0 (I=0) or 1 (I=1)");
+  if (nphi < 1 || nset < 1 || !sets) return ctr::fail(CTR_ERR_ARG, "ctr_pipi_sets: nphi=%d, nset=%d", nphi, nset);
+  if (!aligned(prop_rows) || !aligned(prop_diag) || !aligned(phi) || !aligned(corr))
+    return ctr::fail(CTR_ERR_ARG, "ctr_pipi_sets: null or misaligned pointer");
+  return ctr::pipi_sets(nev, nt, tf_begin, tf_end, isospin, prop_rows, prop_diag, phi, nphi, nset, sets, corr,
+                        (cudaStream_t)stream, engine);
+}
+
+int ctr_rhopi_sigmapi_sets(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
+                           const double* prop_diag, const double* phi, int nphi, const double* mom5_p1p2,
+                           const double* mom2_p1p2, int nset, const int32_t* sets, double* rhopi, double* triangle,
+                           double* hor_fish, void* stream) {
+  CTR_TRY(chain_args(engine, nev, nt, tf_begin, tf_end));
+  if (nphi < 1 || nset < 1 || !sets)
+    return ctr::fail(CTR_ERR_ARG, "ctr_rhopi_sigmapi_sets: nphi=%d, nset=%d", nphi, nset);
+  if (!aligned(prop_diag) || !aligned(phi) || ((rhopi || triangle) && !aligned(prop_rows)) ||
+      (rhopi && (!aligned(mom5_p1p2) || !aligned(rhopi))) || ((triangle || hor_fish) && !aligned(mom2_p1p2)) ||
+      (triangle && !aligned(triangle)) || (hor_fish && !aligned(hor_fish)))
+    return ctr::fail(CTR_ERR_ARG, "ctr_rhopi_sigmapi_sets: null or misaligned pointer");
+  return ctr::rhopi_sigmapi_sets(nev, nt, tf_begin, tf_end, prop_rows, prop_diag, phi, nphi, mom5_p1p2, mom2_p1p2,
+                                 nset, sets, rhopi, triangle, hor_fish, (cudaStream_t)stream, engine);
 }
 
 int ctr_loop_unity(int engine, int nev, int nt, const double* prop_diag, const double* mom, double* loop,

@@ -585,7 +585,15 @@ extern "C" int ctr_split_set_refine(double rel_tol) {
 
 extern "C" long long ctr_split_refined(void) { return ctr::g_refined_last; }
 
+extern "C" int ctr_split_flops(double* executed_mma, double* block_products, int reset) {
+  if (executed_mma) *executed_mma = ctr::g_split_mma_flops;
+  if (block_products) *block_products = ctr::g_split_products;
+  if (reset) ctr::g_split_mma_flops = ctr::g_split_products = 0.0;
+  return CTR_OK;
+}
+
 namespace ctr {
+double g_split_mma_flops = 0.0, g_split_products = 0.0;
 double g_refine_tol = 1e-9;
 long long g_refined_last = 0;
 }  // namespace ctr
@@ -760,6 +768,150 @@ int zgemm_split_tasks(int N, const ZTask* tasks, int ntask, cudaStream_t stream)
                                       (const int*)d_bexp, stream));
       SplitGemmBatch G{(const SplitGemmInst*)d_gi, 1, ntiles, nchunk, N, nb * N, SPLIT_M, nullptr, 1, N, 1};
       CTR_TRY(launch_split_gemm(G, ni, d_err, stream));
+      if (!capturing()) g_split_products += (double)ni * nb * nterm;
+    }
+  }
+  return CTR_OK;
+}
+
+}  // namespace ctr
+
+namespace ctr {
+
+// Split-engine execution of block grids (GridTask, ctr_internal.h) on the
+// high-precision configuration.  Each grid's slabs are cut into pieces of at
+// most SPLIT_STACK slabs; a piece is one GEMM instance whose left operand
+// stacks its slabs along M (slice_stack_left), so that M tiles carry padding
+// rows only at the end of a piece; the right side (nb blocks along N) is sliced
+// once per distinct right side of a launch.  Pieces of equal shape (terms,
+// right blocks, slabs) form one persistent launch; the epilogue writes slab s of
+// right block j at C0[j] + s Nev^2, i.e. row s Nev + r of the piece.
+int zgemm_split_grids(int N, const std::vector<GridTask>& grids, cudaStream_t stream) {
+  if (grids.empty()) return CTR_OK;
+  if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d (got %d)", SPLIT_MAXK, N);
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  const size_t N2 = (size_t)N * N;
+  struct Piece {
+    int g, s0, ns;
+  };
+  std::map<std::tuple<int, int, int>, std::vector<Piece>> buckets;
+  for (int g = 0; g < (int)grids.size(); g++) {
+    const GridTask& G = grids[g];
+    if (G.nterm < 1 || G.nterm > 4 || G.nterm * N > 512 || G.nb < 1 || G.nb > SPLIT_TASK_NB || G.nslab < 1 ||
+        (int)G.A.size() != G.nslab * G.nterm)
+      return fail(CTR_ERR_ARG, "split grid %d: %d terms of Nev %d, %d right blocks, %d slabs", g, G.nterm, N, G.nb,
+                  G.nslab);
+    for (int q = 0; q < G.nterm; q++) {
+      int ex;
+      if (!(G.w[q] != 0.f) || std::fabs(std::frexp(G.w[q], &ex)) != 0.5f)
+        return fail(CTR_ERR_UNSUPPORTED, "split grid %d: weight %g is not a power of two", g, G.w[q]);
+    }
+    for (int s0 = 0; s0 < G.nslab; s0 += SPLIT_STACK) {
+      const int ns = std::min(SPLIT_STACK, G.nslab - s0);
+      buckets[std::make_tuple(G.nterm, G.nb, ns)].push_back(Piece{g, s0, ns});
+    }
+  }
+  for (auto& bk : buckets) {
+    const int nterm = std::get<0>(bk.first), nb = std::get<1>(bk.first), ns = std::get<2>(bk.first);
+    const int K = nterm * N, nchunk = cdiv(K, SPLIT_K), ntiles = cdiv(nb * N, CfgHP::BN),
+              mtiles = cdiv(ns * N, SPLIT_M);
+    const int eplus = K > 128 ? 1 : 0;
+    const size_t l_b = align256((size_t)mtiles * nchunk * CfgHP::A_STAGE), le_b = align256((size_t)mtiles * SPLIT_M * 4);
+    const size_t r_b = align256((size_t)ntiles * nchunk * CfgHP::B_STAGE), re_b = align256((size_t)ntiles * CfgHP::BN * 4);
+    const size_t per = l_b + le_b + r_b + re_b;  // one left and at most one distinct right per piece
+    const std::vector<Piece>& all = bk.second;
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(all.size(), ((size_t)4 << 30) / per));
+    for (size_t i0 = 0; i0 < all.size(); i0 += batch) {
+      const int ni = (int)std::min<size_t>(batch, all.size() - i0);
+      void* mem;
+      CTR_TRY(workspace(WS_SPLITTASK).get((size_t)ni * per, &mem));
+      uint8_t* lbase = (uint8_t*)mem;
+      uint8_t* rbase = lbase + (size_t)ni * (l_b + le_b);
+      std::vector<SliceStackLJob> lj(ni);
+      std::vector<SliceTaskRJob> rj;
+      std::map<const double2*, int> bid;
+      std::vector<const double2*> blks;
+      auto block_index = [&](const double2* p) {
+        auto b = bid.find(p);
+        if (b == bid.end()) {
+          b = bid.emplace(p, (int)blks.size()).first;
+          blks.push_back(p);
+        }
+        return b->second;
+      };
+      std::map<std::vector<uintptr_t>, int> rid;
+      std::vector<SplitGemmInst> gi(ni);
+      std::vector<double2*> outs((size_t)ni * SPLIT_TASK_NB, nullptr);
+      for (int i = 0; i < ni; i++) {
+        const Piece& pc = all[i0 + i];
+        const GridTask& G = grids[pc.g];
+        SliceStackLJob& L = lj[i];
+        std::memset(&L, 0, sizeof(L));
+        for (int q = 0; q < nterm; q++) {
+          int ex;
+          std::frexp(G.w[q], &ex);
+          L.w[q] = G.w[q];
+          L.wexp[q] = ex - 1;
+        }
+        for (int sl = 0; sl < pc.ns; sl++)
+          for (int q = 0; q < nterm; q++) {
+            const double2* a = G.A[(size_t)(pc.s0 + sl) * nterm + q];
+            L.a[sl][q] = a;
+            L.bi[sl][q] = block_index(a);
+          }
+        L.nslab = pc.ns;
+        L.nterm = nterm;
+        L.dag = G.adag;
+        L.eplus = eplus;
+        L.out = lbase + (size_t)i * (l_b + le_b);
+        L.exps = (int*)(L.out + l_b);
+        std::vector<uintptr_t> key;
+        for (int j = 0; j < nb; j++)
+          for (int q = 0; q < nterm; q++) key.push_back((uintptr_t)G.B[j][q]);
+        key.push_back((uintptr_t)G.bdag);
+        auto it = rid.find(key);
+        if (it == rid.end()) {
+          SliceTaskRJob R;
+          std::memset(&R, 0, sizeof(R));
+          R.nb = nb;
+          R.nterm = nterm;
+          R.eplus = eplus;
+          R.dag = G.bdag;
+          for (int j = 0; j < nb; j++)
+            for (int q = 0; q < nterm; q++) {
+              R.b[j][q] = G.B[j][q];
+              R.bi[j][q] = block_index(G.B[j][q]);
+            }
+          R.out = rbase + rj.size() * (r_b + re_b);
+          R.exps = (int*)(R.out + r_b);
+          it = rid.emplace(key, (int)rj.size()).first;
+          rj.push_back(R);
+        }
+        for (int j = 0; j < nb; j++) outs[(size_t)i * SPLIT_TASK_NB + j] = G.C0[j] + (size_t)pc.s0 * N2;
+        gi[i] = SplitGemmInst{L.out, rj[it->second].out, L.exps, rj[it->second].exps, nullptr, nullptr};
+      }
+      void* d1[4];
+      CTR_TRY(upload_group(WS_SPLITJOBS,
+                           {{lj.data(), lj.size() * sizeof(SliceStackLJob)},
+                            {rj.data(), rj.size() * sizeof(SliceTaskRJob)},
+                            {outs.data(), outs.size() * sizeof(double2*)},
+                            {blks.data(), blks.size() * sizeof(const double2*)}},
+                           d1, stream));
+      for (int i = 0; i < ni; i++) gi[i].outs = (double2* const*)d1[2] + (size_t)i * SPLIT_TASK_NB;
+      void* d_gi;
+      CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
+      void* d_bexp;
+      CTR_TRY(workspace(WS_BLOCKEXP).get(blks.size() * 2 * N * sizeof(int), &d_bexp));
+      CTR_TRY(launch_block_exp((const double2* const*)d1[3], (int)blks.size(), N, (int*)d_bexp, stream));
+      CTR_TRY(launch_slice_stack_left((const SliceStackLJob*)d1[0], ni, N, nchunk, mtiles, (const int*)d_bexp,
+                                      stream));
+      CTR_TRY(launch_slice_task_right((const SliceTaskRJob*)d1[1], (int)rj.size(), N, nchunk, ntiles,
+                                      (const int*)d_bexp, stream));
+      SplitGemmBatch B{(const SplitGemmInst*)d_gi, mtiles, ntiles, nchunk, ns * N, nb * N, mtiles * SPLIT_M,
+                       nullptr, 1, N, 1};
+      CTR_TRY(launch_split_gemm(B, ni, d_err, stream));
+      if (!capturing()) g_split_products += (double)ni * ns * nb * nterm;
     }
   }
   return CTR_OK;

@@ -586,6 +586,74 @@ __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJo
   for (int i = threadIdx.x; i < C::A_STAGE / 16; i += 256) d[i] = src[i];
 }
 
+// Stacked left operand slices: CTA = (job, M tile, K chunk).  Row g of the stack
+// is row g % nev of slab g / nev; 128 rows x 16 k, 8 elements a thread.
+template <class C>
+__global__ void __launch_bounds__(256) slice_stack_left_kernel(const SliceStackLJob* __restrict__ jobs, int nev,
+                                                               int nchunk, int mtiles, const int* __restrict__ bexp) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  int* sexp = (int*)sm;
+  uint8_t* stage = sm + 512;
+  const int kc = blockIdx.x % nchunk, t = blockIdx.x / nchunk;
+  const SliceStackLJob& J = jobs[t / mtiles];
+  const int mt = t % mtiles;
+  const int K = J.nterm * nev, rows = J.nslab * nev;
+  if (threadIdx.x < SPLIT_M) {
+    const int g = mt * SPLIT_M + threadIdx.x;
+    int e = -30000;
+    if (g < rows) {
+      const int sl = g / nev, r = g - sl * nev;
+      for (int q = 0; q < J.nterm; q++) {
+        const int b = bexp[((size_t)J.bi[sl][q] * 2 + ((J.dag >> q) & 1)) * nev + r];
+        if (b > -30000) e = max(e, b + J.wexp[q]);
+      }
+    }
+    const int E = (e < -1000 ? 0 : e) + J.eplus;
+    sexp[threadIdx.x] = E;
+    if (kc == 0) J.exps[g] = E;
+  }
+  constexpr int PER = SPLIT_M * SPLIT_K / 256;
+  double2 v[PER];
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 256;
+    const int rr = e >> 4, k = kc * SPLIT_K + (e & 15);
+    const int g = mt * SPLIT_M + rr;
+    v[u] = make_double2(0.0, 0.0);
+    if (k < K && g < rows) {
+      const int sl = g / nev, r = g - sl * nev, q = k / nev, j = k - q * nev;
+      double2 x;
+      if ((J.dag >> q) & 1) {
+        x = J.a[sl][q][(size_t)j * nev + r];
+        x.y = -x.y;
+      } else {
+        x = J.a[sl][q][(size_t)r * nev + j];
+      }
+      const double w = (double)J.w[q];
+      v[u] = make_double2(x.x * w, x.y * w);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 256;
+    const int rr = e >> 4, kk = e & 15;
+    const int E = sexp[rr];
+    bool nr, ni;
+    const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v[u].x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v[u].y, E, ni));
+    const uint32_t off = core_offset(rr, kk);
+#pragma unroll
+    for (int s = 0; s < C::NS; s++) {
+      *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::A_SUB + off) = slice_bf16(Ur, s, nr);
+      *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::A_SUB + off) = slice_bf16(Ui, s, ni);
+    }
+  }
+  __syncthreads();
+  int4* d = (int4*)(J.out + ((size_t)mt * nchunk + kc) * C::A_STAGE);
+  const int4* src = (const int4*)stage;
+  for (int i = threadIdx.x; i < C::A_STAGE / 16; i += 256) d[i] = src[i];
+}
+
 // Right operand slices: CTA = (job, N tile, K chunk); BN columns x 16 k.
 template <class C>
 __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
@@ -1470,7 +1538,7 @@ static int ensure_smem(K kernel, size_t smem, bool& done) {
 }
 static bool g_attr_sls = false, g_attr_srs = false, g_attr_tg = false, g_attr_sld = false, g_attr_srd = false;
 static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr = false, g_attr_std = false,
-            g_attr_hp = false;
+            g_attr_hp = false, g_attr_stl = false;
 static int g_nsm = 0;
 
 template <class C>
@@ -1502,6 +1570,7 @@ int split_kernels_prepare() {
   CTR_TRY(ensure_smem(trace_groups_kernel, trace_groups_max_smem(), g_attr_tg));
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
+  CTR_TRY(ensure_smem(slice_stack_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_stl));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
   return CTR_OK;
@@ -1570,6 +1639,19 @@ int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int 
   return CTR_OK;
 }
 
+int launch_slice_stack_left(const SliceStackLJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, const int* bexp,
+                            cudaStream_t s) {
+  if (njobs == 0) return CTR_OK;
+  const size_t smem = 512 + CfgHP::A_STAGE;
+  CTR_TRY(ensure_smem(slice_stack_left_kernel<CfgHP>, smem, g_attr_stl));
+  const long long grid = (long long)njobs * mtiles * nchunk;
+  if (grid > 0x7fffffffLL) return fail(CTR_ERR_ARG, "stacked slicer: grid too large");
+  TimedLaunch tl(s, "slice_stack_left");
+  slice_stack_left_kernel<CfgHP><<<(unsigned)grid, 256, smem, s>>>(d_jobs, nev, nchunk, mtiles, bexp);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, const int* bexp,
                             cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
@@ -1609,6 +1691,9 @@ static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err,
   TimedLaunch tl(s, name);
   split_gemm_kernel<C><<<grid, gemm_threads<C>(), smem, s>>>(g, (int)total, d_err);
   CTR_CUDA(cudaGetLastError());
+  // slice pairs i + j < NS, each two packed MMAs of M x 2BN x 16: 8 M BN 16 flops
+  if (!capturing())
+    g_split_mma_flops += (double)total * (C::NS * (C::NS + 1) / 2) * 8.0 * SPLIT_M * C::BN * SPLIT_K * g.nchunk;
   return CTR_OK;
 }
 

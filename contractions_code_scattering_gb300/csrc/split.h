@@ -126,6 +126,21 @@ struct SliceTaskRJob {
   int* exps;     // [ntiles * CfgHP::BN]
 };
 
+// Stacked left operand of a block grid (the task form with M stacking): slab s
+// (< nslab) contributes Nev rows of sum_q w_q op(a[s][q]) (terms along K as in
+// SliceTaskLJob); the slabs follow one another along M, so an M tile may span
+// several slabs.  The weights and transposes are the same for every slab.
+constexpr int SPLIT_STACK = 32;
+struct SliceStackLJob {
+  const double2* a[SPLIT_STACK][4];
+  int bi[SPLIT_STACK][4];
+  float w[4];
+  int wexp[4];
+  int nslab, nterm, dag, eplus;
+  uint8_t* out;  // [mtiles][nchunk][CfgHP::A_STAGE]
+  int* exps;     // [mtiles * SPLIT_M]
+};
+
 // Closing trace of one two-sided row: element offsets of its A block (cd, L)
 // and B block (ab, R) inside a pair's product matrices, and its coefficient.
 struct TraceRow {
@@ -220,6 +235,10 @@ int launch_block_exp(const double2* const* d_blk, int nblk, int nev, int* bexp, 
 int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int nchunk, const int* bexp,
                            cudaStream_t s);
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, const int* bexp,
+                            cudaStream_t s);
+// Stacked left operands of block grids: CTA = (job, M tile, K chunk), every job of
+// the launch with mtiles M tiles.
+int launch_slice_stack_left(const SliceStackLJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, const int* bexp,
                             cudaStream_t s);
 
 }  // namespace ctr

@@ -106,6 +106,31 @@ int ctr_pipi(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin,
              const double* prop_diag, const double* p1, const double* p2, const double* p3, const double* p4,
              double* corr, void* stream);
 
+/* pi pi for many momentum sets in one call (a batched form of ctr_pipi, no counterpart in the
+ * reference, which takes one set of four elementals per call): phi [Nt][nphi][N][N] holds every
+ * elemental; set s contracts with P1..P4 = phi[:, sets[4s + k]] (k = 0..3, host array
+ * [nset][4]).  corr [nset][tf_end-tf_begin][Nt][5], each set's entries as ctr_pipi gives them.
+ * Block products and traces that several sets share (e.g. Phi(q) tau, tau Phi(q) tau^dag for the
+ * sets (p, -p) and (-p, p)) are computed once; every stage of a pair batch is one launch. */
+int ctr_pipi_sets(int engine, int nev, int nt, int tf_begin, int tf_end, int isospin, const double* prop_rows,
+                  const double* prop_diag, const double* phi, int nphi, int nset, const int32_t* sets, double* corr,
+                  void* stream);
+
+/* rho -> pi pi (the three polarisations) and sigma -> pi pi (triangle, horizontal fish) for
+ * many pion momentum pairs in one call (a batched form of ctr_rhopi and ctr_sigmapi, no
+ * counterpart in the reference, which takes one pair per call): set s uses
+ * P1 = phi[:, sets[2s]], P2 = phi[:, sets[2s + 1]] (phi [Nt][nphi][N][N], sets host [nset][2]);
+ * the sink operators mom5_p1p2 [Nt][5][N][N] (rho) and mom2_p1p2 [Nt][2][N][N] (sigma) are
+ * the same for every set.  Both families contract X = tau(tf,ti) G R(ti),
+ * R = Phi_P2 taud Phi_P1: X is computed once per set and pair and multiplied by all the
+ * sink operators the outputs need in one stacked launch.  Outputs (each may be NULL; then
+ * its operands may be NULL too): rhopi [nset][3][tf_end-tf_begin][Nt][4] (idir 0..2, as
+ * ctr_rhopi), triangle [nset][tf_end-tf_begin][Nt][2] and hor_fish [nset][Nt] (as ctr_sigmapi). */
+int ctr_rhopi_sigmapi_sets(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
+                           const double* prop_diag, const double* phi, int nphi, const double* mom5_p1p2,
+                           const double* mom2_p1p2, int nset, const int32_t* sets, double* rhopi, double* triangle,
+                           double* hor_fish, void* stream);
+
 /* Loop with unit spin structure (run_ContractLoopUnity, lib/contract_kernels_loop_unity.cu:45-107):
  * loop[t] = sum_s Tr[tau(t,t)_{ss} Phi(t)]. */
 int ctr_loop_unity(int engine, int nev, int nt, const double* prop_diag, const double* mom, double* loop,
@@ -293,6 +318,12 @@ int ctr_split_available(void);
 int ctr_split_set_refine(double rel_tol);
 /* Number of entries the last split call recomputed. */
 long long ctr_split_refined(void);
+/* Work of the split engine's high-precision and standard GEMM launches since the
+ * last reset: executed_mma = BF16 tensor-core flops executed, padding included;
+ * block_products = Nev x Nev complex block products of the high-precision (chain)
+ * launches, 8 Nev^3 FP64-equivalent flops each.  Eager launches only (replays of
+ * recorded graphs are not counted).  reset != 0 zeroes both after reading. */
+int ctr_split_flops(double* executed_mma, double* block_products, int reset);
 
 /* Synchronise the stream and report the first device-side error flag. */
 int ctr_sync(void* stream);

@@ -222,18 +222,88 @@ def _i1_from_i0_rows(d):
 @pytest.mark.parametrize("engine,tol", [("fp64", TOL), ("split", 1e-9)])
 @pytest.mark.parametrize("iso", [0, 1])
 def test_pipi_19_pair_set(pipi19, engine, iso, tol):
+    """Each pair through ctr_pipi, and all 19 sets in one ctr_pipi_sets call (bitwise the same)."""
     c = pipi19
     dv, tf = c["dev"], c["tf"]
     row = dv["prop"][tf:tf + 1].contiguous()
+    moms = list(dv["phi"])
+    phi_all = torch.stack([dv["phi"][p] for p in moms], dim=1).contiguous()
+    sets = [(moms.index(a), moms.index(b), moms.index(a), moms.index(b)) for a, b in c["pairs"]]
+    batched = _np(api.run_contract_pipi_sets(row, dv["diag"], phi_all, sets, iso, engine=engine,
+                                             tf_range=(tf, tf + 1)))
     stats = []
-    for a, b in c["pairs"]:
+    for k, (a, b) in enumerate(c["pairs"]):
         d = c["refs"][(a, b)]
         ref = d["corr"] if iso == 0 else _i1_from_i0_rows(d)
         pa, pb = dv["phi"][a], dv["phi"][b]
         got = _np(api.run_contract_pipi(row, dv["diag"], pa, pb, pa, pb, iso, engine=engine, tf_range=(tf, tf + 1)))
         stats.append(P.entrywise(got[0], ref, tol, P.pipi_rows_abs(d, iso), "pair %s I%d %s" % (a, iso, engine)))
+        assert np.array_equal(batched[k], got), "set %d: ctr_pipi_sets differs from ctr_pipi" % k
     print("pipi 19 pairs I%d %s: worst per-entry rel %.2e, %d entries needed the floor"
           % (iso, engine, max(s["max_rel"] for s in stats), sum(s["needed_floor"] for s in stats)))
+
+
+@pytest.mark.parametrize("engine", ["fp64", "split"])
+@pytest.mark.parametrize("iso", [0, 1])
+def test_pipi_sets_bitwise_equal_to_per_set_calls(cuda, engine, iso):
+    """ctr_pipi_sets on sets that share elementals (p, -p), (-p, p), an asymmetric set and
+    p = 0: every set's entries are bitwise those of its own ctr_pipi call, over a t_sink
+    row range."""
+    nt, n = 4, 12
+    prop = synth.make_prop(nt, n, seed=1500)
+    moms = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 1), (0, -1, -1)]
+    phis = synth.make_phi_momenta(nt, n, moms, seed=1501)
+    phi_all = _dev(np.stack([phis[p] for p in moms], axis=1), cuda)
+    sets = [(1, 2, 1, 2), (2, 1, 2, 1), (1, 2, 3, 4), (0, 0, 0, 0), (3, 4, 3, 4)]
+    tp = _dev(prop, cuda)
+    diag = api.prop_diag(tp)
+    tr = (1, 3)
+    rows = tp[tr[0]:tr[1]].contiguous()
+    got = _np(api.run_contract_pipi_sets(rows, diag, phi_all, sets, iso, engine=engine, tf_range=tr))
+    for k, q in enumerate(sets):
+        ps = [phi_all[:, j].contiguous() for j in q]
+        one = _np(api.run_contract_pipi(rows, diag, *ps, iso, engine=engine, tf_range=tr))
+        assert np.array_equal(got[k], one), "set %d (%s engine)" % (k, engine)
+    ref, ab = ref_pipi(prop, [phis[moms[j]] for j in sets[2]], iso, range(tr[0], tr[1]))
+    P.entrywise(got[2], ref, TOL if engine == "fp64" else SPLIT_TOL, ab, "asymmetric set vs oracle")
+
+
+@pytest.mark.parametrize("engine", ["fp64", "split"])
+def test_rhopi_sigmapi_sets_bitwise_equal_to_per_set_calls(cuda, engine):
+    """ctr_rhopi_sigmapi_sets: every set's rho -> pi pi (three polarisations), sigma -> pi pi
+    triangle and horizontal fish are bitwise those of its own ctr_rhopi / ctr_sigmapi calls,
+    over a t_sink row range, with sets that share elementals; one set against the oracle."""
+    nt, n = 4, 12
+    prop = synth.make_prop(nt, n, seed=1600, decay=0.25)
+    moms = [(0, 0, 0), (1, 1, 0), (-1, -1, 0), (0, 0, 1), (0, 0, -1)]
+    phis = synth.make_phi_momenta(nt, n, moms, seed=1601)
+    phi_all = _dev(np.stack([phis[p] for p in moms], axis=1), cuda)
+    rng = np.random.default_rng(1602)
+    mom5 = np.ascontiguousarray(np.stack([synth.make_phi_random(nt, n, rng) for _ in range(5)], axis=1))
+    mom2 = np.ascontiguousarray(np.stack([synth.make_phi_random(nt, n, rng) for _ in range(2)], axis=1))
+    d5, d2 = _dev(mom5, cuda), _dev(mom2, cuda)
+    sets = [(1, 2), (2, 1), (3, 4), (0, 0), (1, 4)]
+    tp = _dev(prop, cuda)
+    diag = api.prop_diag(tp)
+    tr = (1, 3)
+    rows = tp[tr[0]:tr[1]].contiguous()
+    got = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(rows, diag, phi_all, sets, d5, d2, engine=engine,
+                                                                     tf_range=tr).items()}
+    for k, (a, b) in enumerate(sets):
+        pa, pb = phi_all[:, a].contiguous(), phi_all[:, b].contiguous()
+        for idir in range(3):
+            one = _np(api.run_contract_rhopi(rows, diag, pa, pb, d5, idir, engine=engine, tf_range=tr))
+            assert np.array_equal(got["rhopi"][k, idir], one), "set %d idir %d (%s)" % (k, idir, engine)
+        hf, tri = api.run_contract_sigmapi(rows, diag, pa, pb, d2, engine=engine, tf_range=tr)
+        assert np.array_equal(got["triangle"][k], _np(tri)), "set %d triangle (%s)" % (k, engine)
+        assert np.array_equal(got["hor_fish"][k], _np(hf)), "set %d hor fish (%s)" % (k, engine)
+    tol = TOL if engine == "fp64" else SPLIT_TOL
+    ref, ab = ref_rhopi(prop, phis[moms[1]], phis[moms[4]], mom5, 2, range(tr[0], tr[1]))
+    P.entrywise(got["rhopi"][4, 2], ref, tol, ab, "set (1,4) rho-pipi idir 2 vs oracle")
+    ref, ab = ref_triangle(prop, phis[moms[1]], phis[moms[4]], mom2, range(tr[0], tr[1]))
+    P.entrywise(got["triangle"][4], ref, tol, ab, "set (1,4) triangle vs oracle")
+    ref, ab = ref_hor_fish(prop, phis[moms[1]], phis[moms[4]])
+    P.entrywise(got["hor_fish"][4], ref, tol, ab, "set (1,4) hor fish vs oracle")
 
 
 def test_block_product_tasks_split_vs_fp64(cuda):
