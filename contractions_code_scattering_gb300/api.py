@@ -182,25 +182,26 @@ def run_contract_pipi_sets(prop_rows, diag, phi, sets, isospin, engine="fp64", t
 
 
 def run_contract_rhopi_sigmapi_sets(prop_rows, diag, phi, sets, mom5=None, mom2=None, engine="fp64", tf_range=None,
-                                    rhopi=True, triangle=True, hor_fish=True, stream=None):
+                                    rhopi=True, triangle=True, hor_fish=True, out=None, stream=None):
     """rho -> pi pi (3 polarisations) and sigma -> pi pi for many pion pairs in one call
     (include/ctr.h: ctr_rhopi_sigmapi_sets).  phi: [Nt, nphi, N, N]; sets: [nset, 2]
     indices of (P1, P2); mom5 [Nt, 5, N, N], mom2 [Nt, 2, N, N].  Returns a dict with
     'rhopi' [nset, 3, rows, Nt, 4], 'triangle' [nset, rows, Nt, 2], 'hor_fish' [nset, Nt]
-    for the outputs requested (device)."""
+    for the outputs requested (device); out: a dict of such tensors to fill instead."""
     import torch
     nt, nphi, nev = phi.shape[0], phi.shape[1], phi.shape[-1]
     sets = np.ascontiguousarray(np.asarray(sets, dtype=np.int32).reshape(-1, 2))
     ns = len(sets)
     tf0, tf1 = _rows(tf_range, nt)
     kw = dict(dtype=torch.complex128, device=phi.device)
-    out = {}
-    if rhopi:
-        out["rhopi"] = torch.empty((ns, 3, tf1 - tf0, nt, 4), **kw)
-    if triangle:
-        out["triangle"] = torch.empty((ns, tf1 - tf0, nt, 2), **kw)
-    if hor_fish:
-        out["hor_fish"] = torch.empty((ns, nt), **kw)
+    if out is None:
+        out = {}
+        if rhopi:
+            out["rhopi"] = torch.empty((ns, 3, tf1 - tf0, nt, 4), **kw)
+        if triangle:
+            out["triangle"] = torch.empty((ns, tf1 - tf0, nt, 2), **kw)
+        if hor_fish:
+            out["hor_fish"] = torch.empty((ns, nt), **kw)
     opt = lambda t, name: _dev(t, name) if t is not None else None
     check(lib().ctr_rhopi_sigmapi_sets(_engine(engine), nev, nt, tf0, tf1,
                                        opt(prop_rows, "prop_rows") if (rhopi or triangle) else None, _dev(diag, "diag"),

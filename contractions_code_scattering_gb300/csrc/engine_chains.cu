@@ -651,6 +651,18 @@ int pipi_sets(int N, int Nt, int tf_begin, int tf_end, int iso, const double* pr
     ydt[k] = fam(cL[k], cDt[k]);
   }
   const int nYF = (int)YF.size();
+  std::vector<std::vector<int>> yby;  // Y families grouped by their left combo
+  {
+    std::map<int, int> at;
+    for (int f = 0; f < nYF; f++) {
+      auto it = at.find(YF[f].first);
+      if (it == at.end()) {
+        it = at.emplace(YF[f].first, (int)yby.size()).first;
+        yby.emplace_back();
+      }
+      yby[it->second].push_back(f);
+    }
+  }
   // F = Phi_qf(tf) Pm(qp): per Pm index, the elementals it is multiplied by
   std::vector<std::vector<int>> FK(nW);
   std::vector<int> fpos(nset * 2);
@@ -794,17 +806,28 @@ int pipi_sets(int N, int Nt, int tf_begin, int tf_end, int iso, const double* pr
           }
           g0.push_back(std::move(gv));
         }
-      // Ysq / Ydt = X G R: slab (pair, row block a), right block b of R(t_src)
-      for (int f = 0; f < nYF; f++) {
-        GridTask gy = grid(4 * m, 4, 4, g5w, 0, 0);
-        for (int pp = 0; pp < m; pp++)
-          for (int a = 0; a < 4; a++)
-            for (int kk = 0; kk < 4; kk++) gy.A[(size_t)(pp * 4 + a) * 4 + kk] = Xblk(YF[f].first, i0 + pp, a, kk);
-        for (int j = 0; j < 4; j++) {
-          for (int kk = 0; kk < 4; kk++) gy.B[j][kk] = M[(size_t)YF[f].second * Nt + ti] + (size_t)(kk * 4 + j) * N2;
-          gy.C0[j] = bY[(size_t)g * nYF + f] + (size_t)j * 4 * m * N2;
+      // Ysq / Ydt = X G R: slab (pair, row block a), right block b of R(t_src).  The
+      // families with the same left X (a set's Ysq and Ydt) share one grid of up to
+      // 8 right blocks, so that X's rows are sliced once for both.
+      for (size_t h = 0; h < yby.size(); h++) {
+        const std::vector<int>& fl = yby[h];
+        for (size_t f0 = 0; f0 < fl.size(); f0 += 2) {
+          const int nf = (int)std::min<size_t>(2, fl.size() - f0);
+          GridTask gy = grid(4 * m, 4 * nf, 4, g5w, 0, 0);
+          const int cl = YF[fl[f0]].first;
+          for (int pp = 0; pp < m; pp++)
+            for (int a = 0; a < 4; a++)
+              for (int kk = 0; kk < 4; kk++) gy.A[(size_t)(pp * 4 + a) * 4 + kk] = Xblk(cl, i0 + pp, a, kk);
+          for (int u = 0; u < nf; u++) {
+            const int f = fl[f0 + u];
+            for (int j = 0; j < 4; j++) {
+              for (int kk = 0; kk < 4; kk++)
+                gy.B[u * 4 + j][kk] = M[(size_t)YF[f].second * Nt + ti] + (size_t)(kk * 4 + j) * N2;
+              gy.C0[u * 4 + j] = bY[(size_t)g * nYF + f] + (size_t)j * 4 * m * N2;
+            }
+          }
+          g1.push_back(std::move(gy));
         }
-        g1.push_back(std::move(gy));
       }
     }
     if (iso == 0)

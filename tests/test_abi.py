@@ -47,3 +47,23 @@ def test_twosided_rejects_bad_rows():
                         coef.ctypes.data_as(ctypes.c_void_p), oi.ctypes.data_as(ctypes.c_void_p), 1, p, None)
     assert rc == 1
     assert b"spin index" in L.ctr_last_error()
+
+
+def test_momentum_set_calls_reject_bad_arguments():
+    """The set calls check their sizes, isospin, pointers and elemental indices before
+    touching a device (no GPU needed)."""
+    L = lib()
+    fake = ctypes.c_void_p(1 << 20)  # aligned stand-in: rejected before any use
+    sets = (ctypes.c_int32 * 4)(0, 1, 0, 5)
+    rc = L.ctr_pipi_sets(0, 8, 4, 0, 4, 0, fake, fake, fake, 3, 1, ctypes.cast(sets, ctypes.c_void_p), fake, None)
+    assert rc == 1 and b"not in [0,3)" in L.ctr_last_error()
+    assert L.ctr_pipi_sets(0, 8, 4, 0, 4, 2, fake, fake, fake, 3, 1, ctypes.cast(sets, ctypes.c_void_p), fake,
+                           None) == 1
+    assert L.ctr_pipi_sets(0, 8, 4, 0, 4, 0, None, fake, fake, 3, 1, ctypes.cast(sets, ctypes.c_void_p), fake,
+                           None) == 1
+    pairs = (ctypes.c_int32 * 2)(0, 7)
+    rc = L.ctr_rhopi_sigmapi_sets(0, 8, 4, 0, 4, fake, fake, fake, 3, fake, fake, 1,
+                                  ctypes.cast(pairs, ctypes.c_void_p), fake, fake, fake, None)
+    assert rc == 1 and b"not in [0,3)" in L.ctr_last_error()
+    assert L.ctr_rhopi_sigmapi_sets(0, 8, 4, 2, 1, fake, fake, fake, 3, fake, fake, 1,
+                                    ctypes.cast(pairs, ctypes.c_void_p), fake, fake, fake, None) == 1

@@ -199,6 +199,52 @@ def test_graph_chain_families(cuda, chains, engine, tol):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("engine,tol", [("fp64", 1e-15), ("split", 1e-15), ("split", 1e-9)])
+def test_graph_momentum_set_calls(cuda, engine, tol):
+    """ctr_pipi_sets and ctr_rhopi_sigmapi_sets recorded in one graph (the split engine's
+    refinement between segments at tol 1e-15): the replay equals the eager calls bitwise."""
+    nt, n = 3, 12
+    prop = torch.from_numpy(synth.make_prop(nt, n, seed=1700)).to(cuda)
+    moms = [(0, 0, 0), (1, 0, 0), (-1, 0, 0)]
+    phis = synth.make_phi_momenta(nt, n, moms, seed=1701)
+    phi = torch.from_numpy(np.ascontiguousarray(np.stack([phis[p] for p in moms], axis=1))).to(cuda)
+    rng = np.random.default_rng(1702)
+    mom5 = torch.from_numpy(np.ascontiguousarray(np.stack([synth.make_phi_random(nt, n, rng) for _ in range(5)],
+                                                          axis=1))).to(cuda)
+    mom2 = mom5[:, :2].contiguous()
+    diag = api.prop_diag(prop)
+    s = torch.cuda.Stream()
+    pp_sets, rs_sets = [(1, 2, 1, 2), (2, 1, 2, 1), (0, 0, 0, 0)], [(1, 2), (2, 1), (0, 0)]
+
+    def outs():
+        kw = dict(dtype=torch.complex128, device=cuda)
+        return dict(pp=torch.empty((3, nt, nt, 5), **kw),
+                    rs=dict(rhopi=torch.empty((3, 3, nt, nt, 4), **kw), triangle=torch.empty((3, nt, nt, 2), **kw),
+                            hor_fish=torch.empty((3, nt), **kw)))
+
+    def calls(o):
+        api.run_contract_pipi_sets(prop, diag, phi, pp_sets, 0, engine=engine, out=o["pp"], stream=s)
+        api.run_contract_rhopi_sigmapi_sets(prop, diag, phi, rs_sets, mom5, mom2, engine=engine, out=o["rs"], stream=s)
+
+    try:
+        _refine(tol)
+        eager, rec = outs(), outs()
+        torch.cuda.synchronize()
+        calls(eager)
+        s.synchronize()
+        with api.Graph(s) as g:
+            calls(rec)
+        g.launch(s)
+        s.synchronize()
+        assert np.array_equal(rec["pp"].cpu().numpy(), eager["pp"].cpu().numpy())
+        for k in eager["rs"]:
+            assert np.array_equal(rec["rs"][k].cpu().numpy(), eager["rs"][k].cpu().numpy()), k
+        g.close()
+    finally:
+        _refine(1e-9)
+
+
+@pytest.mark.gpu
 def test_graph_rejects_host_planned_calls(cuda):
     """A call that plans on device data cannot be recorded: ctr_graph_end fails and the stream stays usable."""
     nt, n = 2, 8
