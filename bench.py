@@ -49,7 +49,7 @@ def parse():
                                                               "gives a small case of the same kernels, e.g. for ncu)")
     ap.add_argument("--nev", type=int, default=NEV)
     ap.add_argument("--configs", type=int, default=1, help="append one timed step of the pi pi (19 pairs), mixed "
-                    "(Nev=128) and reference-kernel workloads to the headline line (0 = skip)")
+                    "(Nev=128), profile-adjoint and reference-kernel workloads to the headline line (0 = skip)")
     ap.add_argument("--mixed-form", default="sets", choices=["sets", "pairs"],
                     help="mixed workload: one ctr_rhopi_sigmapi_sets call for the 27 pairs, or calls per pair")
     ap.add_argument("--pipi-form", default="sets", choices=["sets", "pairs"],
@@ -574,7 +574,8 @@ def main():
         del tau, phi, out
         torch.cuda.synchronize()
         line["configs"] = {}
-        for name, fn in (("pipi", pipi_block), ("mixed", mixed_block), ("legacy_gpu", legacy_block)):
+        for name, fn in (("pipi", pipi_block), ("mixed", mixed_block), ("adjoint", adjoint_block),
+                         ("legacy_gpu", legacy_block)):
             try:
                 line["configs"][name] = fn(args)
             except Exception as e:  # recorded, so that the headline line still prints
@@ -999,6 +1000,10 @@ def mixed_block(args, full=False):
 
 
 def run_adjoint(args):
+    print(json.dumps(adjoint_block(args, full=True)))
+
+
+def adjoint_block(args, full=False):
     """Distillation-profile objective and its gradient at Nev=100, Lt=64: rho (p=0) for
     t = 2..9 and the pi pi I=0 set at dt = 4, f_k = exp(-lambda_k/0.3); forward plus
     backward per evaluation, and FP64 central differences (h = 1e-6) on a few f_k."""
@@ -1027,7 +1032,8 @@ def run_adjoint(args):
         L.backward()
         return L.item(), f.grad
 
-    t, launches, kern = _timed(evaluate, args.steps, args.warmup)
+    steps, warm = (args.steps, args.warmup) if full else (1, 1)
+    t, launches, kern = _timed(evaluate, steps, warm)
     L, grad = evaluate()
     grad = grad.cpu().numpy()
     kw64 = dict(kw, engine="fp64")  # the differences are taken on the FP64 forward
@@ -1043,13 +1049,15 @@ def run_adjoint(args):
         fd[k] = (lp - lm) / (2 * h)
     worst = max(abs(fd[k] - grad[k]) for k in fd) / np.abs(grad).max()
     line = {"workload": "adjoint", "metric": "profile objective + gradient evaluations/s @Nev=100,Lt=64",
-            "value": 1.0 / t, "unit": "evaluations/s", "ms_per_evaluation": 1e3 * t, "steps": args.steps,
+            "value": 1.0 / t, "unit": "evaluations/s", "ms_per_evaluation": 1e3 * t, "steps": steps,
             "engine": kw["engine"],
-            "warmup": args.warmup, "objective": L, "grad_norm": float(np.linalg.norm(grad)),
+            "warmup": warm, "objective": L, "grad_norm": float(np.linalg.norm(grad)),
             "fd_check": {"h": h, "forward": "fp64 engine", "components": {str(k): [fd[k], float(grad[k])] for k in fd},
                          "max_abs_diff_over_max_grad": worst},
-            "gpu_launches": launches, "kernels": kern}
-    print(json.dumps(line))
+            "gpu_launches": launches, "kernels": {k: v for k, v in kern.items() if not k.startswith("_")}}
+    del tau, phis, extra, mom5
+    torch.cuda.synchronize()
+    return line
 
 
 def run_legacy_gpu(args):

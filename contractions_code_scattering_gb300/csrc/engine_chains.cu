@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <utility>
 
 #include "kernels.h"
@@ -1169,23 +1170,31 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
 namespace {
 
 // Row sums of batch items whose rows' trace values sit anywhere: row r of item it
-// is trace slot rowslot[it * nrows + r]; output o sums rows idx[off[o] .. off[o+1])
-// in that order into out[ent[it] * nout + o]; with trabs, entries whose error
-// estimate exceeds the tolerance append ent * nout + o to the refinement list.
+// is trace slot rowslot[it * nrows + r], times rcoef[r] where given; output o sums
+// rows idx[off[o] .. off[o+1]) in that order into out[ent[it] * nout + o]; with
+// trabs, entries whose error estimate exceeds the tolerance append ent * nout + o
+// to the refinement list.
 __global__ void rowsum_items_kernel(const double2* __restrict__ trv, const double* __restrict__ trabs,
                                     const int* __restrict__ rowslot, int nrows, const int* __restrict__ off,
-                                    const int* __restrict__ idx, int nout, const int* __restrict__ ent, int nitem,
-                                    double2* __restrict__ out, double eps_over_tol, int* __restrict__ count,
-                                    int* __restrict__ list) {
+                                    const int* __restrict__ idx, const float2* __restrict__ rcoef, int nout,
+                                    const int* __restrict__ ent, int nitem, double2* __restrict__ out,
+                                    double eps_over_tol, int* __restrict__ count, int* __restrict__ list) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= nitem * nout) return;
   const int it = g / nout, o = g % nout;
   double re = 0.0, im = 0.0, sc = 0.0;
   for (int k = off[o]; k < off[o + 1]; k++) {
-    const int j = rowslot[(size_t)it * nrows + idx[k]];
-    re += trv[j].x;
-    im += trv[j].y;
-    if (trabs) sc += trabs[j];
+    const int r = idx[k], j = rowslot[(size_t)it * nrows + r];
+    double2 v = trv[j];
+    double a = trabs ? trabs[j] : 0.0;
+    if (rcoef) {  // the row's coefficient, applied as the trace kernel applies it
+      const double2 c = make_double2((double)rcoef[r].x, (double)rcoef[r].y);
+      v = cmul(c, v);
+      a = sqrt(c.x * c.x + c.y * c.y) * a;
+    }
+    re += v.x;
+    im += v.y;
+    sc += a;
   }
   const size_t e = (size_t)ent[it] * nout + o;
   out[e] = make_double2(re, im);
@@ -1197,8 +1206,10 @@ __global__ void rowsum_items_kernel(const double2* __restrict__ trv, const doubl
 // Item tables of one row-sum launch (host), and their device copies.
 struct RowItems {
   std::vector<int> slot, csr, ent;
+  std::vector<float2> coef;  // per row, or empty
   int nrows = 0, nout = 0;
   const int *d_slot = nullptr, *d_csr = nullptr, *d_ent = nullptr;
+  const float2* d_coef = nullptr;
 };
 
 // Uploads the tables of several row-sum launches in one staging copy.
@@ -1208,13 +1219,15 @@ int upload_items(const Ctx& c, std::vector<RowItems*> items) {
     parts.push_back({r->slot.data(), r->slot.size() * sizeof(int)});
     parts.push_back({r->csr.data(), r->csr.size() * sizeof(int)});
     parts.push_back({r->ent.data(), r->ent.size() * sizeof(int)});
+    parts.push_back({r->coef.data(), r->coef.size() * sizeof(float2)});
   }
   std::vector<void*> d(parts.size());
   CTR_TRY(upload_group(WS_MISC, parts, d.data(), c.s));
   for (size_t i = 0; i < items.size(); i++) {
-    items[i]->d_slot = (const int*)d[3 * i];
-    items[i]->d_csr = (const int*)d[3 * i + 1];
-    items[i]->d_ent = (const int*)d[3 * i + 2];
+    items[i]->d_slot = (const int*)d[4 * i];
+    items[i]->d_csr = (const int*)d[4 * i + 1];
+    items[i]->d_ent = (const int*)d[4 * i + 2];
+    items[i]->d_coef = items[i]->coef.empty() ? nullptr : (const float2*)d[4 * i + 3];
   }
   return CTR_OK;
 }
@@ -1225,8 +1238,8 @@ int rowsum_items(const Ctx& c, const double2* trv, const double* tra, const RowI
   TimedLaunch tl(c.s, "rowsum_items");
   const int n = (int)r.ent.size() * r.nout;
   rowsum_items_kernel<<<(n + 127) / 128, 128, 0, c.s>>>(trv, rf.on ? tra : nullptr, r.d_slot, r.nrows, r.d_csr,
-                                                        r.d_csr + r.nout + 1, r.nout, r.d_ent, (int)r.ent.size(), out,
-                                                        rf.eps_over_tol, rf.count, rf.list);
+                                                        r.d_csr + r.nout + 1, r.d_coef, r.nout, r.d_ent,
+                                                        (int)r.ent.size(), out, rf.eps_over_tol, rf.count, rf.list);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
@@ -1355,6 +1368,22 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       ops.push_back(5 + ik);
     }
   const int nops = (int)ops.size();
+  // the distinct traces (slab, X block, tau block) of the three polarisations' groups
+  std::vector<std::tuple<int, int, int>> uniq;
+  std::vector<int> uidx[3];
+  if (rhopi) {
+    std::map<std::tuple<int, int, int>, int> at;
+    for (int idir = 0; idir < 3; idir++)
+      for (const Grp& g : grp[idir]) {
+        const auto key = std::make_tuple(g.slab, g.s5 * 4 + g.s2, g.s3 * 4 + g.s2);
+        auto it = at.find(key);
+        if (it == at.end()) {
+          it = at.emplace(key, (int)uniq.size()).first;
+          uniq.push_back(key);
+        }
+        uidx[idir].push_back(it->second);
+      }
+  }
   std::vector<int> csr_tr = {0, 16, 32};
   for (int k = 0; k < 32; k++) csr_tr.push_back(k);
 
@@ -1363,7 +1392,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
     for (int tfl = 0; tfl < rows; tfl++) order[k++] = tfl * Nt + ti;
   const int ngr = rhopi ? (int)grp[0].size() : 0;
   const size_t blk_pair = 16 * (size_t)nC * (1 + nops);
-  const size_t tr_pair = (size_t)nset * ((rhopi ? 3 * ngr : 0) + (tri ? 32 : 0));
+  const size_t tr_pair = (size_t)nset * (uniq.size() + (tri ? 32 : 0));
   const size_t per_pair = blk_pair * N2 * sizeof(double2) + tr_pair * (sizeof(double2) + sizeof(double));
   const int batch = std::max(1, std::min(npairs, (int)(sets_budget() / std::max<size_t>(per_pair, 1))));
   Refine rf_rp, rf_tr;
@@ -1463,6 +1492,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       it_rp[idir].nrows = ngr;
       it_rp[idir].nout = 4;
       it_rp[idir].csr = csr_rp[idir];
+      for (const Grp& g : grp[idir]) it_rp[idir].coef.push_back(make_float2(g.cre, g.cim));
     }
     it_tr.nrows = 32;
     it_tr.nout = 2;
@@ -1472,13 +1502,17 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       const int pair = order[p0 + i];
       for (int k = 0; k < nset; k++) {
         const int ci = cR[k];
-        if (rhopi)
+        if (rhopi) {
+          // Tr-Had(Phi_ip X_{s5 s2}, tau_{s3 s2}) without its coefficient, once for the three
+          // polarisations (those of ip = 0, 1 are shared); the row sums apply the coefficients
+          const int base = (int)tp.tt.size();
+          for (const auto& u : uniq)
+            tp.add(Yblk(std::get<0>(u), ci, i, std::get<1>(u)), T + std::get<2>(u) * N2, 1.f, 0.f, 0);
           for (int idir = 0; idir < 3; idir++) {
-            for (const Grp& g : grp[idir])
-              it_rp[idir].slot.push_back(tp.add(Yblk(g.slab, ci, i, g.s5 * 4 + g.s2), T + (g.s3 * 4 + g.s2) * N2,
-                                                g.cre, g.cim, 0));
+            for (int g = 0; g < ngr; g++) it_rp[idir].slot.push_back(base + uidx[idir][g]);
             it_rp[idir].ent.push_back((k * 3 + idir) * npairs + pair);
           }
+        }
         if (tri) {
           for (int ik = 0; ik < 2; ik++)
             for (int b = 0; b < 16; b++)
