@@ -164,7 +164,8 @@ def test_mixed_config_shape_split(cuda):
     which the split engine's leading level stays exact; perambulator decay 0.25,
     momentum elementals Phi(+-p) for p = (1,1,1) and random rho / sigma operators.
     rho -> pi pi (3 polarisations), sigma -> pi pi (triangle and horizontal fish) and
-    the sigma loops, per entry against the oracle on t_sink rows 0 and 2."""
+    the sigma loops, per entry against the oracle on t_sink rows 0 and 2; the batched
+    ctr_rhopi_sigmapi_sets gives the same bits."""
     nt, n = 3, 128
     prop = synth.make_prop(nt, n, seed=900, decay=0.25)
     moms = [(1, 1, 1), (-1, -1, -1)]
@@ -191,6 +192,14 @@ def test_mixed_config_shape_split(cuda):
         got = _np(api.run_contract_loop_unity(diag, d2[:, k].contiguous(), engine="split"))
         ref, ab = ref_loop(prop, mom2[:, k])
         P.entrywise(got, ref, tol, ab, "sigma loop %d" % k)
+    # the same pair through the batched call (with the reversed pair as a second set): bitwise
+    phi_all = torch.stack([dp1, dp2], dim=1).contiguous()
+    bat = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(tp, diag, phi_all, [(0, 1), (1, 0)], d5, d2,
+                                                                     engine="split").items()}
+    for idir in range(3):
+        assert np.array_equal(bat["rhopi"][0, idir], _np(api.run_contract_rhopi(tp, diag, dp1, dp2, d5, idir,
+                                                                                 engine="split")))
+    assert np.array_equal(bat["triangle"][0], _np(tri)) and np.array_equal(bat["hor_fish"][0], _np(hf))
 
 
 @pytest.fixture(scope="module")
