@@ -968,17 +968,18 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
     if (s1 != 0) continue;  // one representative per group
     grp.push_back(Grp{bx / 64, s2, s3, s5, Tb.rhopi_ip[r], Tb.rhopi_coef[r][0] * G5[s1], Tb.rhopi_coef[r][1] * G5[s1]});
   }
-  // distinct products Phi_ip(tf) X_{s5 s2}
-  std::vector<int> pkeys;  // ip*16 + s5*4 + s2
+  // The trace of a row, Tr-Had(Phi_ip(tf) X_{s5 s2}, tau_{s3 s2}), is taken as
+  // Tr-Had(X_{s5 s2}, Z) with Z = Phi_ip(tf)^dag tau_{s3 s2}: the same sum, but Z does not
+  // depend on the pion pair (P1, P2), so a batch of pairs shares it, and it does not
+  // wait for X.  Distinct Z products (ip, s3, s2):
+  std::vector<int> zkeys;  // ip*16 + s3*4 + s2
   for (auto& g : grp) {
-    int k = g.ip * 16 + g.s5 * 4 + g.s2;
-    if (std::find(pkeys.begin(), pkeys.end(), k) == pkeys.end()) pkeys.push_back(k);
+    int k = g.ip * 16 + g.s3 * 4 + g.s2;
+    if (std::find(zkeys.begin(), zkeys.end(), k) == zkeys.end()) zkeys.push_back(k);
   }
-  const int nprod = (int)pkeys.size(), ngrp = (int)grp.size();
-  const int nbuf = 1 + (nprod + 15) / 16;
+  const int nprod = (int)zkeys.size(), ngrp = (int)grp.size();
   const size_t per_pair = (size_t)(16 + nprod) * N2 * sizeof(double2) + ngrp * sizeof(double2);
   const int batch = batch_pairs(per_pair, npairs);
-  (void)nbuf;
   Refine rf;
   CTR_TRY(refine_begin(c, (size_t)npairs * 4, WS_REFINE, rf));
   std::vector<int> off(5, 0), idx(ngrp);
@@ -1001,29 +1002,28 @@ int rhopi_chain(int N, int Nt, int tf_begin, int tf_end, int idir, const double*
     double2* Bm = (double2*)mem;
     double2* TR = (double2*)trm;
     double* TRA = (double*)tra;
-    std::vector<ZTask> st1, st2;
+    std::vector<ZTask> st1;
     std::vector<TraceTask> tt;
     for (int q = 0; q < np; q++) {
       const int pr = pair_of(p0 + q), tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
       const double2* T = tau + ((size_t)tfl * Nt + ti) * blk16;
       double2* X = Bm + (size_t)q * (16 + nprod) * N2;
-      double2* Y = X + blk16;
+      double2* Z = X + blk16;
       block_gemm_g5(c, T, R + ti * blk16, X, st1);  // X = T G R
       for (int k = 0; k < nprod; k++) {
-        const int ip = pkeys[k] / 16, s5 = (pkeys[k] / 4) % 4, s2 = pkeys[k] % 4;
-        st2.push_back(zt(P12 + ((size_t)tf * 5 + ip) * N2, X + (s5 * 4 + s2) * N2, Y + k * N2));
+        const int ip = zkeys[k] / 16, s3 = (zkeys[k] / 4) % 4, s2 = zkeys[k] % 4;
+        st1.push_back(zt(P12 + ((size_t)tf * 5 + ip) * N2, T + (s3 * 4 + s2) * N2, Z + k * N2, 1));  // Phi^dag tau
       }
       for (int g = 0; g < ngrp; g++) {
-        const int k = (int)(std::find(pkeys.begin(), pkeys.end(), grp[g].ip * 16 + grp[g].s5 * 4 + grp[g].s2) -
-                            pkeys.begin());
-        tt.push_back(tr(Y + k * N2, T + (grp[g].s3 * 4 + grp[g].s2) * N2, TR + (size_t)q * ngrp + g, grp[g].cre,
+        const int k = (int)(std::find(zkeys.begin(), zkeys.end(), grp[g].ip * 16 + grp[g].s3 * 4 + grp[g].s2) -
+                            zkeys.begin());
+        tt.push_back(tr(X + (grp[g].s5 * 4 + grp[g].s2) * N2, Z + k * N2, TR + (size_t)q * ngrp + g, grp[g].cre,
                         grp[g].cim, 0));
       }
     }
     if (TRA)
       for (size_t k = 0; k < tt.size(); k++) tt[k].absout = TRA + (tt[k].out - TR);
     CTR_TRY(run_stage(c, st1, WS_TASKS));
-    CTR_TRY(run_stage(c, st2, WS_TASKS2));
     CTR_TRY(run_traces(c, tt));
     if (rf.on)
       CTR_TRY(launch_rowsum_refine(TR, TRA, ngrp, (const int*)d_csr, (const int*)d_csr + 5, 4, np,
@@ -1104,8 +1104,10 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
                        }));
   }
   if (!tri) return CTR_OK;
-  // triangle (lib/calculate_sigmapi_triangle_core.h): X = T G R, Y_{ik, s1 s5} = Phix2_ik(tf) X_{s1 s5},
-  // trace vs tau_{s1 s5}, weight g5(s1)
+  // triangle (lib/calculate_sigmapi_triangle_core.h): X = T G R and the trace
+  // Tr-Had(Phix2_ik(tf) X_{s1 s5}, tau_{s1 s5}) with weight g5(s1), taken as
+  // Tr-Had(X_{s1 s5}, Z_{ik, s1 s5}) with Z = Phix2_ik(tf)^dag tau_{s1 s5}, which does not
+  // depend on the pion pair and does not wait for X.
   const size_t per_pair = (size_t)(16 + 32) * N2 * sizeof(double2) + 32 * sizeof(double2);
   const int batch = batch_pairs(per_pair, npairs);
   std::vector<int> csr(3 + 32);
@@ -1124,24 +1126,23 @@ int sigmapi_chain(int N, int Nt, int tf_begin, int tf_end, const double* prop_ro
     double2* Bm = (double2*)mem;
     double2* TR = (double2*)trm;
     double* TRA = (double*)tra;
-    std::vector<ZTask> st1, st2;
+    std::vector<ZTask> st1;
     std::vector<TraceTask> tt;
     for (int q = 0; q < np; q++) {
       const int pr = pair_of(p0 + q), tfl = pr / Nt, ti = pr % Nt, tf = tf_begin + tfl;
       const double2* T = tau + ((size_t)tfl * Nt + ti) * blk16;
       double2* X = Bm + (size_t)q * 48 * N2;
-      double2* Y = X + blk16;
+      double2* Z = X + blk16;
       block_gemm_g5(c, T, R + ti * blk16, X, st1);
       for (int ik = 0; ik < 2; ik++)
         for (int b = 0; b < 16; b++) {
-          st2.push_back(zt(Px2 + ((size_t)tf * 2 + ik) * N2, X + b * N2, Y + (ik * 16 + b) * N2));
-          tt.push_back(tr(Y + (ik * 16 + b) * N2, T + b * N2, TR + (size_t)q * 32 + ik * 16 + b,
+          st1.push_back(zt(Px2 + ((size_t)tf * 2 + ik) * N2, T + b * N2, Z + (ik * 16 + b) * N2, 1));
+          tt.push_back(tr(X + b * N2, Z + (ik * 16 + b) * N2, TR + (size_t)q * 32 + ik * 16 + b,
                           (float)G5[b / 4], 0.f, 0));
           if (TRA) tt.back().absout = TRA + (size_t)q * 32 + ik * 16 + b;
         }
     }
     CTR_TRY(run_stage(c, st1, WS_TASKS));
-    CTR_TRY(run_stage(c, st2, WS_TASKS2));
     CTR_TRY(run_traces(c, tt));
     if (rf.on)
       CTR_TRY(launch_rowsum_refine(TR, TRA, 32, (const int*)d_csr, (const int*)d_csr + 3, 2, np,
@@ -1368,7 +1369,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       ops.push_back(5 + ik);
     }
   const int nops = (int)ops.size();
-  // the distinct traces (slab, X block, tau block) of the three polarisations' groups
+  // the distinct traces (slab, X block, Z block) of the three polarisations' groups
   std::vector<std::tuple<int, int, int>> uniq;
   std::vector<int> uidx[3];
   if (rhopi) {
@@ -1391,7 +1392,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
   for (int ti = 0, k = 0; ti < Nt; ti++)
     for (int tfl = 0; tfl < rows; tfl++) order[k++] = tfl * Nt + ti;
   const int ngr = rhopi ? (int)grp[0].size() : 0;
-  const size_t blk_pair = 16 * (size_t)nC * (1 + nops);
+  const size_t blk_pair = 16 * ((size_t)nC + nops);
   const size_t tr_pair = (size_t)nset * (uniq.size() + (tri ? 32 : 0));
   const size_t per_pair = blk_pair * N2 * sizeof(double2) + tr_pair * (sizeof(double2) + sizeof(double));
   const int batch = std::max(1, std::min(npairs, (int)(sets_budget() / std::max<size_t>(per_pair, 1))));
@@ -1424,17 +1425,16 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       pos[i] = gr.back().second++;
     }
     const int ng = (int)gr.size();
-    std::vector<double2*> bX((size_t)ng * nC), bY((size_t)np * nC);
+    std::vector<double2*> bX((size_t)ng * nC), bZ(np);
     for (int g = 0; g < ng; g++)
       for (int ci = 0; ci < nC; ci++) bX[(size_t)g * nC + ci] = alloc(16 * (size_t)gr[g].second);
-    for (int i = 0; i < np; i++)
-      for (int ci = 0; ci < nC; ci++) bY[(size_t)i * nC + ci] = alloc(16 * (size_t)nops);
-    // X(ci, i)_{a b} and Y(op slab, ci, i)_b
+    for (int i = 0; i < np; i++) bZ[i] = alloc(16 * (size_t)nops);
+    // X(ci, i)_{a b} and Z(op slab, i)_b = Op(tf)^dag tau_b (shared by all sets)
     auto Xblk = [&](int ci, int i, int a, int b) {
       return bX[(size_t)gof[i] * nC + ci] + ((size_t)b * 4 * gr[gof[i]].second + pos[i] * 4 + a) * N2;
     };
-    auto Yblk = [&](int sl, int ci, int i, int b) { return bY[(size_t)i * nC + ci] + ((size_t)b * nops + sl) * N2; };
-    std::vector<GridTask> g0, g1;
+    auto Zblk = [&](int sl, int i, int b) { return bZ[i] + ((size_t)b * nops + sl) * N2; };
+    std::vector<GridTask> g0;
     for (int g = 0; g < ng; g++) {
       const int i0 = gr[g].first, m = gr[g].second, ti = tiv[i0];
       for (int ci = 0; ci < nC; ci++) {
@@ -1459,27 +1459,27 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       }
     }
     for (int i = 0; i < np; i++)
-      for (int ci = 0; ci < nC; ci++)
-        for (int jb = 0; jb < 2; jb++) {
-          // Y = Op(tf) X_b: slab = sink operator, right block b of X
-          GridTask gy;
-          std::memset(gy.B, 0, sizeof(gy.B));
-          std::memset(gy.C0, 0, sizeof(gy.C0));
-          std::copy(one, one + 4, gy.w);
-          gy.nslab = nops;
-          gy.nb = 8;
-          gy.nterm = 1;
-          gy.adag = gy.bdag = 0;
-          gy.A.resize(nops);
-          for (int sl = 0; sl < nops; sl++)
-            gy.A[sl] = ops[sl] < 5 ? P5 + ((size_t)tfv[i] * 5 + ops[sl]) * N2 : P2x + ((size_t)tfv[i] * 2 + ops[sl] - 5) * N2;
-          for (int j = 0; j < 8; j++) {
-            const int b = 8 * jb + j;
-            gy.B[j][0] = Xblk(ci, i, b / 4, b % 4);
-            gy.C0[j] = bY[(size_t)i * nC + ci] + (size_t)b * nops * N2;
-          }
-          g1.push_back(std::move(gy));
+      for (int jb = 0; jb < 2; jb++) {
+        // Z = Op(tf)^dag tau_b: slab = sink operator, right block b of tau
+        GridTask gz;
+        std::memset(gz.B, 0, sizeof(gz.B));
+        std::memset(gz.C0, 0, sizeof(gz.C0));
+        std::copy(one, one + 4, gz.w);
+        gz.nslab = nops;
+        gz.nb = 8;
+        gz.nterm = 1;
+        gz.adag = 1;
+        gz.bdag = 0;
+        gz.A.resize(nops);
+        for (int sl = 0; sl < nops; sl++)
+          gz.A[sl] = ops[sl] < 5 ? P5 + ((size_t)tfv[i] * 5 + ops[sl]) * N2 : P2x + ((size_t)tfv[i] * 2 + ops[sl] - 5) * N2;
+        for (int j = 0; j < 8; j++) {
+          const int b = 8 * jb + j;
+          gz.B[j][0] = Tv[i] + (size_t)b * N2;
+          gz.C0[j] = bZ[i] + (size_t)b * nops * N2;
         }
+        g0.push_back(std::move(gz));
+      }
     // traces
     const size_t ntr = (size_t)np * tr_pair;
     double2* trv = base + used;
@@ -1498,16 +1498,16 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
     it_tr.nout = 2;
     it_tr.csr = csr_tr;
     for (int i = 0; i < np; i++) {
-      const double2* T = Tv[i];
       const int pair = order[p0 + i];
       for (int k = 0; k < nset; k++) {
         const int ci = cR[k];
         if (rhopi) {
-          // Tr-Had(Phi_ip X_{s5 s2}, tau_{s3 s2}) without its coefficient, once for the three
+          // Tr-Had(X_{s5 s2}, Phi_ip^dag tau_{s3 s2}) without its coefficient, once for the three
           // polarisations (those of ip = 0, 1 are shared); the row sums apply the coefficients
           const int base = (int)tp.tt.size();
           for (const auto& u : uniq)
-            tp.add(Yblk(std::get<0>(u), ci, i, std::get<1>(u)), T + std::get<2>(u) * N2, 1.f, 0.f, 0);
+            tp.add(Xblk(ci, i, std::get<1>(u) / 4, std::get<1>(u) % 4), Zblk(std::get<0>(u), i, std::get<2>(u)), 1.f,
+                   0.f, 0);
           for (int idir = 0; idir < 3; idir++) {
             for (int g = 0; g < ngr; g++) it_rp[idir].slot.push_back(base + uidx[idir][g]);
             it_rp[idir].ent.push_back((k * 3 + idir) * npairs + pair);
@@ -1516,7 +1516,8 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
         if (tri) {
           for (int ik = 0; ik < 2; ik++)
             for (int b = 0; b < 16; b++)
-              it_tr.slot.push_back(tp.add(Yblk(slab_of[5 + ik], ci, i, b), T + b * N2, (float)G5[b / 4], 0.f, 0));
+              it_tr.slot.push_back(
+                  tp.add(Xblk(ci, i, b / 4, b % 4), Zblk(slab_of[5 + ik], i, b), (float)G5[b / 4], 0.f, 0));
           it_tr.ent.push_back(k * npairs + pair);
         }
       }
@@ -1526,7 +1527,6 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       if (tra) tp.tt[k].absout = tra + k;
     }
     CTR_TRY(run_grids(c, g0, WS_TASKS));
-    CTR_TRY(run_grids(c, g1, WS_TASKS2));
     CTR_TRY(run_traces(c, tp.tt));
     CTR_TRY(upload_items(c, {&it_rp[0], &it_rp[1], &it_rp[2], &it_tr}));
     for (int idir = 0; idir < 3 && rhopi; idir++)

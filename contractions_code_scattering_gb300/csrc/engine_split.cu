@@ -910,6 +910,19 @@ int zgemm_split_grids(int N, const std::vector<GridTask>& grids, cudaStream_t st
                                       (const int*)d_bexp, stream));
       SplitGemmBatch B{(const SplitGemmInst*)d_gi, mtiles, ntiles, nchunk, ns * N, nb * N, mtiles * SPLIT_M,
                        nullptr, 1, N, 1};
+      // persistent tile walk (N tiles or M tiles innermost), autotuned per tile shape
+      // by re-launching the GEMM on the same operands (it rewrites the same outputs)
+      char gshape[96];
+      snprintf(gshape, sizeof(gshape), "hp,m=%d,n=%d,k=%d", mtiles, ntiles, nchunk);
+      int order = 0;
+      CTR_TRY(tune_resolve("split_gemm.order", gshape, 2, 0, stream,
+                           [&](int c) {
+                             SplitGemmBatch t = B;
+                             t.order = c;
+                             return launch_split_gemm(t, ni, d_err, stream);
+                           },
+                           &order));
+      B.order = order;
       CTR_TRY(launch_split_gemm(B, ni, d_err, stream));
       if (!capturing()) g_split_products += (double)ni * ns * nb * nterm;
     }
