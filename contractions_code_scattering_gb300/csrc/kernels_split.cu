@@ -785,43 +785,98 @@ __device__ __forceinline__ double pow2d(int e) {
 template <int NTHR>
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(NTHR) : "memory"); }
 
-// All MMAs of one K chunk: NS(NS+1)/2 slice pairs (i + j < NS) x 4 real
-// products into the 2 NL level accumulators.  adesc / bdesc describe sub-tile
-// (slice 0, re) of the stage; the other sub-tiles are constant byte offsets
-// (added as offset >> 4 to the start-address field, which cannot carry:
-// shared addresses are < 2^18).
+// TMEM hand-back groups: the epilogue drains the level accumulators in groups,
+// levels {0, 1} first, then each further level on its own, and hands every
+// group back as soon as it holds it in registers.  The first K chunk of the
+// next tile issues its MMAs group by group, each after that group's hand-back,
+// so the MMAs of the early levels run while later levels are still drained.
 template <class C>
-__device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
+constexpr int tmem_groups() { return C::NL - 1; }
+__host__ __device__ constexpr int level_group(int l) { return l <= 1 ? 0 : l - 1; }
+
+// The MMAs of one slice pair (i, j) of one K chunk into its level accumulator.
+// adesc / bdesc describe sub-tile (slice 0, re) of the stage; the other
+// sub-tiles are constant byte offsets (added as offset >> 4 to the
+// start-address field, which cannot carry: shared addresses are < 2^18).
+template <class C, int I, int J>
+__device__ __forceinline__ void issue_pair(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
   constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, C::BN, false);
   constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, C::BN, true);
   constexpr uint32_t id_wide = idesc_bf16_f32(SPLIT_M, 2 * C::BN, false);
-#pragma unroll
-  for (int i = 0; i < C::NS; i++) {
-#pragma unroll
-    for (int j = 0; j + i < C::NS; j++) {
-      const int lvl = (i + j) < C::NL - 1 ? (i + j) : C::NL - 1;
-      // in loop order the first pair of level l is (0, l)
-      const uint32_t accum = (!first_chunk || !(i == 0 && j <= C::NL - 1)) ? 1u : 0u;
-      const uint64_t ar = adesc + (uint64_t)(((i * 2 + 0) * C::A_SUB) >> 4);
-      const uint64_t ai = adesc + (uint64_t)(((i * 2 + 1) * C::A_SUB) >> 4);
-      if (C::PACK) {
-        // planes -Yi, Yr, Yi of slice j are adjacent along N (row groups 256 B apart)
-        const uint64_t b_nr = bdesc + (uint64_t)(((j * 3 + 0) * C::B_SUB) >> 4);  // [-Yi | Yr]
-        const uint64_t b_ri = bdesc + (uint64_t)(((j * 3 + 1) * C::B_SUB) >> 4);  // [Yr | Yi]
-        const uint32_t d = tbase + (uint32_t)C::acc_col(0, lvl);
-        umma_f16(d, ar, b_ri, id_wide, accum);  // [Re | Im] += Xr [Yr | Yi]
-        umma_f16(d, ai, b_nr, id_wide, 1u);     // [Re | Im] += Xi [-Yi | Yr]
-      } else {
-        const uint64_t br = bdesc + (uint64_t)(((j * 2 + 0) * C::B_SUB) >> 4);
-        const uint64_t bi = bdesc + (uint64_t)(((j * 2 + 1) * C::B_SUB) >> 4);
-        const uint32_t dre = tbase + (uint32_t)C::acc_col(0, lvl);
-        const uint32_t dim = tbase + (uint32_t)C::acc_col(1, lvl);
-        umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
-        umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
-        umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
-        umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
-      }
+  constexpr int lvl = (I + J) < C::NL - 1 ? (I + J) : C::NL - 1;
+  // in i-major order the first pair of level l is (0, l)
+  const uint32_t accum = (!first_chunk || !(I == 0 && J <= C::NL - 1)) ? 1u : 0u;
+  const uint64_t ar = adesc + (uint64_t)(((I * 2 + 0) * C::A_SUB) >> 4);
+  const uint64_t ai = adesc + (uint64_t)(((I * 2 + 1) * C::A_SUB) >> 4);
+  if constexpr (C::PACK) {
+    // planes -Yi, Yr, Yi of slice j are adjacent along N (row groups 256 B apart)
+    const uint64_t b_nr = bdesc + (uint64_t)(((J * 3 + 0) * C::B_SUB) >> 4);  // [-Yi | Yr]
+    const uint64_t b_ri = bdesc + (uint64_t)(((J * 3 + 1) * C::B_SUB) >> 4);  // [Yr | Yi]
+    const uint32_t d = tbase + (uint32_t)C::acc_col(0, lvl);
+    umma_f16(d, ar, b_ri, id_wide, accum);  // [Re | Im] += Xr [Yr | Yi]
+    umma_f16(d, ai, b_nr, id_wide, 1u);     // [Re | Im] += Xi [-Yi | Yr]
+  } else {
+    const uint64_t br = bdesc + (uint64_t)(((J * 2 + 0) * C::B_SUB) >> 4);
+    const uint64_t bi = bdesc + (uint64_t)(((J * 2 + 1) * C::B_SUB) >> 4);
+    const uint32_t dre = tbase + (uint32_t)C::acc_col(0, lvl);
+    const uint32_t dim = tbase + (uint32_t)C::acc_col(1, lvl);
+    umma_f16(dre, ar, br, id_pos, accum);  // Re += Xr Yr
+    umma_f16(dre, ai, bi, id_neg, 1u);     // Re -= Xi Yi
+    umma_f16(dim, ar, bi, id_pos, accum);  // Im += Xr Yi
+    umma_f16(dim, ai, br, id_pos, 1u);     // Im += Xi Yr
+  }
+}
+
+// The slice pairs (i, j), i + j < NS, whose level falls in hand-back group G
+// (G < 0: all pairs), in i-major order.  Every level accumulator sees its
+// pairs in the same order whatever the grouping, so the FP32 last level sums
+// them in the same order and the results do not depend on it.
+template <class C, int G, int I = 0, int J = 0>
+__device__ __forceinline__ void issue_pairs(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
+  if constexpr (I < C::NS) {
+    if constexpr (I + J < C::NS) {
+      constexpr int lvl = (I + J) < C::NL - 1 ? (I + J) : C::NL - 1;
+      if constexpr (G < 0 || level_group(lvl) == G) issue_pair<C, I, J>(tbase, adesc, bdesc, first_chunk);
+      issue_pairs<C, G, I, J + 1>(tbase, adesc, bdesc, first_chunk);
+    } else {
+      issue_pairs<C, G, I + 1, 0>(tbase, adesc, bdesc, first_chunk);
     }
+  }
+}
+
+// All MMAs of one K chunk: NS(NS+1)/2 slice pairs (i + j < NS) into the NL
+// level accumulators.
+template <class C>
+__device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
+  issue_pairs<C, -1>(tbase, adesc, bdesc, first_chunk);
+}
+
+// The MMAs of hand-back group g (runtime index) of one K chunk.
+template <class C>
+__device__ __forceinline__ void issue_group(int g, uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
+  static_assert(tmem_groups<C>() >= 2 && tmem_groups<C>() <= 4, "hand-back groups");
+  if (g == 0)
+    issue_pairs<C, 0>(tbase, adesc, bdesc, first_chunk);
+  else if (g == 1)
+    issue_pairs<C, 1>(tbase, adesc, bdesc, first_chunk);
+  else if (g == 2)
+    issue_pairs<C, 2>(tbase, adesc, bdesc, first_chunk);
+  else if constexpr (tmem_groups<C>() > 3)
+    issue_pairs<C, 3>(tbase, adesc, bdesc, first_chunk);
+}
+
+// NC consecutive TMEM columns of this warp's 32 lanes into v (NC = 16, 12, 8 or 4).
+template <int NC>
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float* v) {
+  static_assert(NC % 4 == 0 && NC <= 16, "TMEM load width");
+  if constexpr (NC == 16) {
+    tmem_ld16(taddr, v);
+  } else if constexpr (NC >= 8) {
+    tmem_ld8(taddr, v);
+    if constexpr (NC > 8) tmem_ld_cols<NC - 8>(taddr + 8, v + 8);
+  } else {
+    tmem_ld4(taddr, v);
+    if constexpr (NC > 4) tmem_ld_cols<NC - 4>(taddr + 4, v + 4);
   }
 }
 
@@ -850,8 +905,8 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
   uint64_t* full = (uint64_t*)(smem + NSTAGE * (C::A_STAGE + C::B_STAGE));
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = empty + NSTAGE;
-  uint64_t* tempty = tfull + 1;
-  uint64_t* drainb = tempty + 1;
+  uint64_t* tempty = tfull + 1;  // one per hand-back group
+  uint64_t* drainb = tempty + tmem_groups<C>();
   uint32_t* tslot = (uint32_t*)(drainb + 1);
   int* sexp = (int*)(tslot + 4);  // C::BN column exponents of the current tile
   // complex128 output: destination of row 0 of each column of the current tile
@@ -867,7 +922,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, C::EPI_WARPS);  // one arrival per epilogue warp
+    for (int g = 0; g < tmem_groups<C>(); g++) mbar_init(&tempty[g], C::EPI_WARPS);  // one arrival per epilogue warp
     mbar_init(drainb, 1);
     fence_mbar_init();
     // A CTA that starts after another one recorded a failure does nothing.
@@ -914,13 +969,6 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
       const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
       for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x, local++) {
-        // wait until the epilogue drained the previous tile's accumulators
-        if (local > 0 && !mbar_wait(tempty, (local - 1) & 1, 2 * WAIT_NS, err)) {
-          atomicExch(err, 4);
-          ok = false;
-          break;
-        }
-        tc_fence_after();
         for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
           const int s = g_chunk % NSTAGE;
           if (!mbar_wait(&full[s], (g_chunk / NSTAGE) & 1, WAIT_NS, err)) {
@@ -929,8 +977,23 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             break;
           }
           tc_fence_after();
-          issue_chunk<C>(tbase, adesc0 + (uint64_t)((s * C::A_STAGE) >> 4),
-                         bdesc0 + (uint64_t)((s * C::B_STAGE) >> 4), kc == 0);
+          const uint64_t ad = adesc0 + (uint64_t)((s * C::A_STAGE) >> 4);
+          const uint64_t bd = bdesc0 + (uint64_t)((s * C::B_STAGE) >> 4);
+          if (kc == 0) {
+            // first chunk: each group of levels once the epilogue handed it back
+            for (int grp = 0; grp < tmem_groups<C>() && ok; grp++) {
+              if (local > 0 && !mbar_wait(&tempty[grp], (local - 1) & 1, 2 * WAIT_NS, err)) {
+                atomicExch(err, 4);
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              issue_group<C>(grp, tbase, ad, bd, true);
+            }
+            if (!ok) break;
+          } else {
+            issue_chunk<C>(tbase, ad, bd, false);
+          }
           umma_commit(&empty[s]);  // stage s free once these MMAs have read it
         }
         if (ok) umma_commit(tfull);
@@ -979,6 +1042,12 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       // the MMA warp before it writes anything to global memory, so the next
       // tile's MMAs run while this tile's products are stored.
       const int cbase = half * CPW;
+      // hand TMEM group grp back to the MMA warp (after this warp's loads of it)
+      auto hand_back = [&](int grp) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[grp]);
+      };
       if constexpr (C::INT_OUT) {
         // complex128 output: the exact levels and the last one summed exactly
         // in 64-bit integers (units 2^-54 of the row/column scale; level 0 is
@@ -988,37 +1057,35 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
         // FP32 -> int32 conversion of v 2^(16+9l) is exact; the last level is
         // rounded to 2^-54 (|v| < 2^-24 there, so it fits an int32 as well;
         // 64-bit conversions would go through GB300's slow FP64 pipe).
-        constexpr int CW = C::EPI_CW;
+        // Integer sums do not depend on the order of the levels.
+        auto level_units = [](float v, int l) -> long long {
+          if (l < C::NL - 1) return (long long)__float2int_rn(v * __int_as_float((127 + 16 + 9 * l) << 23)) << (38 - 9 * l);
+          // the last level holds pairs i+j >= NL-1: |v| 2^54 <= 5 K 2^16 2^-52 2^54 < 2^30
+          return (long long)__float2int_rn(v * __int_as_float((127 + 54) << 23));
+        };
         long long acc[2][CPW];
 #pragma unroll
-        for (int cc = 0; cc < CPW; cc += CW) {
+        for (int part = 0; part < 2; part++) {  // group 0: levels 0 and 1
+          float v0[CPW], v1[CPW];
+          tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 0) + cbase), v0);
+          tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 1) + cbase), v1);
+          tmem_ld_wait();
+#pragma unroll
+          for (int c = 0; c < CPW; c++) acc[part][c] = level_units(v0[c], 0) + level_units(v1[c], 1);
+        }
+        hand_back(0);
+#pragma unroll
+        for (int l = 2; l < C::NL; l++) {  // group l - 1: level l
 #pragma unroll
           for (int part = 0; part < 2; part++) {
-            float v[C::NL][CW];
-#pragma unroll
-            for (int l = 0; l < C::NL; l++) {
-              if constexpr (CW == 8)
-                tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
-              else
-                tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
-            }
+            float v[CPW];
+            tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, l) + cbase), v);
             tmem_ld_wait();
 #pragma unroll
-            for (int c = 0; c < CW; c++) {
-              long long a = 0;
-#pragma unroll
-              for (int l = 0; l < C::NL - 1; l++)
-                a += (long long)__float2int_rn(v[l][c] * __int_as_float((127 + 16 + 9 * l) << 23)) << (38 - 9 * l);
-              // the last level holds pairs i+j >= NL-1: |v| 2^54 <= 5 K 2^16 2^-52 2^54 < 2^30
-              a += (long long)__float2int_rn(v[C::NL - 1][c] * __int_as_float((127 + 54) << 23));
-              acc[part][cc + c] = a;
-            }
+            for (int c = 0; c < CPW; c++) acc[part][c] += level_units(v[c], l);
           }
+          hand_back(l - 1);
         }
-        // accumulators drained: hand TMEM back to the MMA warp
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(tempty);
         if (rvalid) {
           const int erow = I->lexp[grow];
 #pragma unroll
@@ -1032,57 +1099,67 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
       } else {
         // float-float output: levels 0 .. NL-2 exact, combined by exact two-sums;
         // the rounding errors and the last level go to the low word.
-        // res[c] = (re hi, re lo, im hi, im lo) of column cbase + c.
-        constexpr int CW = C::EPI_CW;
+        // (s, e)[part][c]: running sum and error of column cbase + c; after
+        // the last level, (hi, lo).
         const int ldo = g.ldo;
-        float4 res[CPW];
+        if (g.levels) {
+          // raw level values for the exactness tests, read before any hand-back
+          // (the loads are warp-collective; rows past the end store nothing)
+#pragma unroll 1
+          for (int pl = 0; pl < 2 * C::NL; pl++) {
+            const int part = pl / C::NL, l = pl % C::NL;
 #pragma unroll
-        for (int cc = 0; cc < CPW; cc += CW) {
+            for (int cc = 0; cc < CPW; cc += 4) {
+              float v[4];
+              tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v);
+              tmem_ld_wait();
 #pragma unroll
-          for (int part = 0; part < 2; part++) {
-            float v[C::NL][CW];
-#pragma unroll
-            for (int l = 0; l < C::NL; l++) {
-              if constexpr (CW == 8)
-                tmem_ld8(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
-              else
-                tmem_ld4(tl + (uint32_t)(C::acc_col(part, l) + cbase + cc), v[l]);
-            }
-            tmem_ld_wait();
-            if (g.levels && rvalid) {
-              for (int c = 0; c < CW; c++) {
+              for (int c = 0; c < 4; c++) {
                 const int gcol = nt * C::BN + cbase + cc + c;
-                if (gcol < g.ncols)
-                  for (int l = 0; l < C::NL; l++)
-                    g.levels[((size_t)(part * C::NL + l) * g.ncols + gcol) * ldo + grow] = v[l][c];
-              }
-            }
-#pragma unroll
-            for (int c = 0; c < CW; c++) {
-              float s = v[0][c], e = 0.f;
-#pragma unroll
-              for (int l = 1; l < C::NL - 1; l++) {
-                float t, d;
-                two_sum(s, v[l][c], t, d);
-                s = t;
-                e += d;
-              }
-              float h, lw;
-              fast_two_sum(s, e + v[C::NL - 1][c], h, lw);
-              if (part == 0) {
-                res[cc + c].x = h;
-                res[cc + c].y = lw;
-              } else {
-                res[cc + c].z = h;
-                res[cc + c].w = lw;
+                if (rvalid && gcol < g.ncols) g.levels[((size_t)(part * C::NL + l) * g.ncols + gcol) * ldo + grow] = v[c];
               }
             }
           }
         }
-        // accumulators drained: hand TMEM back to the MMA warp
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(tempty);
+        float s[2][CPW], e[2][CPW];
+#pragma unroll
+        for (int part = 0; part < 2; part++) {  // group 0: levels 0 and 1
+          tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 0) + cbase), s[part]);
+          tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 1) + cbase), e[part]);
+          tmem_ld_wait();
+#pragma unroll
+          for (int c = 0; c < CPW; c++) {
+            float t, d;
+            two_sum(s[part][c], e[part][c], t, d);
+            s[part][c] = t;
+            e[part][c] = 0.f + d;
+          }
+        }
+        hand_back(0);
+#pragma unroll
+        for (int l = 2; l < C::NL; l++) {  // group l - 1: level l
+#pragma unroll
+          for (int part = 0; part < 2; part++) {
+            float v[CPW];
+            tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, l) + cbase), v);
+            tmem_ld_wait();
+#pragma unroll
+            for (int c = 0; c < CPW; c++) {
+              if (l < C::NL - 1) {
+                float t, d;
+                two_sum(s[part][c], v[c], t, d);
+                s[part][c] = t;
+                e[part][c] += d;
+              } else {
+                float h, lw;
+                fast_two_sum(s[part][c], e[part][c] + v[c], h, lw);
+                s[part][c] = h;
+                e[part][c] = lw;
+              }
+            }
+          }
+          hand_back(l - 1);
+        }
         if (rvalid && !g.levels) {
           float4* outp = I->out;
 #pragma unroll
@@ -1093,10 +1170,10 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             // scale stays well inside FP32's normal range; below 2^-100 the
             // product is written as NaN, which flags the entries that use it for
             // recomputation in FP64 range
-            const int e = erow + sexp[cbase + c];
-            const float sc = e < FF_MIN_EXP ? __int_as_float(0x7fc00000) : pow2f(e);
+            const int ex = erow + sexp[cbase + c];
+            const float sc = ex < FF_MIN_EXP ? __int_as_float(0x7fc00000) : pow2f(ex);
             outp[(size_t)gcol * ldo + grow] =
-                make_float4(res[c].x * sc, res[c].y * sc, res[c].z * sc, res[c].w * sc);
+                make_float4(s[0][c] * sc, e[0][c] * sc, s[1][c] * sc, e[1][c] * sc);
           }
         }
       }

@@ -83,6 +83,14 @@ Plan make_plan(int* status) {
     P.row_b[r] = (int16_t)ib;
     P.coef[r] = make_float2(T.rho_coef[r][0], T.rho_coef[r][1]);
   }
+  // Output r / 16 is the reference's rule; the table must agree with it: the 16
+  // spin rows of an output share one operator pair (lp, rp).  A table that
+  // breaks this is refused rather than summed into the wrong outputs.
+  for (int r = 0; r < kRows; r++)
+    if (T.rho_lprp[r][0] != T.rho_lprp[r & ~15][0] || T.rho_lprp[r][1] != T.rho_lprp[r & ~15][1]) {
+      *status = CTR_ERR_UNSUPPORTED;
+      return P;
+    }
   // CSR of the outputs: counts by output index r / 16, then rows in ascending order
   int cnt[kOut] = {};
   for (int r = 0; r < kRows; r++) cnt[r / 16]++;
@@ -166,7 +174,7 @@ int rho_noalloc(int N, int Nt, int tf, const double* prop_row, const double* mom
   if (need > kScratchBytes)
     return fail(CTR_ERR_ARG, "ctr_rho_noalloc: Nev=%d needs %zu bytes of scratch, the fixed maximum is %zu (Nev <= 114)",
                 N, need, kScratchBytes);
-  if (g_plan_status != CTR_OK) return fail(g_plan_status, "ctr_rho_noalloc: the rho table has too many blocks");
+  if (g_plan_status != CTR_OK) return fail(g_plan_status, "ctr_rho_noalloc: the rho table does not fit the fixed plan (too many blocks, or an output whose 16 rows mix operator pairs)");
   // Looked up on every call: cheap once the module is loaded, and never stale
   // after a cudaDeviceReset (which reloads the module elsewhere).
   void* base = nullptr;
