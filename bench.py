@@ -316,6 +316,11 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.tune_force:
+        from contractions_code_scattering_gb300 import api as _api
+        for kv in args.tune_force:
+            knob, val = kv.split("=")
+            _api.tune_force(knob, int(val))
     if args.workload != "rho":
         WORKLOADS[args.workload](args)
         return
@@ -326,9 +331,6 @@ def main():
     ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
     api.device_init(local)
-    for kv in args.tune_force:
-        knob, val = kv.split("=")
-        api.tune_force(knob, int(val))
     nt, nev = args.nt or NT, args.nev
     moms, rows, coef, oi, nout = workload(nt, nev)
     diagrams = nt * nt * nout
