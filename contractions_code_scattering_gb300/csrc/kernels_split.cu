@@ -739,15 +739,9 @@ constexpr uint64_t WAIT_NS = 2000000000ull;  // 2 s per wait
 
 constexpr int GEMM_SMEM_TAIL = 1024;  // barriers, TMEM slot, column exponents and output pointers
 
-// Bytes of one stage's right operand in a CTA: all planes, or the two planes a
-// CTA of a pair holds.
-template <class C, bool PAIR>
-constexpr int gemm_b_stage() {
-  return PAIR ? C::NS * 2 * C::B_SUB : C::B_STAGE;
-}
-template <class C, bool PAIR = false>
+template <class C>
 constexpr size_t gemm_smem_bytes() {
-  return (size_t)NSTAGE * (C::A_STAGE + gemm_b_stage<C, PAIR>()) + GEMM_SMEM_TAIL;
+  return (size_t)NSTAGE * (C::A_STAGE + C::B_STAGE) + GEMM_SMEM_TAIL;
 }
 static_assert(2 * CfgStd::NL * CfgStd::BN <= (int)TMEM_COLS && 2 * CfgHP::NL * CfgHP::BN <= (int)TMEM_COLS,
               "accumulators exceed TMEM");
@@ -788,6 +782,8 @@ __device__ __forceinline__ double pow2d(int e) {
   return __longlong_as_double((long long)(1023 + e) << 52);
 }
 
+template <int NTHR>
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(NTHR) : "memory"); }
 
 // TMEM hand-back groups: the epilogue drains the level accumulators in groups,
 // levels {0, 1} first, then each further level on its own, and hands every
@@ -802,26 +798,17 @@ __host__ __device__ constexpr int level_group(int l) { return l <= 1 ? 0 : l - 1
 // adesc / bdesc describe sub-tile (slice 0, re) of the stage; the other
 // sub-tiles are constant byte offsets (added as offset >> 4 to the
 // start-address field, which cannot carry: shared addresses are < 2^18).
-template <class C, bool PAIR, int I, int J>
+template <class C, int I, int J>
 __device__ __forceinline__ void issue_pair(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
   constexpr uint32_t id_pos = idesc_bf16_f32(SPLIT_M, C::BN, false);
   constexpr uint32_t id_neg = idesc_bf16_f32(SPLIT_M, C::BN, true);
-  constexpr uint32_t id_wide = idesc_bf16_f32(PAIR ? 2 * SPLIT_M : SPLIT_M, 2 * C::BN, false);
+  constexpr uint32_t id_wide = idesc_bf16_f32(SPLIT_M, 2 * C::BN, false);
   constexpr int lvl = (I + J) < C::NL - 1 ? (I + J) : C::NL - 1;
   // in i-major order the first pair of level l is (0, l)
   const uint32_t accum = (!first_chunk || !(I == 0 && J <= C::NL - 1)) ? 1u : 0u;
   const uint64_t ar = adesc + (uint64_t)(((I * 2 + 0) * C::A_SUB) >> 4);
   const uint64_t ai = adesc + (uint64_t)(((I * 2 + 1) * C::A_SUB) >> 4);
-  if constexpr (PAIR) {
-    // each CTA holds two planes of slice j: the first half of the MMA's N
-    // (even CTA: -Yi, Yr) or the second (odd CTA: Yr, Yi), at the same offsets
-    static_assert(C::PACK, "CTA-pair tiles use packed complex MMAs");
-    const uint64_t b_nr = bdesc + (uint64_t)(((J * 2 + 0) * C::B_SUB) >> 4);  // [-Yi | Yr]
-    const uint64_t b_ri = bdesc + (uint64_t)(((J * 2 + 1) * C::B_SUB) >> 4);  // [Yr | Yi]
-    const uint32_t d = tbase + (uint32_t)C::acc_col(0, lvl);
-    umma_f16_pair(d, ar, b_ri, id_wide, accum);  // [Re | Im] += Xr [Yr | Yi]
-    umma_f16_pair(d, ai, b_nr, id_wide, 1u);     // [Re | Im] += Xi [-Yi | Yr]
-  } else if constexpr (C::PACK) {
+  if constexpr (C::PACK) {
     // planes -Yi, Yr, Yi of slice j are adjacent along N (row groups 256 B apart)
     const uint64_t b_nr = bdesc + (uint64_t)(((J * 3 + 0) * C::B_SUB) >> 4);  // [-Yi | Yr]
     const uint64_t b_ri = bdesc + (uint64_t)(((J * 3 + 1) * C::B_SUB) >> 4);  // [Yr | Yi]
@@ -844,38 +831,38 @@ __device__ __forceinline__ void issue_pair(uint32_t tbase, uint64_t adesc, uint6
 // (G < 0: all pairs), in i-major order.  Every level accumulator sees its
 // pairs in the same order whatever the grouping, so the FP32 last level sums
 // them in the same order and the results do not depend on it.
-template <class C, bool PAIR, int G, int I = 0, int J = 0>
+template <class C, int G, int I = 0, int J = 0>
 __device__ __forceinline__ void issue_pairs(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
   if constexpr (I < C::NS) {
     if constexpr (I + J < C::NS) {
       constexpr int lvl = (I + J) < C::NL - 1 ? (I + J) : C::NL - 1;
-      if constexpr (G < 0 || level_group(lvl) == G) issue_pair<C, PAIR, I, J>(tbase, adesc, bdesc, first_chunk);
-      issue_pairs<C, PAIR, G, I, J + 1>(tbase, adesc, bdesc, first_chunk);
+      if constexpr (G < 0 || level_group(lvl) == G) issue_pair<C, I, J>(tbase, adesc, bdesc, first_chunk);
+      issue_pairs<C, G, I, J + 1>(tbase, adesc, bdesc, first_chunk);
     } else {
-      issue_pairs<C, PAIR, G, I + 1, 0>(tbase, adesc, bdesc, first_chunk);
+      issue_pairs<C, G, I + 1, 0>(tbase, adesc, bdesc, first_chunk);
     }
   }
 }
 
 // All MMAs of one K chunk: NS(NS+1)/2 slice pairs (i + j < NS) into the NL
 // level accumulators.
-template <class C, bool PAIR>
+template <class C>
 __device__ __forceinline__ void issue_chunk(uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
-  issue_pairs<C, PAIR, -1>(tbase, adesc, bdesc, first_chunk);
+  issue_pairs<C, -1>(tbase, adesc, bdesc, first_chunk);
 }
 
 // The MMAs of hand-back group g (runtime index) of one K chunk.
-template <class C, bool PAIR>
+template <class C>
 __device__ __forceinline__ void issue_group(int g, uint32_t tbase, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
   static_assert(tmem_groups<C>() >= 2 && tmem_groups<C>() <= 4, "hand-back groups");
   if (g == 0)
-    issue_pairs<C, PAIR, 0>(tbase, adesc, bdesc, first_chunk);
+    issue_pairs<C, 0>(tbase, adesc, bdesc, first_chunk);
   else if (g == 1)
-    issue_pairs<C, PAIR, 1>(tbase, adesc, bdesc, first_chunk);
+    issue_pairs<C, 1>(tbase, adesc, bdesc, first_chunk);
   else if (g == 2)
-    issue_pairs<C, PAIR, 2>(tbase, adesc, bdesc, first_chunk);
+    issue_pairs<C, 2>(tbase, adesc, bdesc, first_chunk);
   else if constexpr (tmem_groups<C>() > 3)
-    issue_pairs<C, PAIR, 3>(tbase, adesc, bdesc, first_chunk);
+    issue_pairs<C, 3>(tbase, adesc, bdesc, first_chunk);
 }
 
 // NC consecutive TMEM columns of this warp's 32 lanes into v (NC = 16, 12, 8 or 4).
@@ -896,72 +883,56 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float* v) {
 // Output tile -> (instance, M tile, N tile).  order 0 walks the N tiles of one
 // M tile first (consecutive CTAs share the left operand tile), order 1 the M
 // tiles of one N tile first (they share the right operand tile).
-// (mtiles counts M units: M tiles, or M tile pairs of the CTA-pair form.)
-__device__ __forceinline__ void tile_coords(const SplitGemmBatch& g, int tile, int mtiles, int& inst, int& mt,
-                                            int& nt) {
-  const int per_inst = mtiles * g.ntiles;
+__device__ __forceinline__ void tile_coords(const SplitGemmBatch& g, int tile, int& inst, int& mt, int& nt) {
+  const int per_inst = g.mtiles * g.ntiles;
   inst = tile / per_inst;
   const int r = tile - inst * per_inst;
-  if ((g.order & 1) == 0) {
+  if (g.order == 0) {
     mt = r / g.ntiles;
     nt = r - mt * g.ntiles;
   } else {
-    nt = r / mtiles;
-    mt = r - nt * mtiles;
+    nt = r / g.mtiles;
+    mt = r - nt * g.mtiles;
   }
 }
 
-template <class C, bool PAIR>
+template <class C>
 __global__ void __launch_bounds__(gemm_threads<C>(), 1)
     split_gemm_kernel(SplitGemmBatch g, int ntiles_total, int* __restrict__ err) {
-  // PAIR: clusters of two CTAs, each pair walking units of 2 M tiles x 1 N
-  // tile with M = 256 MMAs issued by the even CTA (cta_group::2); ntiles_total
-  // then counts those units.  Otherwise one CTA per unit of 1 M tile x 1 N tile.
-  constexpr int BSTG = gemm_b_stage<C, PAIR>();
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA = smem;
   uint8_t* sB = smem + NSTAGE * C::A_STAGE;
-  uint64_t* full = (uint64_t*)(smem + NSTAGE * (C::A_STAGE + BSTG));
+  uint64_t* full = (uint64_t*)(smem + NSTAGE * (C::A_STAGE + C::B_STAGE));
   uint64_t* empty = full + NSTAGE;
   uint64_t* tfull = empty + NSTAGE;
   uint64_t* tempty = tfull + 1;  // one per hand-back group
   uint64_t* drainb = tempty + tmem_groups<C>();
   uint32_t* tslot = (uint32_t*)(drainb + 1);
-  static_assert(8 * (2 * NSTAGE + 2 + tmem_groups<C>()) + 16 <= GEMM_SMEM_TAIL, "GEMM shared-memory tail");
+  int* sexp = (int*)(tslot + 4);  // C::BN column exponents of the current tile
+  // complex128 output: destination of row 0 of each column of the current tile
+  double2** colp = (double2**)(smem + NSTAGE * (C::A_STAGE + C::B_STAGE) + 512);
+  static_assert(512 + 8 * C::BN <= GEMM_SMEM_TAIL && 16 * 8 + 16 + 4 * C::BN <= 512, "GEMM shared-memory tail");
 
   volatile int* status = (volatile int*)(tslot + 1);  // block-uniform decisions
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
-  const int unit0 = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
-  const int unit_step = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
-  const int mpairs = (g.mtiles + 1) >> 1;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; s++) {
-      // the even CTA's full barrier also takes the odd CTA's relayed arrival
-      mbar_init(&full[s], PAIR && rank == 0 ? 2 : 1);
+      mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    // one arrival per epilogue warp (of both CTAs of a pair)
-    for (int g = 0; g < tmem_groups<C>(); g++) mbar_init(&tempty[g], (PAIR ? 2 : 1) * C::EPI_WARPS);
+    for (int g = 0; g < tmem_groups<C>(); g++) mbar_init(&tempty[g], C::EPI_WARPS);  // one arrival per epilogue warp
     mbar_init(drainb, 1);
     fence_mbar_init();
     // A CTA that starts after another one recorded a failure does nothing.
-    // (CTA pairs always run: the TMEM allocation below is collective.)
-    status[0] = PAIR ? 0 : *(volatile int*)err;
+    status[0] = *(volatile int*)err;
   }
   __syncthreads();
   if (status[0]) return;  // uniform: every thread read the same shared value
-  if constexpr (PAIR) cluster_sync();  // both CTAs' barriers initialised before any remote arrival
   if (warp == 0) {
-    if constexpr (PAIR) {
-      tmem_alloc_pair(tslot, TMEM_COLS);
-      tmem_relinquish_pair();
-    } else {
-      tmem_alloc(tslot, TMEM_COLS);
-      tmem_relinquish();
-    }
+    tmem_alloc(tslot, TMEM_COLS);
+    tmem_relinquish();
   }
   tc_fence_before();
   __syncthreads();
@@ -972,15 +943,12 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
     if (lane == 0) {
       uint32_t g_chunk = 0;
       bool ok = true;
-      for (int tile = unit0; tile < ntiles_total && ok; tile += unit_step) {
+      for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x) {
         int inst, mt, nt;
-        tile_coords(g, tile, PAIR ? mpairs : g.mtiles, inst, mt, nt);
-        if constexpr (PAIR) mt = 2 * mt + (int)rank;
+        tile_coords(g, tile, inst, mt, nt);
         const SplitGemmInst* I = &g.inst[inst];
-        const bool avalid = !PAIR || mt < g.mtiles;  // the odd CTA past the last M tile loads no rows
         const uint8_t* gA = I->left + (size_t)mt * g.nchunk * C::A_STAGE;
         const uint8_t* gB = I->right + (size_t)nt * g.nchunk * C::B_STAGE;
-        const uint32_t bytes = (avalid ? C::A_STAGE : 0) + BSTG;
         for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
           const int s = g_chunk % NSTAGE;
           if (g_chunk >= NSTAGE && !mbar_wait(&empty[s], ((g_chunk / NSTAGE) - 1) & 1, WAIT_NS, err)) {
@@ -988,27 +956,19 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             ok = false;
             break;
           }
-          mbar_arrive_expect_tx(&full[s], bytes);
-          if (avalid) bulk_g2s(sA + s * C::A_STAGE, gA + (size_t)kc * C::A_STAGE, C::A_STAGE, &full[s]);
-          if constexpr (PAIR) {
-            // slice j's planes (-Yi, Yr) (even CTA) or (Yr, Yi) (odd CTA)
-            const uint8_t* src = gB + (size_t)kc * C::B_STAGE + rank * C::B_SUB;
-#pragma unroll
-            for (int j = 0; j < C::NS; j++)
-              bulk_g2s(sB + s * BSTG + j * 2 * C::B_SUB, src + j * 3 * C::B_SUB, 2 * C::B_SUB, &full[s]);
-          } else {
-            bulk_g2s(sB + s * BSTG, gB + (size_t)kc * C::B_STAGE, C::B_STAGE, &full[s]);
-          }
+          mbar_arrive_expect_tx(&full[s], C::A_STAGE + C::B_STAGE);
+          bulk_g2s(sA + s * C::A_STAGE, gA + (size_t)kc * C::A_STAGE, C::A_STAGE, &full[s]);
+          bulk_g2s(sB + s * C::B_STAGE, gB + (size_t)kc * C::B_STAGE, C::B_STAGE, &full[s]);
         }
       }
     }
   } else if (warp == 1) {
-    if (lane == 0 && PAIR && rank != 0) {
-      // odd CTA of a pair: relay each stage's arrival to the even CTA, whose
-      // MMAs read this CTA's shared memory as well
-      uint32_t g_chunk = 0;
+    if (lane == 0) {
+      uint32_t g_chunk = 0, local = 0;
       bool ok = true;
-      for (int tile = unit0; tile < ntiles_total && ok; tile += unit_step) {
+      const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
+      const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
+      for (int tile = blockIdx.x; tile < ntiles_total && ok; tile += gridDim.x, local++) {
         for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
           const int s = g_chunk % NSTAGE;
           if (!mbar_wait(&full[s], (g_chunk / NSTAGE) & 1, WAIT_NS, err)) {
@@ -1016,56 +976,30 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             ok = false;
             break;
           }
-          mbar_arrive_cluster(mapa_shared(smem_u32(&full[s]), 0));
-        }
-      }
-      if (!mbar_wait(drainb, 0, 2 * WAIT_NS)) atomicExch(err, 5);
-    } else if (lane == 0) {
-      uint32_t g_chunk = 0, local = 0;
-      bool ok = true;
-      const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
-      const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
-      auto wait_x = [&](uint64_t* bar, uint32_t parity, uint64_t ns) {
-        return PAIR ? mbar_wait_cluster(bar, parity, ns, err) : mbar_wait(bar, parity, ns, err);
-      };
-      auto commit = [&](uint64_t* bar) {
-        if constexpr (PAIR)
-          umma_commit_pair(bar);
-        else
-          umma_commit(bar);
-      };
-      for (int tile = unit0; tile < ntiles_total && ok; tile += unit_step, local++) {
-        for (int kc = 0; kc < g.nchunk; kc++, g_chunk++) {
-          const int s = g_chunk % NSTAGE;
-          if (!wait_x(&full[s], (g_chunk / NSTAGE) & 1, WAIT_NS)) {
-            atomicExch(err, 2);
-            ok = false;
-            break;
-          }
           tc_fence_after();
           const uint64_t ad = adesc0 + (uint64_t)((s * C::A_STAGE) >> 4);
-          const uint64_t bd = bdesc0 + (uint64_t)((s * BSTG) >> 4);
+          const uint64_t bd = bdesc0 + (uint64_t)((s * C::B_STAGE) >> 4);
           if (kc == 0) {
             // first chunk: each group of levels once the epilogue handed it back
             for (int grp = 0; grp < tmem_groups<C>() && ok; grp++) {
-              if (local > 0 && !wait_x(&tempty[grp], (local - 1) & 1, 2 * WAIT_NS)) {
+              if (local > 0 && !mbar_wait(&tempty[grp], (local - 1) & 1, 2 * WAIT_NS, err)) {
                 atomicExch(err, 4);
                 ok = false;
                 break;
               }
               tc_fence_after();
-              issue_group<C, PAIR>(grp, tbase, ad, bd, true);
+              issue_group<C>(grp, tbase, ad, bd, true);
             }
             if (!ok) break;
           } else {
-            issue_chunk<C, PAIR>(tbase, ad, bd, false);
+            issue_chunk<C>(tbase, ad, bd, false);
           }
-          commit(&empty[s]);  // stage s free (in both CTAs of a pair) once these MMAs have read it
+          umma_commit(&empty[s]);  // stage s free once these MMAs have read it
         }
-        if (ok) commit(tfull);
+        if (ok) umma_commit(tfull);
       }
       // wait for every issued MMA before the accumulators are released
-      commit(drainb);
+      umma_commit(drainb);
       if (!mbar_wait(drainb, 0, WAIT_NS)) atomicExch(err, 5);
     }
   } else {
@@ -1073,54 +1007,46 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
     // warps of a quadrant split the tile's columns between them
     constexpr int EPH = C::EPI_WARPS / 4, CPW = C::BN / EPH;
     const int q = warp & 3, half = (warp - 2) / 4;
+    const int et = threadIdx.x - 64;  // 0 .. 32 * EPI_WARPS - 1 within the epilogue group
     const int row = q * 32 + lane;
     const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
     uint32_t local = 0;
-    for (int tile = unit0; tile < ntiles_total; tile += unit_step, local++) {
+    for (int tile = blockIdx.x; tile < ntiles_total; tile += gridDim.x, local++) {
       int inst, mt, nt;
-      tile_coords(g, tile, PAIR ? mpairs : g.mtiles, inst, mt, nt);
-      if constexpr (PAIR) mt = 2 * mt + (int)rank;
+      tile_coords(g, tile, inst, mt, nt);
       const SplitGemmInst* I = &g.inst[inst];
-      // Lane c < CPW of each warp holds the exponent (and, for complex128
-      // output, the destination) of the warp's column cbase + c.
-      const int cbase = half * CPW;
-      int my_cexp = 0;
-      double2* my_colp = nullptr;
-      if (lane < CPW) {
-        const int gcol = nt * C::BN + cbase + lane;
-        my_cexp = I->rexp[gcol];
-        if constexpr (C::INT_OUT)
-          if (gcol < g.ncols) my_colp = I->outs[gcol / g.blkn] + (gcol % g.blkn);
+      // stage this tile's column exponents; the barrier also keeps the previous
+      // tile's values until every epilogue thread has used them
+      epi_bar<32 * C::EPI_WARPS>();
+      if (et < C::BN) {
+        sexp[et] = I->rexp[nt * C::BN + et];
+        if constexpr (C::INT_OUT) {
+          const int gcol = nt * C::BN + et;
+          colp[et] = gcol < g.ncols ? I->outs[gcol / g.blkn] + (gcol % g.blkn) : nullptr;
+        }
       }
       const int grow = mt * SPLIT_M + row;
-      // (the odd CTA of a pair past the last M tile computes padding rows only)
-      const bool rvalid = mt < g.mtiles && grow < g.mrows;
-      const int erow = mt < g.mtiles ? I->lexp[grow] : 0;
-      // One thread waits for the accumulators (the other epilogue warps sleep
-      // in the barrier rather than poll); the outcome goes through shared
-      // memory, double-buffered by tile, so that all epilogue warps leave the
-      // loop together.
-      if (threadIdx.x == 64) {
+      const bool rvalid = grow < g.mrows;
+      const int erow = I->lexp[grow];
+      // one thread waits for the accumulators; the outcome is shared so that
+      // all epilogue threads leave the loop together
+      if (et == 0) {
         const bool done = mbar_wait(tfull, local & 1, 4 * WAIT_NS, err);
         if (!done) atomicExch(err, 3);
-        status[1 + (local & 1)] = done ? 0 : 1;
+        status[1] = done ? 0 : 1;
       }
-      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI_WARPS) : "memory");
-      if (status[1 + (local & 1)]) break;
+      epi_bar<32 * C::EPI_WARPS>();
+      if (status[1]) break;
       tc_fence_after();
       // Each warp drains its CPW columns into registers and hands TMEM back to
       // the MMA warp before it writes anything to global memory, so the next
       // tile's MMAs run while this tile's products are stored.
+      const int cbase = half * CPW;
       // hand TMEM group grp back to the MMA warp (after this warp's loads of it)
       auto hand_back = [&](int grp) {
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) {
-          if (PAIR && rank != 0)
-            mbar_arrive_cluster(mapa_shared(smem_u32(&tempty[grp]), 0));  // the even CTA issues the MMAs
-          else
-            mbar_arrive(&tempty[grp]);
-        }
+        if (lane == 0) mbar_arrive(&tempty[grp]);
       };
       if constexpr (C::INT_OUT) {
         // complex128 output: the exact levels and the last one summed exactly
@@ -1137,21 +1063,19 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
           // the last level holds pairs i+j >= NL-1: |v| 2^54 <= 5 K 2^16 2^-52 2^54 < 2^30
           return (long long)__float2int_rn(v * __int_as_float((127 + 54) << 23));
         };
+        // (each group goes back as soon as its last load has landed, before
+        // that load's values are folded in: the MMA warp waits on the loads only)
         long long acc[2][CPW];
-        {  // group 0: levels 0 and 1, both parts, one wait
-          float v0[2][CPW], v1[2][CPW];
 #pragma unroll
-          for (int part = 0; part < 2; part++) {
-            tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 0) + cbase), v0[part]);
-            tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 1) + cbase), v1[part]);
-          }
+        for (int part = 0; part < 2; part++) {  // group 0: levels 0 and 1
+          float v0[CPW], v1[CPW];
+          tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 0) + cbase), v0);
+          tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 1) + cbase), v1);
           tmem_ld_wait();
+          if (part == 1) hand_back(0);
 #pragma unroll
-          for (int part = 0; part < 2; part++)
-#pragma unroll
-            for (int c = 0; c < CPW; c++) acc[part][c] = level_units(v0[part][c], 0) + level_units(v1[part][c], 1);
+          for (int c = 0; c < CPW; c++) acc[part][c] = level_units(v0[c], 0) + level_units(v1[c], 1);
         }
-        hand_back(0);
 #pragma unroll
         for (int l = 2; l < C::NL; l++) {  // group l - 1: level l
 #pragma unroll
@@ -1159,17 +1083,20 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             float v[CPW];
             tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, l) + cbase), v);
             tmem_ld_wait();
+            if (part == 1) hand_back(l - 1);
 #pragma unroll
             for (int c = 0; c < CPW; c++) acc[part][c] += level_units(v[c], l);
           }
-          hand_back(l - 1);
         }
+        if (rvalid) {
+          const int erow = I->lexp[grow];
 #pragma unroll
-        for (int c = 0; c < CPW; c++) {
-          double2* dst = (double2*)__shfl_sync(0xffffffffu, (unsigned long long)my_colp, c);
-          const int e = erow + __shfl_sync(0xffffffffu, my_cexp, c) - 54;
-          if (rvalid && dst)
+          for (int c = 0; c < CPW; c++) {
+            double2* dst = colp[cbase + c];
+            if (!dst) continue;
+            const int e = erow + sexp[cbase + c] - 54;
             dst[(size_t)grow * g.blkn] = make_double2(i2d_scaled(acc[0][c], e), i2d_scaled(acc[1][c], e));
+          }
         }
       } else {
         // float-float output: levels 0 .. NL-2 exact, combined by exact two-sums;
@@ -1196,16 +1123,15 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             }
           }
         }
+        // (each group goes back as soon as its last load has landed, before
+        // that load's values are folded in: the MMA warp waits on the loads only)
         float s[2][CPW], e[2][CPW];
-        // group 0: levels 0 and 1, both parts, one wait
 #pragma unroll
-        for (int part = 0; part < 2; part++) {
+        for (int part = 0; part < 2; part++) {  // group 0: levels 0 and 1
           tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 0) + cbase), s[part]);
           tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, 1) + cbase), e[part]);
-        }
-        tmem_ld_wait();
-#pragma unroll
-        for (int part = 0; part < 2; part++)
+          tmem_ld_wait();
+          if (part == 1) hand_back(0);
 #pragma unroll
           for (int c = 0; c < CPW; c++) {
             float t, d;
@@ -1213,7 +1139,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             s[part][c] = t;
             e[part][c] = 0.f + d;
           }
-        hand_back(0);
+        }
 #pragma unroll
         for (int l = 2; l < C::NL; l++) {  // group l - 1: level l
 #pragma unroll
@@ -1221,6 +1147,7 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
             float v[CPW];
             tmem_ld_cols<CPW>(tl + (uint32_t)(C::acc_col(part, l) + cbase), v);
             tmem_ld_wait();
+            if (part == 1) hand_back(l - 1);
 #pragma unroll
             for (int c = 0; c < CPW; c++) {
               if (l < C::NL - 1) {
@@ -1236,19 +1163,18 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
               }
             }
           }
-          hand_back(l - 1);
         }
-        if (!g.levels) {
+        if (rvalid && !g.levels) {
           float4* outp = I->out;
 #pragma unroll
           for (int c = 0; c < CPW; c++) {
             const int gcol = nt * C::BN + cbase + c;
-            const int ex = erow + __shfl_sync(0xffffffffu, my_cexp, c);
-            if (!rvalid || gcol >= g.ncols) continue;
+            if (gcol >= g.ncols) continue;
             // the float-float products and their traces stay accurate while the
             // scale stays well inside FP32's normal range; below 2^-100 the
             // product is written as NaN, which flags the entries that use it for
             // recomputation in FP64 range
+            const int ex = erow + sexp[cbase + c];
             const float sc = ex < FF_MIN_EXP ? __int_as_float(0x7fc00000) : pow2f(ex);
             outp[(size_t)gcol * ldo + grow] =
                 make_float4(s[0][c] * sc, e[0][c] * sc, s[1][c] * sc, e[1][c] * sc);
@@ -1259,13 +1185,9 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
   }
   tc_fence_before();
   __syncthreads();
-  if constexpr (PAIR) cluster_sync();  // neither CTA leaves while the other may still address it
   if (warp == 0) {
     tc_fence_after();
-    if constexpr (PAIR)
-      tmem_dealloc_pair(tbase, TMEM_COLS);
-    else
-      tmem_dealloc(tbase, TMEM_COLS);
+    tmem_dealloc(tbase, TMEM_COLS);
   }
 }
 
@@ -1700,19 +1622,12 @@ static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr =
             g_attr_hp = false, g_attr_stl = false;
 static int g_nsm = 0;
 
-static bool g_attr_std2 = false, g_attr_hp2 = false;
-static int g_pair_clusters[2] = {0, 0};  // co-resident CTA pairs (CfgStd, CfgHP)
-
-template <class C, bool PAIR>
+template <class C>
 static bool& gemm_attr_flag();
 template <>
-bool& gemm_attr_flag<CfgStd, false>() { return g_attr_std; }
+bool& gemm_attr_flag<CfgStd>() { return g_attr_std; }
 template <>
-bool& gemm_attr_flag<CfgHP, false>() { return g_attr_hp; }
-template <>
-bool& gemm_attr_flag<CfgStd, true>() { return g_attr_std2; }
-template <>
-bool& gemm_attr_flag<CfgHP, true>() { return g_attr_hp2; }
+bool& gemm_attr_flag<CfgHP>() { return g_attr_hp; }
 
 static int sm_count(int* out) {
   if (!g_nsm) {
@@ -1737,10 +1652,8 @@ int split_kernels_prepare() {
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
   CTR_TRY(ensure_smem(slice_stack_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_stl));
-  CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd, false>, gemm_smem_bytes<CfgStd>(), g_attr_std));
-  CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP, false>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
-  CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd, true>, gemm_smem_bytes<CfgStd, true>(), g_attr_std2));
-  CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP, true>, gemm_smem_bytes<CfgHP, true>(), g_attr_hp2));
+  CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
+  CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
   return CTR_OK;
 }
 
@@ -1850,14 +1763,14 @@ int launch_block_exp(const double2* const* d_blk, int nblk, int nev, int* bexp, 
 template <class C>
 static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, const char* name) {
   const size_t smem = gemm_smem_bytes<C>();
-  CTR_TRY(ensure_smem(split_gemm_kernel<C, false>, smem, gemm_attr_flag<C, false>()));
+  CTR_TRY(ensure_smem(split_gemm_kernel<C>, smem, gemm_attr_flag<C>()));
   int nsm;
   CTR_TRY(sm_count(&nsm));
   const long long total = (long long)ninst * g.mtiles * g.ntiles;
   if (total > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
   const int grid = (int)std::min<long long>(total, nsm);
   TimedLaunch tl(s, name);
-  split_gemm_kernel<C, false><<<grid, gemm_threads<C>(), smem, s>>>(g, (int)total, d_err);
+  split_gemm_kernel<C><<<grid, gemm_threads<C>(), smem, s>>>(g, (int)total, d_err);
   CTR_CUDA(cudaGetLastError());
   // slice pairs i + j < NS, each two packed MMAs of M x 2BN x 16: 8 M BN 16 flops
   if (!capturing())
@@ -1865,61 +1778,13 @@ static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err,
   return CTR_OK;
 }
 
-// The CTA-pair form: clusters of two CTAs (one TPC), M = 256 MMAs, each CTA
-// loading its own 128 rows of the left operand and half of the right one.
-// The grid holds as many pairs as fit on the device at once (persistent).
-template <class C>
-static int launch_split_gemm_pair(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, const char* name) {
-  constexpr int ci = C::INT_OUT ? 1 : 0;
-  const size_t smem = gemm_smem_bytes<C, true>();
-  CTR_TRY(ensure_smem(split_gemm_kernel<C, true>, smem, gemm_attr_flag<C, true>()));
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.blockDim = dim3(gemm_threads<C>());
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  if (!g_pair_clusters[ci]) {
-    int nsm;
-    CTR_TRY(sm_count(&nsm));
-    cfg.gridDim = dim3(2 * (nsm / 2));
-    int nc = 0;
-    CTR_CUDA(cudaOccupancyMaxActiveClusters(&nc, (void*)split_gemm_kernel<C, true>, &cfg));
-    if (nc < 1) return fail(CTR_ERR_UNSUPPORTED, "split GEMM: no CTA pair fits on this device");
-    g_pair_clusters[ci] = nc;
-  }
-  const long long mpairs = (g.mtiles + 1) / 2;
-  const long long units = (long long)ninst * mpairs * g.ntiles;
-  if (units > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
-  cfg.gridDim = dim3((unsigned)(2 * std::min<long long>(units, g_pair_clusters[ci])));
-  TimedLaunch tl(s, name);
-  CTR_CUDA(cudaLaunchKernelEx(&cfg, split_gemm_kernel<C, true>, g, (int)units, d_err));
-  // useful tiles only: the odd CTA past an odd M tile count computes padding
-  if (!capturing())
-    g_split_mma_flops +=
-        (double)ninst * g.mtiles * g.ntiles * (C::NS * (C::NS + 1) / 2) * 8.0 * SPLIT_M * C::BN * SPLIT_K * g.nchunk;
-  return CTR_OK;
-}
-
-int launch_split_gemm(const SplitGemmBatch& g0, int ninst, int* d_err, cudaStream_t s) {
+int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
   if (ninst == 0) return CTR_OK;
-  // "split_gemm.form" pinned to 0 / 1 selects the single-CTA / CTA-pair form
-  // for every launch (order bit 1 otherwise, from the callers' tile schedule)
-  SplitGemmBatch g = g0;
-  const int form = tune_forced("split_gemm.form");
-  if (form == 0 || form == 1) g.order = (g.order & 1) | (form << 1);
   if (g.hp) {
     if (g.out_mode != 1 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: the high-precision tiles write complex128");
-    if (g.order & 2) return launch_split_gemm_pair<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");
     return launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");
   }
   if (g.out_mode != 0) return fail(CTR_ERR_ARG, "split GEMM: the standard tiles write float-float");
-  if (g.order & 2) return launch_split_gemm_pair<CfgStd>(g, ninst, d_err, s, "split_gemm");
   return launch_split_gemm_cfg<CfgStd>(g, ninst, d_err, s, "split_gemm");
 }
 
