@@ -47,6 +47,22 @@ __device__ __forceinline__ int f64_exp_bound(double x) {
   return be == 0 ? -30000 : be - 1022;
 }
 
+// f64_fixed of x * (+-2^k) without the FP64 product: a power-of-two factor
+// only moves the exponent (and flips the sign when `flip`).  A product that
+// would leave the normal range (|x 2^k| < 2^-1022) gives 0, as the subnormal
+// FP64 product does in f64_fixed; the sign is the product's in every case.
+__device__ __forceinline__ uint64_t f64_fixed_pow2(double x, int k, bool flip, int E, bool& neg) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  neg = ((b >> 63) != 0) != flip;
+  const int be = (int)((b >> 52) & 0x7FF);
+  if (be == 0 || be + k <= 0) return 0;
+  const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  const int sh = be + k - 1012 - E;
+  if (sh >= 0) return m << sh;
+  if (sh <= -64) return 0;
+  return m >> (-sh);
+}
+
 // 63-bit fixed-point magnitude of x / 2^E (|x| < 2^E) and its sign.
 __device__ __forceinline__ uint64_t f64_fixed(double x, int E, bool& neg) {
   const uint64_t b = (uint64_t)__double_as_longlong(x);
@@ -445,32 +461,30 @@ __global__ void __launch_bounds__(256) slice_right_staged_kernel(const SliceRigh
 }
 
 // ------------------------------------------------------ task-form slicers
-__device__ __forceinline__ double2 task_left_elem(const SliceTaskLJob& J, int nev, int r, int k) {
+// Element (r, k) of a left task operand before its term's weight and
+// conjugation, which the slicers apply as exponent and sign (the weights are
+// real powers of two).
+__device__ __forceinline__ double2 task_left_raw(const SliceTaskLJob& J, int nev, int r, int k) {
   const int q = k / nev, j = k - q * nev;
   if (r >= nev || q >= J.nterm) return make_double2(0.0, 0.0);
-  double2 v;
-  if ((J.dag >> q) & 1) {
-    v = J.a[q][(size_t)j * nev + r];
-    v.y = -v.y;
-  } else {
-    v = J.a[q][(size_t)r * nev + j];
-  }
-  const double w = (double)J.w[q];
-  return make_double2(v.x * w, v.y * w);
+  return ((J.dag >> q) & 1) ? J.a[q][(size_t)j * nev + r] : J.a[q][(size_t)r * nev + j];
 }
 
-__device__ __forceinline__ double2 task_right_elem(const SliceTaskRJob& J, int nev, int k, int n) {
+// Fixed-point magnitudes and signs of w_q op(x) for term q, with w_q = +-2^wexp_q
+// and op the identity or the complex conjugate (dag): integer operations only.
+__device__ __forceinline__ void weighted_fixed(double2 x, int wexp, bool wneg, bool dag, int E, uint64_t& Ur,
+                                               bool& nr, uint64_t& Ui, bool& ni) {
+  Ur = f64_fixed_pow2(x.x, wexp, wneg, E, nr);
+  Ui = f64_fixed_pow2(x.y, wexp, wneg != dag, E, ni);
+}
+
+// Element (k, n) of a right task operand before its conjugation (applied as a
+// sign by the slicer).
+__device__ __forceinline__ double2 task_right_raw(const SliceTaskRJob& J, int nev, int k, int n) {
   const int q = k / nev, i = k - q * nev, jb = n / nev, c = n - jb * nev;
   if (q >= J.nterm || jb >= J.nb) return make_double2(0.0, 0.0);
   const double2* B = J.b[jb][q];
-  double2 v;
-  if ((J.dag >> (4 * jb + q)) & 1) {
-    v = B[(size_t)c * nev + i];
-    v.y = -v.y;
-  } else {
-    v = B[(size_t)i * nev + c];
-  }
-  return v;
+  return ((J.dag >> (4 * jb + q)) & 1) ? B[(size_t)c * nev + i] : B[(size_t)i * nev + c];
 }
 
 // Every (block, term) of a right job conjugate-transposed.
@@ -563,16 +577,20 @@ __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJo
   for (int u = 0; u < PER; u++) {
     const int e = threadIdx.x + u * 256;
     const int rr = e >> 4, k = kc * SPLIT_K + (e & 15);
-    v[u] = k < K ? task_left_elem(J, nev, rr, k) : make_double2(0.0, 0.0);
+    v[u] = k < K ? task_left_raw(J, nev, rr, k) : make_double2(0.0, 0.0);
   }
   __syncthreads();
 #pragma unroll
   for (int u = 0; u < PER; u++) {
     const int e = threadIdx.x + u * 256;
     const int rr = e >> 4, kk = e & 15;
+    const int q = min((kc * SPLIT_K + kk) / nev, J.nterm - 1);
     const int E = sexp[rr];
     bool nr, ni;
-    const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v[u].x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v[u].y, E, ni));
+    uint64_t Ur, Ui;
+    weighted_fixed(v[u], J.wexp[q], J.w[q] < 0.f, (J.dag >> q) & 1, E, Ur, nr, Ui, ni);
+    Ur = round_fixed<C::NS>(Ur);
+    Ui = round_fixed<C::NS>(Ui);
     const uint32_t off = core_offset(rr, kk);
 #pragma unroll
     for (int s = 0; s < C::NS; s++) {
@@ -622,15 +640,7 @@ __global__ void __launch_bounds__(256) slice_stack_left_kernel(const SliceStackL
     v[u] = make_double2(0.0, 0.0);
     if (k < K && g < rows) {
       const int sl = g / nev, r = g - sl * nev, q = k / nev, j = k - q * nev;
-      double2 x;
-      if ((J.dag >> q) & 1) {
-        x = J.a[sl][q][(size_t)j * nev + r];
-        x.y = -x.y;
-      } else {
-        x = J.a[sl][q][(size_t)r * nev + j];
-      }
-      const double w = (double)J.w[q];
-      v[u] = make_double2(x.x * w, x.y * w);
+      v[u] = ((J.dag >> q) & 1) ? J.a[sl][q][(size_t)j * nev + r] : J.a[sl][q][(size_t)r * nev + j];
     }
   }
   __syncthreads();
@@ -638,9 +648,13 @@ __global__ void __launch_bounds__(256) slice_stack_left_kernel(const SliceStackL
   for (int u = 0; u < PER; u++) {
     const int e = threadIdx.x + u * 256;
     const int rr = e >> 4, kk = e & 15;
+    const int q = min((kc * SPLIT_K + kk) / nev, J.nterm - 1);
     const int E = sexp[rr];
     bool nr, ni;
-    const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v[u].x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v[u].y, E, ni));
+    uint64_t Ur, Ui;
+    weighted_fixed(v[u], J.wexp[q], J.w[q] < 0.f, (J.dag >> q) & 1, E, Ur, nr, Ui, ni);
+    Ur = round_fixed<C::NS>(Ur);
+    Ui = round_fixed<C::NS>(Ui);
     const uint32_t off = core_offset(rr, kk);
 #pragma unroll
     for (int s = 0; s < C::NS; s++) {
@@ -691,7 +705,7 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
     const int e = threadIdx.x + u * 256;
     const int nn = tr ? (e >> 4) : (e % C::BN), kk = tr ? (e & 15) : (e / C::BN);
     const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
-    v[u] = (e < C::BN * SPLIT_K && n < ncols && k < K) ? task_right_elem(J, nev, k, n) : make_double2(0.0, 0.0);
+    v[u] = (e < C::BN * SPLIT_K && n < ncols && k < K) ? task_right_raw(J, nev, k, n) : make_double2(0.0, 0.0);
   }
   __syncthreads();
 #pragma unroll
@@ -699,9 +713,14 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
     const int e = threadIdx.x + u * 256;
     if (e >= C::BN * SPLIT_K) break;
     const int nn = tr ? (e >> 4) : (e % C::BN), kk = tr ? (e & 15) : (e / C::BN);
+    const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
+    const int jb = min(n / nev, J.nb - 1), q = min(k / nev, J.nterm - 1);
     const int E = sexp[nn];
     bool nr, ni;
-    const uint64_t Ur = round_fixed<C::NS>(f64_fixed(v[u].x, E, nr)), Ui = round_fixed<C::NS>(f64_fixed(v[u].y, E, ni));
+    uint64_t Ur, Ui;
+    weighted_fixed(v[u], 0, false, (J.dag >> (4 * jb + q)) & 1, E, Ur, nr, Ui, ni);
+    Ur = round_fixed<C::NS>(Ur);
+    Ui = round_fixed<C::NS>(Ui);
     const uint32_t off = core_offset(nn, kk);
 #pragma unroll
     for (int s = 0; s < C::NS; s++) {
