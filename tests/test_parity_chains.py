@@ -342,6 +342,33 @@ def test_block_product_tasks_split_vs_fp64(cuda):
         assert err <= tol, (engine, err)
 
 
+def test_block_product_tasks_power_of_two_weights(cuda):
+    """Term weights of both signs and several powers of two, with the left blocks
+    conjugate-transposed, on operands far from 1 (2^-600 and 2^500): the split
+    engine applies the weights and conjugations as exponent offsets and signs
+    while slicing, the FP64 engine multiplies them in."""
+    n = 64
+    rng = np.random.default_rng(9)
+    M1 = (rng.normal(size=(8, n, n)) + 1j * rng.normal(size=(8, n, n))) * 2.0 ** -600
+    M1 *= np.exp(-rng.uniform(0, 10, (8, 1, n)))  # columns of M1 (rows of M1^dagger) over 4 decades
+    M2 = (rng.normal(size=(8, n, n)) + 1j * rng.normal(size=(8, n, n))) * 2.0 ** 500
+    w = [0.5, -2.0, 0.25, -1.0]
+    ref = np.zeros((2, n, n), np.complex128)
+    tasks = []
+    for c in range(2):
+        for k in range(4):
+            ref[c] += w[k] * M1[c * 4 + k].conj().T @ M2[c * 4 + k]
+        tasks.append(([c * 4 + k for k in range(4)], [c * 4 + k for k in range(4)], c))
+    x, y = _dev(M1, cuda), _dev(M2, cuda)
+    # entry error against the scale of its row of op(M1) and the largest |M2|
+    scale = np.abs(M1).max(axis=1).reshape(2, 4, n).max(axis=1)[:, :, None] * np.abs(M2).max() * 4 * n * 2
+    for engine, tol in (("fp64", 1e-14), ("split", 1e-12)):
+        out = api.zgemm_tasks(x, y, tasks, weights=w, a_dagger=True, engine=engine)
+        api.sync()
+        err = (np.abs(out.cpu().numpy() - ref) / scale).max()
+        assert err <= tol, (engine, err)
+
+
 def _refine(tol):
     from contractions_code_scattering_gb300._lib import check, lib
     check(lib().ctr_split_set_refine(tol))
