@@ -55,12 +55,12 @@ def parse():
     ap.add_argument("--pipi-form", default="sets", choices=["sets", "pairs"],
                     help="pi pi workload: one ctr_pipi_sets call for the 19 momentum sets, or one ctr_pipi per pair")
     ap.add_argument("--workload", default="rho", choices=["rho", "rho_small", "pipi", "mixed", "adjoint", "legacy_gpu", "elementals",
-                             "fp64_peak"],
+                             "fp64_peak", "mma_probe"],
                     help="rho: the headline rho two-point (Nev=100, Lt=64); rho_small: Nev=32, Lt=16 FP64; "
                          "pipi: pi pi I=0 diagram set, 19 momentum pairs; mixed: rho-pipi / sigma-pipi / "
                          "sigma loops at Nev=128, Lt=48, 27 momenta; adjoint: profile objective and gradient; "
                          "legacy_gpu: the reference's own rho kernel built for sm_103a beside both engines; "
-                         "fp64_peak: cuBLAS DGEMM/ZGEMM rates")
+                         "fp64_peak: cuBLAS DGEMM/ZGEMM rates; mma_probe: the split GEMMs' MMA schedules alone")
     return ap.parse_args()
 
 
@@ -1214,8 +1214,29 @@ def run_fp64_peak(args):
     print(json.dumps({"workload": "fp64_peak", "n": n, **res}))
 
 
+def run_mma_probe(args):
+    """The split GEMMs' per-chunk MMA schedules by themselves on every SM
+    (include/ctr.h: ctr_mma_schedule_probe): no operand copies, no epilogue,
+    operands that stay in shared memory.  Short runs (0.3 ms) show the issue rate;
+    long ones (~100 ms) run under the power limit like the GEMMs do."""
+    from contractions_code_scattering_gb300 import api
+    api.device_init(0)
+    pk = measured_peaks() or {}
+    peak = pk.get("bf16_tflops")
+    res = {}
+    for name, hp in (("standard", False), ("high_precision", True)):
+        for nchunk in (300, 100000):
+            api.mma_schedule_probe(hp, 50)  # module load, TMEM and shared-memory set-up
+            cpm, tf = api.mma_schedule_probe(hp, nchunk)
+            res["%s_nchunk%d" % (name, nchunk)] = {"clocks_per_mma": cpm, "tflops": tf,
+                                                   "frac_of_measured_bf16": tf / peak if peak else None}
+    print(json.dumps({"workload": "mma_probe", "mma": {"standard": "M128 N128 K16 bf16, 30 a chunk",
+                                                       "high_precision": "M128 N96 K16 bf16, 42 a chunk"},
+                      "nominal_clocks_per_mma": {"standard": 64, "high_precision": 48}, **res}))
+
+
 WORKLOADS = {"fp64_peak": run_fp64_peak, "rho_small": run_rho_small, "pipi": run_pipi, "mixed": run_mixed, "adjoint": run_adjoint,
-             "legacy_gpu": run_legacy_gpu, "elementals": run_elementals}
+             "legacy_gpu": run_legacy_gpu, "elementals": run_elementals, "mma_probe": run_mma_probe}
 
 
 if __name__ == "__main__":

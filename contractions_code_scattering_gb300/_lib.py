@@ -65,6 +65,7 @@ def lib(build_if_missing=True):
     L.ctr_zgemm_tasks.argtypes = [i, i, i, vp, vp]
     L.ctr_elementals.argtypes = [i, i, i, i, i, vp, vp, i, vp, i, vp, vp]
     L.ctr_wait_probe.argtypes = [i, vp]
+    L.ctr_mma_schedule_probe.argtypes = [i, i, ctypes.POINTER(d), ctypes.POINTER(d), vp]
     L.ctr_split_set_refine.argtypes = [d]
     L.ctr_split_refined.restype = ctypes.c_longlong
     L.ctr_split_flops.argtypes = [ctypes.POINTER(d), ctypes.POINTER(d), i]

@@ -336,6 +336,14 @@ def tune_load(path):
     check(lib().ctr_tune_load(str(path).encode()))
 
 
+def mma_schedule_probe(hp=False, nchunk=20000, stream=None):
+    """The split GEMM's per-chunk MMA schedule by itself on every SM (include/ctr.h:
+    ctr_mma_schedule_probe): returns (SM clocks per MMA, device BF16 TFLOP/s)."""
+    cpm, tf = ctypes.c_double(), ctypes.c_double()
+    check(lib().ctr_mma_schedule_probe(1 if hp else 0, int(nchunk), ctypes.byref(cpm), ctypes.byref(tf), _stream(stream)))
+    return cpm.value, tf.value
+
+
 def sync(stream=None):
     """Synchronise the stream and raise if a device-side wait of the split engine timed out."""
     check(lib().ctr_sync(_stream(stream)))

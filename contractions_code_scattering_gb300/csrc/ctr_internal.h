@@ -118,6 +118,8 @@ extern double g_split_mma_flops, g_split_products;
 int split_error_check(cudaStream_t s);
 // Runs a bounded device wait that times out after timeout_ms and reports it (ctr_wait_probe).
 int wait_probe(int timeout_ms, cudaStream_t s);
+// The split GEMM's MMA schedule alone (ctr_mma_schedule_probe).
+int mma_schedule_probe(int hp, int nchunk, double* clocks_per_mma, double* tflops, cudaStream_t s);
 int zgemm_split_batched(int N, int nb, const double* const* x, const double* const* y, double* const* c,
                         cudaStream_t stream);
 // A stage of FP64-engine GEMM tasks (struct ZTask, kernels.h) on the split

@@ -242,6 +242,13 @@ int ctr_source_average(int nt, int ncorr, const double* corr, double scale, doub
   return ctr::launch_source_average(nt, ncorr, (const double2*)corr, scale, (double2*)avg, (cudaStream_t)stream);
 }
 
+int ctr_mma_schedule_probe(int hp, int nchunk, double* clocks_per_mma, double* tflops, void* stream) {
+  CTR_NO_CAPTURE("ctr_mma_schedule_probe");
+  if (nchunk < 1 || nchunk > (1 << 20) || !clocks_per_mma || !tflops)
+    return ctr::fail(CTR_ERR_ARG, "ctr_mma_schedule_probe: nchunk %d not in [1, 2^20] or null outputs", nchunk);
+  return ctr::mma_schedule_probe(hp ? 1 : 0, nchunk, clocks_per_mma, tflops, (cudaStream_t)stream);
+}
+
 int ctr_wait_probe(int timeout_ms, void* stream) {
   CTR_NO_CAPTURE("ctr_wait_probe");
   if (timeout_ms < 1 || timeout_ms > 1000) return ctr::fail(CTR_ERR_ARG, "ctr_wait_probe: timeout %d ms not in [1, 1000]", timeout_ms);

@@ -63,6 +63,40 @@ int wait_probe(int timeout_ms, cudaStream_t s) {
   return split_error_check(s);
 }
 
+int mma_schedule_probe(int hp, int nchunk, double* clocks_per_mma, double* tflops, cudaStream_t s) {
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  void* mem;
+  CTR_TRY(workspace(WS_MISC).get(sizeof(unsigned long long), &mem));
+  unsigned long long* d_cyc = (unsigned long long*)mem;
+  CTR_CUDA(cudaMemsetAsync(d_cyc, 0, sizeof(unsigned long long), s));
+  cudaEvent_t e0, e1;
+  CTR_CUDA(cudaEventCreate(&e0));
+  CTR_CUDA(cudaEventCreate(&e1));
+  int nsm = 0, per_chunk = 0, n = 0;
+  CTR_CUDA(cudaEventRecord(e0, s));
+  int rc = launch_mma_schedule_probe(hp, nchunk, d_cyc, d_err, &nsm, &per_chunk, &n, s);
+  if (rc == CTR_OK) {
+    const cudaError_t e = cudaEventRecord(e1, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "probe event", __FILE__, __LINE__);
+  }
+  unsigned long long cyc = 0;
+  float ms = 0.f;
+  if (rc == CTR_OK) rc = download(&cyc, d_cyc, sizeof(cyc), s);
+  if (rc == CTR_OK) {
+    const cudaError_t e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) rc = cuda_fail(e, "probe event", __FILE__, __LINE__);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CTR_TRY(rc);
+  CTR_TRY(split_error_check(s));
+  const double mmas = (double)nchunk * per_chunk;
+  *clocks_per_mma = (double)cyc / nsm / mmas;
+  *tflops = (double)nsm * mmas * 2.0 * SPLIT_M * n * SPLIT_K / (ms * 1e-3) / 1e12;
+  return CTR_OK;
+}
+
 int split_error_check(cudaStream_t s) {
   if (!g_err_dev) return CTR_OK;
   int h = 0;

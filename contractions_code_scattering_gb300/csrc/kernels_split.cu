@@ -1763,6 +1763,93 @@ int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int
   return CTR_OK;
 }
 
+// MMA schedule probe: the split GEMM's exact per-chunk MMA schedule (issue_chunk
+// of configuration C, a commit per chunk, NSTAGE stage buffers) issued back to
+// back by one thread per SM from shared-memory operands that stay put (hashed
+// BF16 digits, magnitudes near 1), with no producer and no epilogue.  It
+// measures what the tensor pipe gives this schedule by itself; the GEMM's own
+// rate against it shows what its pipeline and tile hand-off cost.  cycles[0]
+// accumulates the issuing thread's clock64 span over the CTAs.
+template <class C>
+__global__ void __launch_bounds__(128, 1) mma_schedule_probe_kernel(int nchunk, unsigned long long* __restrict__ cycles,
+                                                                    int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + NSTAGE * C::A_STAGE;
+  __shared__ uint64_t bar, ebar[NSTAGE];
+  __shared__ uint32_t tslot;
+  const int nwords = NSTAGE * (C::A_STAGE + C::B_STAGE) / 4;
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) {
+    uint32_t h = (uint32_t)i * 2654435761u + blockIdx.x * 97u;
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    ((uint32_t*)smem)[i] = (h & 0x807f807fu) | 0x3f003f00u;  // two BF16 of random sign, in [0.5, 1)
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    for (int st = 0; st < NSTAGE; st++) mbar_init(&ebar[st], 1);
+    fence_mbar_init();
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes, then tensor-core reads
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tmem_alloc(&tslot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = tslot;
+  if (threadIdx.x == 0) {
+    const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
+    const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
+    const unsigned long long t0 = clock64();
+    for (int c = 0; c < nchunk; c++) {
+      const int st = c % NSTAGE;
+      issue_chunk<C>(tbase, adesc0 + (uint64_t)((st * C::A_STAGE) >> 4), bdesc0 + (uint64_t)((st * C::B_STAGE) >> 4),
+                     c == 0);
+      umma_commit(&ebar[st]);
+    }
+    umma_commit(&bar);
+    if (!mbar_wait(&bar, 0, WAIT_NS)) atomicExch(err, 8);
+    atomicAdd(cycles, clock64() - t0);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc_fence_after();
+    tmem_dealloc(tbase, TMEM_COLS);
+  }
+}
+
+static bool g_attr_probe_std = false, g_attr_probe_hp = false;
+template <class C>
+static int launch_mma_probe_cfg(int nchunk, unsigned long long* d_cycles, int* d_err, bool& attr, int* nsm_out,
+                                cudaStream_t s) {
+  const size_t smem = (size_t)NSTAGE * (C::A_STAGE + C::B_STAGE);
+  CTR_TRY(ensure_smem(mma_schedule_probe_kernel<C>, smem, attr));
+  int nsm;
+  CTR_TRY(sm_count(&nsm));
+  TimedLaunch tl(s, "mma_schedule_probe");
+  mma_schedule_probe_kernel<C><<<nsm, 128, smem, s>>>(nchunk, d_cycles, d_err);
+  CTR_CUDA(cudaGetLastError());
+  *nsm_out = nsm;
+  return CTR_OK;
+}
+
+int launch_mma_schedule_probe(int hp, int nchunk, unsigned long long* d_cycles, int* d_err, int* nsm, int* mmas_per_chunk,
+                              int* mma_n, cudaStream_t s) {
+  if (hp) {
+    *mmas_per_chunk = CfgHP::NS * (CfgHP::NS + 1);
+    *mma_n = 2 * CfgHP::BN;
+    return launch_mma_probe_cfg<CfgHP>(nchunk, d_cycles, d_err, g_attr_probe_hp, nsm, s);
+  }
+  *mmas_per_chunk = CfgStd::NS * (CfgStd::NS + 1);
+  *mma_n = 2 * CfgStd::BN;
+  return launch_mma_probe_cfg<CfgStd>(nchunk, d_cycles, d_err, g_attr_probe_std, nsm, s);
+}
+
 int launch_wait_probe(unsigned long long timeout_ns, int* d_err, cudaStream_t s) {
   TimedLaunch tl(s, "wait_probe");
   wait_probe_kernel<<<1, 32, 0, s>>>(timeout_ns, d_err);

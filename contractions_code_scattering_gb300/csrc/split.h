@@ -195,6 +195,11 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
 // A bounded wait that runs out (timeout_ns) on an mbarrier nothing arrives at,
 // recording error code 9 in *d_err (the failure-detection check).
 int launch_wait_probe(unsigned long long timeout_ns, int* d_err, cudaStream_t s);
+// The split GEMM's MMA schedule by itself (ctr_mma_schedule_probe): hp selects
+// the high-precision configuration; returns the grid size, MMAs per K chunk and
+// the MMAs' N.
+int launch_mma_schedule_probe(int hp, int nchunk, unsigned long long* d_cycles, int* d_err, int* nsm, int* mmas_per_chunk,
+                              int* mma_n, cudaStream_t s);
 // Raises the shared-memory limits of the split kernels and caches the SM count.
 int split_kernels_prepare();
 // Closing traces over npair pairs: products of pair q at a_base[q] / b_base[q]

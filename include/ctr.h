@@ -198,6 +198,16 @@ int ctr_zgemm_tasks(int engine, int nev, int ntask, const ctr_ztask* tasks /* ho
  * CTR_ERR_TIMEOUT.  Not recordable in a CUDA graph. */
 int ctr_wait_probe(int timeout_ms, void* stream);
 
+/* Tensor-pipe probe (no counterpart in the reference): one thread per SM issues
+ * the split GEMM's per-chunk MMA schedule (hp = 0: the standard configuration,
+ * 15 slice pairs x 2 MMAs of M128 N128 K16; hp = 1: the high-precision one,
+ * 21 x 2 of M128 N96 K16), nchunk chunks back to back from shared-memory
+ * operands that stay in place, with no operand copies and no epilogue.  Returns
+ * the SM clocks per MMA and the BF16 TFLOP/s of the whole device: the ceiling
+ * of the schedule by itself, against which the GEMM's own rate shows what its
+ * operand pipeline and accumulator hand-off cost.  Not recordable in a graph. */
+int ctr_mma_schedule_probe(int hp, int nchunk, double* clocks_per_mma, double* tflops, void* stream);
+
 /* Diagnostics of the split engine: for one product x*y (nev x nev, device),
  * write the raw FP32 tensor-core accumulators before recombination, as
  * levels[8][nev][128] (Re levels 0, 1, 2, >=3, then Im; element (i,j) at

@@ -144,3 +144,14 @@ def test_tensor_core_accumulation_levels(cuda):
     # addends (measured ~2^-18 of the level), i.e. ~2^-45 of the result
     for a in (3, 7):
         assert np.abs(lv[a] - exact[a]).max() <= 2.0 ** -16 * np.abs(exact[a]).max(), report[a]
+
+
+def test_mma_schedule_probe(cuda):
+    """The split GEMMs' MMA schedules issued alone (ctr_mma_schedule_probe): the
+    standard one at the full tensor rate (64 clocks per M128 N128 K16 MMA), the
+    high-precision one bound by its shared-memory operand reads (~56 clocks per
+    M128 N96 K16 MMA); loose bounds, since only the order of magnitude is checked."""
+    cpm, tf = api.mma_schedule_probe(False, 200)
+    assert 60.0 <= cpm <= 90.0 and tf > 500.0, (cpm, tf)
+    cpm, tf = api.mma_schedule_probe(True, 200)
+    assert 44.0 <= cpm <= 80.0 and tf > 400.0, (cpm, tf)
