@@ -357,10 +357,8 @@ int twosided_split(int N, int Nt, int tf_begin, int tf_end, const double* prop_r
     for (SplitGemmBatch* G : {&GA, &GB}) {
       char gshape[96];
       snprintf(gshape, sizeof(gshape), "std,m=%d,n=%d,k=%d", G->mtiles, G->ntiles, G->nchunk);
-      // 0 / 1: tile walks of the single-CTA kernel; 2 / 3: the same of the CTA-pair,
-      // double-buffered kernel
       int order = 0;
-      CTR_TRY(tune_resolve("split_gemm.order", gshape, 4, 0, stream,
+      CTR_TRY(tune_resolve("split_gemm.order", gshape, 2, 0, stream,
                            [&](int c) {
                              SplitGemmBatch t = *G;
                              t.order = c;

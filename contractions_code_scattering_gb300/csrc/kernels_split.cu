@@ -906,7 +906,7 @@ __device__ __forceinline__ void tile_coords(const SplitGemmBatch& g, int tile, i
   const int per_inst = g.mtiles * g.ntiles;
   inst = tile / per_inst;
   const int r = tile - inst * per_inst;
-  if ((g.order & 1) == 0) {
+  if (g.order == 0) {
     mt = r / g.ntiles;
     nt = r - mt * g.ntiles;
   } else {
@@ -1207,272 +1207,6 @@ __global__ void __launch_bounds__(gemm_threads<C>(), 1)
   if (warp == 0) {
     tc_fence_after();
     tmem_dealloc(tbase, TMEM_COLS);
-  }
-}
-
-// --------------------------------------------- CTA-pair, double-buffered GEMM
-// The standard configuration's block products (float-float output) on clusters
-// of two CTAs (one TPC) with M = 256 MMAs (tcgen05.mma.cta_group::2), issued by
-// the even CTA.  A unit is 2 M tiles x 32 complex columns: each CTA loads its
-// own 128 rows of the left operand and, of the right operand's 32 columns, the
-// two planes it supplies to the packed MMAs (even CTA -Yi, Yr; odd CTA Yr, Yi;
-// one half of a 64-column slicer tile).  The accumulators of a unit take 256
-// TMEM columns, so two units alternate in the 512 columns: the epilogue drains
-// one while the MMAs fill the other, and no tile boundary waits for a drain.
-// Same slice pairs, levels and order per accumulator as split_gemm_kernel, so
-// the products are bit-identical.
-constexpr int PDB_BH = 32;                          // complex columns of a unit
-constexpr int PDB_NSTAGE = 4;
-constexpr int PDB_B_SUB = PDB_BH * SPLIT_K * 2;     // one plane half: 1 KB
-constexpr int PDB_B_STAGE = SPLIT_NSLICE * 2 * PDB_B_SUB;
-constexpr int PDB_ACC = CfgStd::NL * 2 * PDB_BH;   // 256 TMEM columns a buffer
-constexpr size_t PDB_SMEM = (size_t)PDB_NSTAGE * (SPLIT_A_STAGE + PDB_B_STAGE) + GEMM_SMEM_TAIL;
-static_assert(2 * PDB_ACC <= (int)TMEM_COLS, "two accumulator buffers");
-
-template <int I = 0, int J = 0>
-__device__ __forceinline__ void pdb_issue(uint32_t d0, uint64_t adesc, uint64_t bdesc, bool first_chunk) {
-  if constexpr (I < SPLIT_NSLICE) {
-    if constexpr (I + J < SPLIT_NSLICE) {
-      constexpr uint32_t idw = idesc_bf16_f32(2 * SPLIT_M, 2 * PDB_BH, false);
-      constexpr int lvl = (I + J) < CfgStd::NL - 1 ? (I + J) : CfgStd::NL - 1;
-      const uint32_t accum = (!first_chunk || !(I == 0 && J <= CfgStd::NL - 1)) ? 1u : 0u;
-      const uint64_t ar = adesc + (uint64_t)(((I * 2 + 0) * SPLIT_A_SUB) >> 4);
-      const uint64_t ai = adesc + (uint64_t)(((I * 2 + 1) * SPLIT_A_SUB) >> 4);
-      const uint64_t b_nr = bdesc + (uint64_t)(((J * 2 + 0) * PDB_B_SUB) >> 4);  // [-Yi | Yr]
-      const uint64_t b_ri = bdesc + (uint64_t)(((J * 2 + 1) * PDB_B_SUB) >> 4);  // [Yr | Yi]
-      const uint32_t d = d0 + (uint32_t)(lvl * 2 * PDB_BH);
-      umma_f16_pair(d, ar, b_ri, idw, accum);  // [Re | Im] += Xr [Yr | Yi]
-      umma_f16_pair(d, ai, b_nr, idw, 1u);     // [Re | Im] += Xi [-Yi | Yr]
-      pdb_issue<I, J + 1>(d0, adesc, bdesc, first_chunk);
-    } else {
-      pdb_issue<I + 1, 0>(d0, adesc, bdesc, first_chunk);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(gemm_threads<CfgStd>(), 1)
-    split_gemm_pair_db_kernel(SplitGemmBatch g, int nunits, int* __restrict__ err) {
-  using C = CfgStd;
-  extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + PDB_NSTAGE * SPLIT_A_STAGE;
-  uint64_t* full = (uint64_t*)(smem + PDB_NSTAGE * (SPLIT_A_STAGE + PDB_B_STAGE));
-  uint64_t* empty = full + PDB_NSTAGE;
-  uint64_t* tfull = empty + PDB_NSTAGE;  // per accumulator buffer
-  uint64_t* tempty = tfull + 2;
-  uint64_t* drainb = tempty + 2;
-  uint32_t* tslot = (uint32_t*)(drainb + 1);
-  volatile int* status = (volatile int*)(tslot + 1);
-  int* sexp = (int*)(tslot + 4);  // PDB_BH column exponents of the current unit
-  static_assert(8 * (2 * PDB_NSTAGE + 5) + 16 + 4 * PDB_BH <= GEMM_SMEM_TAIL, "GEMM shared-memory tail");
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t rank = cluster_ctarank();
-  const int unit0 = (int)(blockIdx.x >> 1), unit_step = (int)(gridDim.x >> 1);
-  const int mpairs = (g.mtiles + 1) >> 1, nhalves = 2 * g.ntiles;
-
-  if (threadIdx.x == 0) {
-    for (int st = 0; st < PDB_NSTAGE; st++) {
-      mbar_init(&full[st], rank == 0 ? 2 : 1);  // the even CTA also takes the odd CTA's relayed arrival
-      mbar_init(&empty[st], 1);
-    }
-    for (int b = 0; b < 2; b++) {
-      mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 2 * C::EPI_WARPS);  // epilogue warps of both CTAs
-    }
-    mbar_init(drainb, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  cluster_sync();  // both CTAs' barriers initialised before any remote arrival
-  if (warp == 0) {
-    tmem_alloc_pair(tslot, TMEM_COLS);
-    tmem_relinquish_pair();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tbase = *tslot;
-  // unit -> (instance, M pair, N half), N halves innermost (order 0) or M pairs innermost (order 1)
-  auto coords = [&](int u, int& inst, int& mt, int& nt, int& h) {
-    const int per = mpairs * nhalves;
-    inst = u / per;
-    const int r = u - inst * per;
-    int mp, nu;
-    if ((g.order & 1) == 0) {
-      mp = r / nhalves;
-      nu = r - mp * nhalves;
-    } else {
-      nu = r / mpairs;
-      mp = r - nu * mpairs;
-    }
-    mt = 2 * mp + (int)rank;
-    nt = nu >> 1;
-    h = nu & 1;
-  };
-
-  if (warp == 0) {
-    if (lane == 0) {
-      uint32_t gc = 0;
-      bool ok = true;
-      for (int u = unit0; u < nunits && ok; u += unit_step) {
-        int inst, mt, nt, h;
-        coords(u, inst, mt, nt, h);
-        const SplitGemmInst* I = &g.inst[inst];
-        const bool avalid = mt < g.mtiles;  // the odd CTA past the last M tile loads no rows
-        const uint8_t* gA = I->left + (size_t)mt * g.nchunk * SPLIT_A_STAGE;
-        const uint8_t* gB = I->right + (size_t)nt * g.nchunk * SPLIT_B_STAGE + h * PDB_B_SUB;
-        const uint32_t bytes = (avalid ? SPLIT_A_STAGE : 0) + PDB_B_STAGE;
-        for (int kc = 0; kc < g.nchunk; kc++, gc++) {
-          const int st = gc % PDB_NSTAGE;
-          if (gc >= PDB_NSTAGE && !mbar_wait(&empty[st], ((gc / PDB_NSTAGE) - 1) & 1, WAIT_NS, err)) {
-            atomicExch(err, 1);
-            ok = false;
-            break;
-          }
-          mbar_arrive_expect_tx(&full[st], bytes);
-          if (avalid) bulk_g2s(sA + st * SPLIT_A_STAGE, gA + (size_t)kc * SPLIT_A_STAGE, SPLIT_A_STAGE, &full[st]);
-          // slice j: planes (-Yi, Yr) for the even CTA, (Yr, Yi) for the odd one, this unit's half of each
-          const uint8_t* src = gB + (size_t)kc * SPLIT_B_STAGE;
-          uint8_t* dst = sB + st * PDB_B_STAGE;
-#pragma unroll
-          for (int j = 0; j < SPLIT_NSLICE; j++) {
-            bulk_g2s(dst + (j * 2 + 0) * PDB_B_SUB, src + (size_t)(j * 3 + rank) * SPLIT_B_SUB, PDB_B_SUB, &full[st]);
-            bulk_g2s(dst + (j * 2 + 1) * PDB_B_SUB, src + (size_t)(j * 3 + rank + 1) * SPLIT_B_SUB, PDB_B_SUB,
-                     &full[st]);
-          }
-        }
-      }
-    }
-  } else if (warp == 1) {
-    if (lane == 0 && rank != 0) {
-      // odd CTA: relay each stage's arrival to the even CTA, whose MMAs read it too
-      uint32_t gc = 0;
-      bool ok = true;
-      for (int u = unit0; u < nunits && ok; u += unit_step)
-        for (int kc = 0; kc < g.nchunk; kc++, gc++) {
-          const int st = gc % PDB_NSTAGE;
-          if (!mbar_wait(&full[st], (gc / PDB_NSTAGE) & 1, WAIT_NS, err)) {
-            atomicExch(err, 2);
-            ok = false;
-            break;
-          }
-          mbar_arrive_cluster(mapa_shared(smem_u32(&full[st]), 0));
-        }
-      if (!mbar_wait(drainb, 0, 2 * WAIT_NS)) atomicExch(err, 5);
-    } else if (lane == 0) {
-      uint32_t gc = 0, local = 0;
-      bool ok = true;
-      const uint64_t adesc0 = sdesc_kmajor_noswz(smem_u32(sA), 128, 256);
-      const uint64_t bdesc0 = sdesc_kmajor_noswz(smem_u32(sB), 128, 256);
-      for (int u = unit0; u < nunits && ok; u += unit_step, local++) {
-        const uint32_t buf = local & 1;
-        // the buffer's previous unit (two back) drained by both CTAs' epilogues
-        if (local >= 2 && !mbar_wait_cluster(&tempty[buf], ((local >> 1) - 1) & 1, 2 * WAIT_NS, err)) {
-          atomicExch(err, 4);
-          break;
-        }
-        tc_fence_after();
-        const uint32_t d0 = tbase + buf * PDB_ACC;
-        for (int kc = 0; kc < g.nchunk; kc++, gc++) {
-          const int st = gc % PDB_NSTAGE;
-          if (!mbar_wait_cluster(&full[st], (gc / PDB_NSTAGE) & 1, WAIT_NS, err)) {
-            atomicExch(err, 2);
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          pdb_issue(d0, adesc0 + (uint64_t)((st * SPLIT_A_STAGE) >> 4), bdesc0 + (uint64_t)((st * PDB_B_STAGE) >> 4),
-                    kc == 0);
-          umma_commit_pair(&empty[st]);  // stage free in both CTAs once these MMAs have read it
-        }
-        if (ok) umma_commit_pair(&tfull[buf]);
-      }
-      umma_commit_pair(drainb);
-      if (!mbar_wait(drainb, 0, WAIT_NS)) atomicExch(err, 5);
-    }
-  } else {
-    // epilogue: warp w drains TMEM lane quadrant w % 4, 8 of the unit's 32 columns
-    constexpr int CPW = PDB_BH / (C::EPI_WARPS / 4);
-    const int q = warp & 3, part_w = (warp - 2) / 4;
-    const int et = threadIdx.x - 64;
-    const int row = q * 32 + lane;
-    const uint32_t tl = tbase + ((uint32_t)(q * 32) << 16);
-    const int ldo = g.ldo;
-    uint32_t local = 0;
-    for (int u = unit0; u < nunits; u += unit_step, local++) {
-      int inst, mt, nt, h;
-      coords(u, inst, mt, nt, h);
-      const SplitGemmInst* I = &g.inst[inst];
-      const uint32_t buf = local & 1;
-      const int col0 = nt * SPLIT_N + h * PDB_BH;  // first column of the unit
-      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI_WARPS) : "memory");
-      if (et < PDB_BH) sexp[et] = I->rexp[col0 + et];
-      const int grow = mt * SPLIT_M + row;
-      const bool rvalid = mt < g.mtiles && grow < g.mrows;
-      const int erow = mt < g.mtiles ? I->lexp[grow] : 0;
-      if (et == 0) {
-        const bool done = mbar_wait(&tfull[buf], (local >> 1) & 1, 4 * WAIT_NS, err);
-        if (!done) atomicExch(err, 3);
-        status[1] = done ? 0 : 1;
-      }
-      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI_WARPS) : "memory");
-      if (status[1]) break;
-      tc_fence_after();
-      const int cbase = part_w * CPW;
-      const uint32_t tb = tl + buf * PDB_ACC;
-      float v[2][C::NL][CPW];
-#pragma unroll
-      for (int part = 0; part < 2; part++)
-#pragma unroll
-        for (int l = 0; l < C::NL; l++) tmem_ld8(tb + (uint32_t)((l * 2 + part) * PDB_BH + cbase), v[part][l]);
-      tmem_ld_wait();
-      // accumulators drained: hand the buffer back to the even CTA's MMA thread
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) {
-        if (rank != 0)
-          mbar_arrive_cluster(mapa_shared(smem_u32(&tempty[buf]), 0));
-        else
-          mbar_arrive(&tempty[buf]);
-      }
-      if (rvalid) {
-        float4* outp = I->out;
-#pragma unroll
-        for (int c = 0; c < CPW; c++) {
-          const int gcol = col0 + cbase + c;
-          float r4[4];
-#pragma unroll
-          for (int part = 0; part < 2; part++) {
-            // levels 0 .. NL-2 exact, combined by exact two-sums; the rounding
-            // errors and the last level go to the low word (as split_gemm_kernel)
-            float sm = v[part][0][c], e = 0.f;
-#pragma unroll
-            for (int l = 1; l < C::NL - 1; l++) {
-              float t, d;
-              two_sum(sm, v[part][l][c], t, d);
-              sm = t;
-              e += d;
-            }
-            float hi, lo;
-            fast_two_sum(sm, e + v[part][C::NL - 1][c], hi, lo);
-            r4[part * 2 + 0] = hi;
-            r4[part * 2 + 1] = lo;
-          }
-          if (gcol >= g.ncols) continue;
-          const int ex = erow + sexp[cbase + c];
-          const float sc = ex < FF_MIN_EXP ? __int_as_float(0x7fc00000) : pow2f(ex);
-          outp[(size_t)gcol * ldo + grow] = make_float4(r4[0] * sc, r4[1] * sc, r4[2] * sc, r4[3] * sc);
-        }
-      }
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  cluster_sync();  // neither CTA leaves while the other may still address it
-  if (warp == 0) {
-    tc_fence_after();
-    tmem_dealloc_pair(tbase, TMEM_COLS);
   }
 }
 
@@ -2150,47 +1884,8 @@ static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err,
   return CTR_OK;
 }
 
-// The CTA-pair double-buffered form of the standard configuration (order bit 1).
-static bool g_attr_pdb = false;
-static int g_pdb_clusters = 0;
-static int launch_split_gemm_pair_db(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
-  if (g.levels) return fail(CTR_ERR_ARG, "split GEMM: the CTA-pair form writes products only");
-  CTR_TRY(ensure_smem(split_gemm_pair_db_kernel, PDB_SMEM, g_attr_pdb));
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.blockDim = dim3(gemm_threads<CfgStd>());
-  cfg.dynamicSmemBytes = PDB_SMEM;
-  cfg.stream = s;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  if (!g_pdb_clusters) {
-    int nsm;
-    CTR_TRY(sm_count(&nsm));
-    cfg.gridDim = dim3(2 * (nsm / 2));
-    int nc = 0;
-    CTR_CUDA(cudaOccupancyMaxActiveClusters(&nc, (void*)split_gemm_pair_db_kernel, &cfg));
-    if (nc < 1) return fail(CTR_ERR_UNSUPPORTED, "split GEMM: no CTA pair fits on this device");
-    g_pdb_clusters = nc;
-  }
-  const long long units = (long long)ninst * ((g.mtiles + 1) / 2) * (2LL * g.ntiles);
-  if (units > 0x7fffffffLL) return fail(CTR_ERR_ARG, "split GEMM: too many tiles");
-  cfg.gridDim = dim3((unsigned)(2 * std::min<long long>(units, g_pdb_clusters)));
-  TimedLaunch tl(s, "split_gemm");
-  CTR_CUDA(cudaLaunchKernelEx(&cfg, split_gemm_pair_db_kernel, g, (int)units, d_err));
-  // useful tiles only: the odd CTA past an odd M tile count computes padding
-  if (!capturing())
-    g_split_mma_flops += (double)ninst * g.mtiles * g.ntiles * (CfgStd::NS * (CfgStd::NS + 1) / 2) * 8.0 * SPLIT_M *
-                         CfgStd::BN * SPLIT_K * g.nchunk;
-  return CTR_OK;
-}
-
 int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
   if (ninst == 0) return CTR_OK;
-  if (!g.hp && g.out_mode == 0 && (g.order & 2)) return launch_split_gemm_pair_db(g, ninst, d_err, s);
   if (g.hp) {
     if (g.out_mode != 1 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: the high-precision tiles write complex128");
     return launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");

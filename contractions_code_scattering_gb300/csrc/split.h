@@ -96,8 +96,7 @@ struct SplitGemmBatch {
   int out_mode;      // 0: float-float column-major, 1: complex128 row-major blocks
   int blkn;          // out_mode 1: columns (and row stride) of one output block
   int hp;            // 0: CfgStd operands and tiles, 1: CfgHP (out_mode 1 only)
-  int order;         // bit 0: persistent tile walk (0 N tiles innermost, 1 M tiles innermost);
-                     // bit 1 (standard configuration): CTA pairs, double-buffered accumulators
+  int order;         // persistent tile walk: 0 N tiles innermost, 1 M tiles innermost
 };
 
 // Operands of the task form C = sum_q w_q op(A_q) op(B_q) (q < nterm <= 4),

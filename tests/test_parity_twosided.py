@@ -108,28 +108,6 @@ def test_staged_slicer_writes_the_same_bytes(cuda, n):
     P.entrywise(got[1], ref, TOL["split"], ab, "rho, staged slicer")
 
 
-@pytest.mark.parametrize("n", [100, 37, 128])
-def test_pair_double_buffered_gemm_is_bitwise_equal(cuda, n):
-    """The standard block products on CTA pairs with double-buffered accumulators
-    (split_gemm.order 2 and 3: M = 256 MMAs over two CTAs, 32-column units) give
-    the same bits as the single-CTA kernel (order 0), including the odd CTA past an
-    odd M tile count (16 stacked blocks of Nev = 100 are 13 tiles)."""
-    nt = 3
-    prop, mom5 = _inputs(nt, n, seed=700 + n)
-    d_prop, d_mom = torch.from_numpy(prop).to(cuda), torch.from_numpy(mom5).to(cuda)
-    got = {}
-    try:
-        for order in (0, 2, 3):
-            api.tune_force("split_gemm.order", order)
-            got[order] = api.run_contract_rho(d_prop, d_mom, engine="split").cpu().numpy()
-    finally:
-        api.tune_force("split_gemm.order", -1)
-    assert np.array_equal(got[0], got[2])
-    assert np.array_equal(got[0], got[3])
-    ref, ab = ref_rho(prop, mom5)
-    P.entrywise(got[2], ref, TOL["split"], ab, "rho, CTA-pair GEMM")
-
-
 @pytest.mark.parametrize("shift", [60, 110])
 def test_split_rho_beyond_float_float_range(cuda, shift):
     """Perambulators scaled by 2^-shift push the split engine's two-sided form
