@@ -644,6 +644,7 @@ def _timed(fn, steps, warmup):
     torch.cuda.synchronize()
     _lib.timing_enable(True)
     _lib.split_flops(reset=True)
+    _lib.gram_flops(reset=True)
     n0 = _lib.launch_count()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -658,6 +659,8 @@ def _timed(fn, steps, warmup):
     kern = {k: {"launches": v[0], "ms": v[2]} for k, v in rep.items()}
     mma, prods = _lib.split_flops()
     kern["_split_work"] = {"mma_flops": mma / steps, "block_products": prods / steps, "steps": steps}
+    gmma, gtr = _lib.gram_flops()
+    kern["_gram_work"] = {"mma_flops": gmma / steps, "traces": gtr / steps, "steps": steps}
     return e0.elapsed_time(e1) / 1e3 / steps, launches, kern
 
 
@@ -679,6 +682,26 @@ def chain_roofline(kern, nev):
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
             "algorithmic": "executed: 21 bf16 slice-pair products x 8 M N K per tile (the library's launch count); "
                            "FP64-equivalent: 8 Nev^3 per complex block product"}
+
+
+def gram_roofline(kern, nev):
+    """gram_gemm (the closing traces of the momentum-set calls as Gram products)
+    against the measured BF16 peak: executed BF16 MMA flops (the library's count,
+    padding included) and the FP64-equivalent rate of the traces (8 Nev^2 each)."""
+    w = kern.get("_gram_work", {})
+    g = kern.get("gram_gemm")
+    if not g or not w.get("mma_flops"):
+        return None
+    t = g["ms"] / 1e3 / max(1, w.get("steps", 1))
+    pk = measured_peaks()
+    peak = pk.get("bf16_tflops", 1924.8)
+    achieved = w["mma_flops"] / t / 1e12
+    return {"kernel": "gram_gemm", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "fp64_equivalent_tflops": w["traces"] * 8.0 * nev ** 2 / t / 1e12,
+            "gemm_ms_per_step": 1e3 * t, "traces_per_step": w["traces"],
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in pk else "fallback 1924.8",
+            "algorithmic": "executed: 21 bf16 slice-pair products x 8 M N K per tile (the library's launch count); "
+                           "FP64-equivalent: 8 Nev^2 per closing trace"}
 
 
 def _errs(a, b):
@@ -952,8 +975,10 @@ def mixed_block(args, full=False):
            "value": diagrams / t, "unit": "diagrams/s", "ms_per_step": 1e3 * t, "steps": steps, "warmup": warm,
            "form": form, "diagrams_per_step": diagrams, "gpu_launches": launches,
            "split_refined_entries_per_step": refined_step, "roofline": chain_roofline(kern, nev),
+           "gram_roofline": gram_roofline(kern, nev),
            "kernels": {k: v for k, v in kern.items() if not k.startswith("_")},
-           "autotune": {k: v for k, v in api.tune_report().items() if k.startswith("split_gemm.order|hp")}}
+           "autotune": {k: v for k, v in api.tune_report().items()
+                        if k.startswith("split_gemm.order|hp") or k.startswith("chains.trace_form")}}
     got = [x.cpu().numpy() for x in holder["r"]]
     if form == "sets":
         with api.Graph(stream) as gr:

@@ -69,6 +69,7 @@ def lib(build_if_missing=True):
     L.ctr_split_set_refine.argtypes = [d]
     L.ctr_split_refined.restype = ctypes.c_longlong
     L.ctr_split_flops.argtypes = [ctypes.POINTER(d), ctypes.POINTER(d), i]
+    L.ctr_gram_flops.argtypes = [ctypes.POINTER(d), ctypes.POINTER(d), i]
     L.ctr_apply_profile.argtypes = [i, ctypes.c_longlong, vp, vp, vp, vp]
     L.ctr_chain_adjoint.argtypes = [i, i, i, i, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]
     L.ctr_rho_profile_vjp.argtypes = [i, i, i, vp, vp, vp, vp, vp, vp, vp]
@@ -135,4 +136,12 @@ def split_flops(reset=False):
     launches since the last reset (include/ctr.h: ctr_split_flops)."""
     a, b = ctypes.c_double(), ctypes.c_double()
     check(lib().ctr_split_flops(ctypes.byref(a), ctypes.byref(b), 1 if reset else 0))
+    return a.value, b.value
+
+
+def gram_flops(reset=False):
+    """(executed BF16 MMA flops, closing traces) of the split engine's Gram-product
+    trace launches since the last reset (include/ctr.h: ctr_gram_flops)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(lib().ctr_gram_flops(ctypes.byref(a), ctypes.byref(b), 1 if reset else 0))
     return a.value, b.value

@@ -98,6 +98,8 @@ enum {
   WS_SPLITJOBS4,    // distinct blocks of a task launch
   WS_BLOCKEXP,      // their row / column exponent bounds
   WS_TRACEGROUPS,   // grouped closing traces of a two-sided call
+  WS_GRAM,          // sliced operands and partial products of Gram traces
+  WS_GRAMJOBS,      // their block, instance and trace tables
   WS_COUNT
 };
 
@@ -113,6 +115,9 @@ extern long long g_refined_last;
 // block products they computed (8 Nev^3 FP64-equivalent flops each).  Counted by
 // eager launches; replays of recorded graphs are not counted.
 extern double g_split_mma_flops, g_split_products;
+// The same for the Gram products of closing traces (ctr_gram_flops): executed
+// BF16 MMA flops and the traces they produced (8 Nev^2 FP64-equivalent flops each).
+extern double g_gram_mma_flops, g_gram_traces;
 
 // Reads (and clears) the device-side error flag of the split engine; syncs the stream.
 int split_error_check(cudaStream_t s);
@@ -141,6 +146,24 @@ struct GridTask {
   int nslab, nb, nterm, adag, bdag;
 };
 int zgemm_split_grids(int N, const std::vector<GridTask>& grids, cudaStream_t stream);
+
+// Closing traces Tr-Had(X, Y) = sum_e X_e conj(Y_e) of many left and right
+// blocks that meet in groups, as Gram products on the split engine: group g has
+// left blocks left[g * mrows + r] and right blocks right[g * ncols + c] (null:
+// a block of zeros); trace k of tr takes (g, r, c) and writes coef * value to
+// trv[slot] and, where tra is not null, its error scale to tra[slot] (a bound of
+// sum |X|_1 |Y|_1 and of the slices' truncation, relative to which the value
+// keeps ~2^-52).
+struct GramPlan {
+  struct Tr {
+    int g, r, c, slot;
+    float cre, cim;
+  };
+  int ngroup = 0, mrows = 0, ncols = 0;
+  std::vector<const double2*> left, right;
+  std::vector<Tr> tr;
+};
+int trace_gram(int N, const GramPlan& plan, double2* trv, double* tra, cudaStream_t stream);
 
 // ------------------------------------------------------------ graph capture
 // A host step that reads device results (e.g. the split engine's refinement

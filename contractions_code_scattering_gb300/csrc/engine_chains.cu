@@ -1487,6 +1487,27 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
     if (used * sizeof(double2) + ntr * (sizeof(double2) + sizeof(double)) > (size_t)np * per_pair)
       return fail(CTR_ERR_ALLOC, "ctr_rhopi_sigmapi_sets: batch arena overflow");
     TracePlan tp;
+    // on the split engine the same traces as Gram products: group i * 4 + s2 of
+    // pair i pairs the X blocks (set combination ci, row block s5, column block
+    // s2) with the Z blocks (sink operator slab, tau block (s3, s2)); every trace
+    // takes an X and a Z block with the same s2
+    GramPlan gp;
+    const bool gram = c.engine == CTR_ENGINE_SPLIT;
+    if (gram) {
+      gp.ngroup = 4 * np;
+      gp.mrows = 4 * nC;
+      gp.ncols = 4 * nops;
+      gp.left.resize((size_t)gp.ngroup * gp.mrows);
+      gp.right.resize((size_t)gp.ngroup * gp.ncols);
+      for (int i = 0; i < np; i++)
+        for (int s2 = 0; s2 < 4; s2++) {
+          const size_t g = (size_t)i * 4 + s2;
+          for (int ci = 0; ci < nC; ci++)
+            for (int s5 = 0; s5 < 4; s5++) gp.left[g * gp.mrows + ci * 4 + s5] = Xblk(ci, i, s5, s2);
+          for (int sl = 0; sl < nops; sl++)
+            for (int s3 = 0; s3 < 4; s3++) gp.right[g * gp.ncols + sl * 4 + s3] = Zblk(sl, i, s3 * 4 + s2);
+        }
+    }
     RowItems it_rp[3], it_tr;
     for (int idir = 0; idir < 3; idir++) {
       it_rp[idir].nrows = ngr;
@@ -1505,9 +1526,11 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
           // Tr-Had(X_{s5 s2}, Phi_ip^dag tau_{s3 s2}) without its coefficient, once for the three
           // polarisations (those of ip = 0, 1 are shared); the row sums apply the coefficients
           const int base = (int)tp.tt.size();
-          for (const auto& u : uniq)
-            tp.add(Xblk(ci, i, std::get<1>(u) / 4, std::get<1>(u) % 4), Zblk(std::get<0>(u), i, std::get<2>(u)), 1.f,
-                   0.f, 0);
+          for (const auto& u : uniq) {
+            const int xb = std::get<1>(u), zb = std::get<2>(u);
+            const int slot = tp.add(Xblk(ci, i, xb / 4, xb % 4), Zblk(std::get<0>(u), i, zb), 1.f, 0.f, 0);
+            if (gram) gp.tr.push_back({i * 4 + xb % 4, ci * 4 + xb / 4, std::get<0>(u) * 4 + zb / 4, slot, 1.f, 0.f});
+          }
           for (int idir = 0; idir < 3; idir++) {
             for (int g = 0; g < ngr; g++) it_rp[idir].slot.push_back(base + uidx[idir][g]);
             it_rp[idir].ent.push_back((k * 3 + idir) * npairs + pair);
@@ -1515,9 +1538,11 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
         }
         if (tri) {
           for (int ik = 0; ik < 2; ik++)
-            for (int b = 0; b < 16; b++)
-              it_tr.slot.push_back(
-                  tp.add(Xblk(ci, i, b / 4, b % 4), Zblk(slab_of[5 + ik], i, b), (float)G5[b / 4], 0.f, 0));
+            for (int b = 0; b < 16; b++) {
+              const int slot = tp.add(Xblk(ci, i, b / 4, b % 4), Zblk(slab_of[5 + ik], i, b), (float)G5[b / 4], 0.f, 0);
+              it_tr.slot.push_back(slot);
+              if (gram) gp.tr.push_back({i * 4 + b % 4, ci * 4 + b / 4, slab_of[5 + ik] * 4 + b / 4, slot, (float)G5[b / 4], 0.f});
+            }
           it_tr.ent.push_back(k * npairs + pair);
         }
       }
@@ -1527,7 +1552,17 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       if (tra) tp.tt[k].absout = tra + k;
     }
     CTR_TRY(run_grids(c, g0, WS_TASKS));
-    CTR_TRY(run_traces(c, tp.tt));
+    if (gram) {
+      // 0: the FP64 trace kernel, 1: Gram products on the tensor cores
+      int form = 1;
+      auto run = [&](int f) { return f ? trace_gram(N, gp, trv, tra, c.s) : run_traces(c, tp.tt); };
+      CTR_TRY(tune_resolve("chains.trace_form", "nev=" + std::to_string(N) + ",m=" + std::to_string(gp.mrows) +
+                                                    ",n=" + std::to_string(gp.ncols),
+                           2, 1, c.s, run, &form));
+      CTR_TRY(run(form));
+    } else {
+      CTR_TRY(run_traces(c, tp.tt));
+    }
     CTR_TRY(upload_items(c, {&it_rp[0], &it_rp[1], &it_rp[2], &it_tr}));
     for (int idir = 0; idir < 3 && rhopi; idir++)
       CTR_TRY(rowsum_items(c, trv, tra, it_rp[idir], (double2*)rhopi, rf_rp));

@@ -626,8 +626,16 @@ extern "C" int ctr_split_flops(double* executed_mma, double* block_products, int
   return CTR_OK;
 }
 
+extern "C" int ctr_gram_flops(double* executed_mma, double* traces, int reset) {
+  if (executed_mma) *executed_mma = ctr::g_gram_mma_flops;
+  if (traces) *traces = ctr::g_gram_traces;
+  if (reset) ctr::g_gram_mma_flops = ctr::g_gram_traces = 0.0;
+  return CTR_OK;
+}
+
 namespace ctr {
 double g_split_mma_flops = 0.0, g_split_products = 0.0;
+double g_gram_mma_flops = 0.0, g_gram_traces = 0.0;
 double g_refine_tol = 1e-9;
 long long g_refined_last = 0;
 }  // namespace ctr
@@ -961,6 +969,82 @@ int zgemm_split_grids(int N, const std::vector<GridTask>& grids, cudaStream_t st
       if (!capturing()) g_split_products += (double)ni * ns * nb * nterm;
     }
   }
+  return CTR_OK;
+}
+
+// Gram traces.  Instance ip = g * npiece + p of a launch is the product of group
+// g's left and right blocks over K piece p (at most GRAM_PIECE elements of
+// the flattened Nev^2): one high-precision tile pair per (M tile, N tile), its
+// complex128 partial product written row-major (rows padded to M tiles,
+// columns to N tiles).  Groups run in launches sized to a 4 GB arena; each
+// launch slices its operands, runs the GEMM and sums its traces' pieces.
+int trace_gram(int N, const GramPlan& P, double2* trv, double* tra, cudaStream_t stream) {
+  if (P.tr.empty()) return CTR_OK;
+  if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d (got %d)", SPLIT_MAXK, N);
+  if (P.ngroup < 1 || P.mrows < 1 || P.ncols < 1 || P.left.size() != (size_t)P.ngroup * P.mrows ||
+      P.right.size() != (size_t)P.ngroup * P.ncols)
+    return fail(CTR_ERR_ARG, "Gram traces: %d groups of %d x %d blocks, tables of %zu and %zu", P.ngroup, P.mrows,
+                P.ncols, P.left.size(), P.right.size());
+  int* d_err;
+  CTR_TRY(err_flag(&d_err));
+  const int n2 = N * N;
+  const int nchunk = std::min(GRAM_PIECE / SPLIT_K, cdiv(n2, SPLIT_K)), npiece = cdiv(n2, nchunk * SPLIT_K);
+  const int mtiles = cdiv(P.mrows, SPLIT_M), ntiles = cdiv(P.ncols, CfgHP::BN);
+  const int lrows = mtiles * SPLIT_M, rcols = ntiles * CfgHP::BN;
+  // per instance: left and right slices, partial product, exponents and norms
+  const size_t l_b = (size_t)mtiles * nchunk * CfgHP::A_STAGE, r_b = (size_t)ntiles * nchunk * CfgHP::B_STAGE;
+  const size_t p_b = (size_t)lrows * rcols * sizeof(double2);
+  const size_t per_inst = l_b + r_b + p_b + (size_t)(lrows + rcols) * (sizeof(int) + sizeof(float));
+  const size_t per_group = (size_t)npiece * per_inst;
+  const int G = (int)std::max<size_t>(1, std::min<size_t>(P.ngroup, ((size_t)4 << 30) / per_group));
+  for (const GramPlan::Tr& t : P.tr)
+    if (t.g < 0 || t.g >= P.ngroup || t.r < 0 || t.r >= P.mrows || t.c < 0 || t.c >= P.ncols)
+      return fail(CTR_ERR_ARG, "Gram traces: trace (%d, %d, %d) outside the plan", t.g, t.r, t.c);
+  // traces by launch, in plan order
+  const int nl = cdiv(P.ngroup, G);
+  std::vector<std::vector<GramTrace>> by(nl);
+  for (const GramPlan::Tr& t : P.tr)
+    by[t.g / G].push_back(GramTrace{t.g % G, t.r, t.c, t.slot, {t.cre, t.cim}});
+  for (int li = 0; li < nl; li++) {
+    const int g0 = li * G, ng = std::min(G, P.ngroup - g0), ni = ng * npiece;
+    void* mem;
+    CTR_TRY(workspace(WS_GRAM).get((size_t)ni * per_inst + 1024, &mem));
+    uint8_t* lsl = (uint8_t*)mem;
+    uint8_t* rsl = lsl + (size_t)ni * l_b;
+    double2* part = (double2*)(rsl + (size_t)ni * r_b);
+    int* lexp = (int*)(part + (size_t)ni * lrows * rcols);
+    int* rexp = lexp + (size_t)ni * lrows;
+    float* lnorm = (float*)(rexp + (size_t)ni * rcols);
+    float* rnorm = lnorm + (size_t)ni * lrows;
+    std::vector<SplitGemmInst> gi(ni);
+    std::vector<double2*> outs(ni);
+    for (int ip = 0; ip < ni; ip++) {
+      outs[ip] = part + (size_t)ip * lrows * rcols;
+      gi[ip] = SplitGemmInst{lsl + (size_t)ip * l_b, rsl + (size_t)ip * r_b, lexp + (size_t)ip * lrows,
+                             rexp + (size_t)ip * rcols, nullptr, nullptr};
+    }
+    const std::vector<GramTrace>& tl = by[li];
+    void* d[4];
+    CTR_TRY(upload_group(WS_GRAMJOBS,
+                         {{P.left.data() + (size_t)g0 * P.mrows, (size_t)ng * P.mrows * sizeof(const double2*)},
+                          {P.right.data() + (size_t)g0 * P.ncols, (size_t)ng * P.ncols * sizeof(const double2*)},
+                          {outs.data(), outs.size() * sizeof(double2*)},
+                          {tl.data(), tl.size() * sizeof(GramTrace)}},
+                         d, stream));
+    for (int ip = 0; ip < ni; ip++) gi[ip].outs = (double2* const*)d[2] + ip;
+    void* d_gi;
+    CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
+    CTR_TRY(launch_slice_gram(false, (const double2* const*)d[0], ng, P.mrows, mtiles, n2, npiece, nchunk, lsl, lexp,
+                              lnorm, stream));
+    CTR_TRY(launch_slice_gram(true, (const double2* const*)d[1], ng, P.ncols, ntiles, n2, npiece, nchunk, rsl, rexp,
+                              rnorm, stream));
+    SplitGemmBatch B{(const SplitGemmInst*)d_gi, mtiles, ntiles, nchunk, P.mrows, P.ncols, lrows, nullptr, 1, rcols, 1};
+    B.order = 0;
+    CTR_TRY(launch_split_gemm(B, ni, d_err, stream, true));
+    CTR_TRY(launch_gram_trace_sum((const GramTrace*)d[3], (int)tl.size(), part, npiece, lrows, rcols, lexp, rexp, lnorm,
+                                  rnorm, trv, tra, stream));
+  }
+  if (!capturing()) g_gram_traces += (double)P.tr.size();
   return CTR_OK;
 }
 

@@ -1625,6 +1625,154 @@ __global__ void wait_probe_kernel(unsigned long long timeout_ns, int* __restrict
   if (!mbar_wait(&bar, 0, timeout_ns)) atomicExch(err, 9);
 }
 
+// ------------------------------------------------ closing traces as Gram products
+// |v| / 2^E as a float from the double's high word (integer operations; the
+// mantissa truncated to 20 bits, enough for a norm that bounds an error), 0
+// below FP32's normal range.  |v| < 2^E, so the result is below 1.
+__device__ __forceinline__ float abs_rel_f32(double v, int E) {
+  const int hi = __double2hiint(v) & 0x7FFFFFFF;
+  const int e = (hi >> 20) - 1023 - E + 127;
+  return e <= 0 ? 0.f : __int_as_float((e << 23) | ((hi & 0xFFFFF) << 3));
+}
+
+// Gram operand slicing: CTA = (instance ip = group * npiece + piece, operand
+// tile t).  Rows of a tile are blocks flattened to n2 elements (TR = 128 left
+// rows, BN right columns); K is the piece.  Pass 1: warp w takes rows w, w + 8,
+// ...: each lane holds 16 of the piece's elements, the row's scale exponent is
+// the largest bound (plus one: the leading digit halved) and its norm the
+// 2-norm of (|Re| + |Im|) / 2^E.  Pass 2: the piece's K chunks in turn, the
+// next chunk's elements loaded while this one is sliced into a shared-memory
+// stage and copied out.  Right tiles hold conj(Y) in the packed planes
+// (-Im, Re, Im).
+template <class C, bool RIGHT>
+__global__ void __launch_bounds__(256) slice_gram_kernel(const double2* const* __restrict__ blk, int nrows, int ntile,
+                                                         int n2, int npiece, int nchunk, uint8_t* __restrict__ out,
+                                                         int* __restrict__ exps, float* __restrict__ norms) {
+  constexpr int TR = RIGHT ? C::BN : SPLIT_M;
+  constexpr int STAGE = RIGHT ? C::B_STAGE : C::A_STAGE;
+  constexpr int SUB = RIGHT ? C::B_SUB : C::A_SUB;
+  constexpr int PER = (TR * SPLIT_K + 255) / 256;
+  constexpr int LPR = GRAM_PIECE / 32;  // elements of a piece a lane holds in pass 1
+  extern __shared__ __align__(128) uint8_t sm[];
+  int* sexp = (int*)sm;                              // [TR]
+  const double2** sptr = (const double2**)(sm + 512);  // [TR]
+  uint8_t* stage = sm + 512 + 8 * SPLIT_M;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ip = blockIdx.x / ntile, t = blockIdx.x - ip * ntile;
+  const int g = ip / npiece, p = ip - g * npiece;
+  const int piece = nchunk * SPLIT_K, k0 = p * piece;
+  const size_t orow = ((size_t)ip * ntile + t) * TR;
+  for (int r = warp; r < TR; r += 8) {
+    const int row = t * TR + r;
+    const double2* b = row < nrows ? blk[(size_t)g * nrows + row] : nullptr;
+    double2 v[LPR];
+#pragma unroll
+    for (int u = 0; u < LPR; u++) {
+      const int k = lane + 32 * u;
+      v[u] = (b && k < piece && k0 + k < n2) ? b[k0 + k] : make_double2(0.0, 0.0);
+    }
+    int m = -30000;
+#pragma unroll
+    for (int u = 0; u < LPR; u++) m = max(m, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
+    for (int off = 16; off; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+    const int E = (m < -1000 ? 0 : m) + 1;
+    float nn = 0.f;
+#pragma unroll
+    for (int u = 0; u < LPR; u++) {
+      const float a = abs_rel_f32(v[u].x, E) + abs_rel_f32(v[u].y, E);
+      nn = fmaf(a, a, nn);
+    }
+    for (int off = 16; off; off >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, off);
+    if (lane == 0) {
+      sexp[r] = E;
+      sptr[r] = b;
+      exps[orow + r] = E;
+      norms[orow + r] = m < -1000 ? 0.f : sqrtf(nn);
+    }
+  }
+  __syncthreads();
+  auto load = [&](int kc, double2* v) {
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + u * 256;
+      const int rr = e >> 4, k = k0 + kc * SPLIT_K + (e & 15);
+      const double2* b = e < TR * SPLIT_K ? sptr[rr] : nullptr;
+      v[u] = (b && k < n2) ? b[k] : make_double2(0.0, 0.0);
+    }
+  };
+  double2 cur[PER], nxt[PER];
+  load(0, cur);
+  uint8_t* dst0 = out + orow / TR * (size_t)nchunk * STAGE;
+  for (int kc = 0; kc < nchunk; kc++) {
+    if (kc + 1 < nchunk) load(kc + 1, nxt);
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + u * 256;
+      if (e >= TR * SPLIT_K) break;
+      const int rr = e >> 4, kk = e & 15;
+      const int E = sexp[rr];
+      bool nr, ni;
+      uint64_t Ur, Ui;
+      weighted_fixed(cur[u], 0, false, RIGHT, E, Ur, nr, Ui, ni);
+      Ur = round_fixed<C::NS>(Ur);
+      Ui = round_fixed<C::NS>(Ui);
+      const uint32_t off = core_offset(rr, kk);
+#pragma unroll
+      for (int s = 0; s < C::NS; s++) {
+        if constexpr (RIGHT) {
+          const __nv_bfloat16 bi = slice_bf16(Ui, s, ni);
+          *(__nv_bfloat16*)(stage + (s * 3 + 0) * SUB + off) = bf16_neg(bi);
+          *(__nv_bfloat16*)(stage + (s * 3 + 1) * SUB + off) = slice_bf16(Ur, s, nr);
+          *(__nv_bfloat16*)(stage + (s * 3 + 2) * SUB + off) = bi;
+        } else {
+          *(__nv_bfloat16*)(stage + (s * 2 + 0) * SUB + off) = slice_bf16(Ur, s, nr);
+          *(__nv_bfloat16*)(stage + (s * 2 + 1) * SUB + off) = slice_bf16(Ui, s, ni);
+        }
+      }
+    }
+    __syncthreads();
+    int4* d = (int4*)(dst0 + (size_t)kc * STAGE);
+    const int4* src = (const int4*)stage;
+    for (int i = threadIdx.x; i < STAGE / 16; i += 256) d[i] = src[i];
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < PER; u++) cur[u] = nxt[u];
+  }
+}
+
+// Trace values of a Gram launch, one thread per trace: the pieces' partial
+// products summed in piece order, times the coefficient; the error scale
+// sum_p (|x_p| |y_p| + 8) 2^(E_x + E_y) bounds sum |x|_1 |y|_1 (Cauchy-Schwarz
+// over the piece) and the truncation of the slices (~2^-54 of the scales an
+// element, 2^-48 over a piece's 512 of them with random signs); a piece whose
+// row or column is all zeros adds neither.
+__global__ void __launch_bounds__(128) gram_trace_sum_kernel(const GramTrace* __restrict__ tr, int ntr,
+                                                             const double2* __restrict__ part, int npiece, int lrows,
+                                                             int rcols, const int* __restrict__ lexp,
+                                                             const int* __restrict__ rexp,
+                                                             const float* __restrict__ lnorm,
+                                                             const float* __restrict__ rnorm, double2* __restrict__ trv,
+                                                             double* __restrict__ tra) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntr) return;
+  const GramTrace T = tr[i];
+  double re = 0.0, im = 0.0, ab = 0.0;
+  for (int p = 0; p < npiece; p++) {
+    const size_t ip = (size_t)T.g * npiece + p;
+    const double2 v = part[(ip * lrows + T.r) * rcols + T.c];
+    re += v.x;
+    im += v.y;
+    if (tra) {
+      const float nx = lnorm[ip * lrows + T.r], ny = rnorm[ip * rcols + T.c];
+      if (nx > 0.f && ny > 0.f)
+        ab += ((double)nx * (double)ny + 8.0) * pow2d(lexp[ip * lrows + T.r] + rexp[ip * rcols + T.c]);
+    }
+  }
+  const double2 c = make_double2((double)T.coef[0], (double)T.coef[1]);
+  trv[T.slot] = cmul(c, make_double2(re, im));
+  if (tra) tra[T.slot] = sqrt(c.x * c.x + c.y * c.y) * ab;
+}
+
 // --------------------------------------------------------------- launchers
 // Dynamic shared-memory limits are raised once per kernel (before any graph
 // capture, through split_kernels_prepare, or at the first launch).
@@ -1763,6 +1911,42 @@ int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int
   return CTR_OK;
 }
 
+static bool g_attr_gl = false, g_attr_gr = false;
+
+int launch_slice_gram(bool right, const double2* const* d_blk, int ngroup, int nrows, int ntile, int n2, int npiece,
+                      int nchunk, uint8_t* out, int* exps, float* norms, cudaStream_t s) {
+  if (ngroup == 0) return CTR_OK;
+  if (nchunk < 1 || nchunk * SPLIT_K > GRAM_PIECE || (long long)npiece * nchunk * SPLIT_K < n2)
+    return fail(CTR_ERR_ARG, "Gram slicer: %d chunks x %d pieces do not cover %d elements", nchunk, npiece, n2);
+  const long long grid = (long long)ngroup * npiece * ntile;
+  if (grid > 0x7fffffffLL) return fail(CTR_ERR_ARG, "Gram slicer: grid too large");
+  const size_t head = 512 + 8 * SPLIT_M;
+  if (right) {
+    CTR_TRY(ensure_smem(slice_gram_kernel<CfgHP, true>, head + CfgHP::B_STAGE, g_attr_gr));
+    TimedLaunch tl(s, "slice_gram_right");
+    slice_gram_kernel<CfgHP, true><<<(unsigned)grid, 256, head + CfgHP::B_STAGE, s>>>(d_blk, nrows, ntile, n2, npiece,
+                                                                                      nchunk, out, exps, norms);
+  } else {
+    CTR_TRY(ensure_smem(slice_gram_kernel<CfgHP, false>, head + CfgHP::A_STAGE, g_attr_gl));
+    TimedLaunch tl(s, "slice_gram_left");
+    slice_gram_kernel<CfgHP, false><<<(unsigned)grid, 256, head + CfgHP::A_STAGE, s>>>(d_blk, nrows, ntile, n2, npiece,
+                                                                                       nchunk, out, exps, norms);
+  }
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
+int launch_gram_trace_sum(const GramTrace* d_tr, int ntr, const double2* part, int npiece, int lrows, int rcols,
+                          const int* lexp, const int* rexp, const float* lnorm, const float* rnorm, double2* trv,
+                          double* tra, cudaStream_t s) {
+  if (ntr == 0) return CTR_OK;
+  TimedLaunch tl(s, "gram_trace_sum");
+  gram_trace_sum_kernel<<<(ntr + 127) / 128, 128, 0, s>>>(d_tr, ntr, part, npiece, lrows, rcols, lexp, rexp, lnorm,
+                                                          rnorm, trv, tra);
+  CTR_CUDA(cudaGetLastError());
+  return CTR_OK;
+}
+
 // MMA schedule probe: the split GEMM's exact per-chunk MMA schedule (issue_chunk
 // of configuration C, a commit per chunk, NSTAGE stage buffers) issued back to
 // back by one thread per SM from shared-memory operands that stay put (hashed
@@ -1867,7 +2051,8 @@ int launch_block_exp(const double2* const* d_blk, int nblk, int nev, int* bexp, 
 }
 
 template <class C>
-static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, const char* name) {
+static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, const char* name,
+                                 double* flops) {
   const size_t smem = gemm_smem_bytes<C>();
   CTR_TRY(ensure_smem(split_gemm_kernel<C>, smem, gemm_attr_flag<C>()));
   int nsm;
@@ -1879,19 +2064,19 @@ static int launch_split_gemm_cfg(const SplitGemmBatch& g, int ninst, int* d_err,
   split_gemm_kernel<C><<<grid, gemm_threads<C>(), smem, s>>>(g, (int)total, d_err);
   CTR_CUDA(cudaGetLastError());
   // slice pairs i + j < NS, each two packed MMAs of M x 2BN x 16: 8 M BN 16 flops
-  if (!capturing())
-    g_split_mma_flops += (double)total * (C::NS * (C::NS + 1) / 2) * 8.0 * SPLIT_M * C::BN * SPLIT_K * g.nchunk;
+  if (!capturing()) *flops += (double)total * (C::NS * (C::NS + 1) / 2) * 8.0 * SPLIT_M * C::BN * SPLIT_K * g.nchunk;
   return CTR_OK;
 }
 
-int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s) {
+int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, bool gram) {
   if (ninst == 0) return CTR_OK;
   if (g.hp) {
     if (g.out_mode != 1 || g.levels) return fail(CTR_ERR_ARG, "split GEMM: the high-precision tiles write complex128");
-    return launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp");
+    return gram ? launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "gram_gemm", &g_gram_mma_flops)
+                : launch_split_gemm_cfg<CfgHP>(g, ninst, d_err, s, "split_gemm_hp", &g_split_mma_flops);
   }
-  if (g.out_mode != 0) return fail(CTR_ERR_ARG, "split GEMM: the standard tiles write float-float");
-  return launch_split_gemm_cfg<CfgStd>(g, ninst, d_err, s, "split_gemm");
+  if (gram || g.out_mode != 0) return fail(CTR_ERR_ARG, "split GEMM: the standard tiles write float-float");
+  return launch_split_gemm_cfg<CfgStd>(g, ninst, d_err, s, "split_gemm", &g_split_mma_flops);
 }
 
 int launch_trace_rows(const TraceRow* d_rows, int nrows, const float4* const* d_abase, const float4* const* d_bbase,

@@ -159,6 +159,20 @@ struct TraceGroup {
   int ta[TG_MAXT], tb[TG_MAXT], tr[TG_MAXT];
 };
 
+// Closing traces as Gram products.  A group of left blocks X_r (r < mrows) and
+// right blocks Y_c (c < ncols) whose traces Tr-Had(X_r, Y_c) = sum_e X_r,e
+// conj(Y_c,e) are many is one product G = X' Y'^dagger, X' and Y' the blocks
+// flattened into rows of Nev^2 elements.  K runs in pieces of at most
+// GRAM_PIECE elements, each an instance of the high-precision GEMM with its own
+// row and column scales (the leading digit halved, so that level 0 stays exact
+// up to K = 512); the pieces' complex128 partial products are summed per trace.
+constexpr int GRAM_PIECE = 512;
+struct GramTrace {
+  int g, r, c;   // group (within the launch), left row, right column
+  int slot;      // output slot: trv[slot], tra[slot]
+  float coef[2]; // complex coefficient of the trace
+};
+
 // ------------------------------------------------------ float-float helpers
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -191,7 +205,27 @@ int launch_slice_left(const SliceLeftJob* d_jobs, int njobs, int nev, int nchunk
                       int form = 0);
 int launch_slice_right(const SliceRightJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, cudaStream_t s,
                        int form = 0);
-int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s);
+// gram: the launch computes Gram products of closing traces (timed as
+// "gram_gemm" and counted apart from the block products' MMA flops).
+int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream_t s, bool gram = false);
+// Gram operands (high-precision tiles): for instance ip = g * npiece + p and
+// tile t, the blocks blk[g * nrows + t * TR + r] (r < TR = 128 left / BN right;
+// rows past nrows or null pointers are zero) over elements [p piece,
+// (p + 1) piece) of their n2, as nchunk K chunks at out + ((ip * ntile + t) *
+// nchunk + kc) * stage; the scale exponent (with the leading digit halved) and
+// the 2-norm of (|Re| + |Im|) / 2^E of each row at exps / norms[ip * ntile * TR
+// + t * TR + r].  right: the operand is conj(Y) as the right planes
+// (-Im, Re, Im) of a K-major B.
+int launch_slice_gram(bool right, const double2* const* d_blk, int ngroup, int nrows, int ntile, int n2, int npiece,
+                      int nchunk, uint8_t* out, int* exps, float* norms, cudaStream_t s);
+// Trace values of a Gram launch: trv[slot] = coef * sum over the pieces of the
+// partial product (r, c) (instance ip's at part + ip * lrows * rcols, row-major
+// rcols), tra[slot] (when not null) = |coef| * sum over the pieces of
+// (|x_p| |y_p| + 8) 2^(E_x + E_y), a bound of sum |x|_1 |y|_1 and of the slices'
+// truncation error (rows or columns of zeros add nothing).
+int launch_gram_trace_sum(const GramTrace* d_tr, int ntr, const double2* part, int npiece, int lrows, int rcols,
+                          const int* lexp, const int* rexp, const float* lnorm, const float* rnorm, double2* trv,
+                          double* tra, cudaStream_t s);
 // A bounded wait that runs out (timeout_ns) on an mbarrier nothing arrives at,
 // recording error code 9 in *d_err (the failure-detection check).
 int launch_wait_probe(unsigned long long timeout_ns, int* d_err, cudaStream_t s);

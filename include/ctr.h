@@ -334,6 +334,11 @@ long long ctr_split_refined(void);
  * launches, 8 Nev^3 FP64-equivalent flops each.  Eager launches only (replays of
  * recorded graphs are not counted).  reset != 0 zeroes both after reading. */
 int ctr_split_flops(double* executed_mma, double* block_products, int reset);
+/* The same for the Gram products that take the closing traces of the split
+ * engine's momentum-set calls (ctr_rhopi_sigmapi_sets): executed_mma = BF16 flops
+ * of those GEMM launches, traces = closing traces they produced (8 Nev^2
+ * FP64-equivalent flops each).  No counterpart in the reference. */
+int ctr_gram_flops(double* executed_mma, double* traces, int reset);
 
 /* Synchronise the stream and report the first device-side error flag. */
 int ctr_sync(void* stream);

@@ -32,6 +32,21 @@ def _dev(a, cuda):
     return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
 
 
+class trace_form:
+    """Forces the split engine's closing-trace form of the momentum-set calls
+    (chains.trace_form: 0 the FP64 trace kernel, 1 Gram products on the tensor
+    cores) inside a with block."""
+
+    def __init__(self, form):
+        self.form = form
+
+    def __enter__(self):
+        api.tune_force("chains.trace_form", self.form)
+
+    def __exit__(self, *exc):
+        api.tune_force("chains.trace_form", -1)
+
+
 # ---- oracle references with their per-entry row magnitudes
 def ref_pipi(prop, ph, iso, tfs=None):
     tfs = range(prop.shape[0]) if tfs is None else tfs
@@ -193,13 +208,28 @@ def test_mixed_config_shape_split(cuda):
         ref, ab = ref_loop(prop, mom2[:, k])
         P.entrywise(got, ref, tol, ab, "sigma loop %d" % k)
     # the same pair through the batched call (with the reversed pair as a second set): bitwise
+    # with the FP64 closing traces the per-set calls use
     phi_all = torch.stack([dp1, dp2], dim=1).contiguous()
-    bat = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(tp, diag, phi_all, [(0, 1), (1, 0)], d5, d2,
-                                                                     engine="split").items()}
+    with trace_form(0):
+        bat = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(tp, diag, phi_all, [(0, 1), (1, 0)], d5, d2,
+                                                                         engine="split").items()}
     for idir in range(3):
         assert np.array_equal(bat["rhopi"][0, idir], _np(api.run_contract_rhopi(tp, diag, dp1, dp2, d5, idir,
                                                                                  engine="split")))
     assert np.array_equal(bat["triangle"][0], _np(tri)) and np.array_equal(bat["hor_fish"][0], _np(hf))
+    # and with the closing traces as Gram products (K = 128^2 in 32 pieces of 512), per entry
+    # against the oracle
+    with trace_form(1):
+        gr = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(tp, diag, phi_all, [(0, 1), (1, 0)], d5, d2,
+                                                                        engine="split").items()}
+    for idir in range(3):
+        ref, ab = ref_rhopi(prop, p1, p2, mom5, idir, rows)
+        P.entrywise(gr["rhopi"][0, idir][rows], ref, tol, ab, "Gram traces: rhopi idir %d" % idir)
+        ref, ab = ref_rhopi(prop, p2, p1, mom5, idir, rows)
+        P.entrywise(gr["rhopi"][1, idir][rows], ref, tol, ab, "Gram traces: reversed set, rhopi idir %d" % idir)
+    ref, ab = ref_triangle(prop, p1, p2, mom2, rows)
+    P.entrywise(gr["triangle"][0][rows], ref, tol, ab, "Gram traces: sigma-pipi triangle")
+    assert np.array_equal(gr["hor_fish"][0], _np(hf))
 
 
 @pytest.fixture(scope="module")
@@ -296,8 +326,9 @@ def test_rhopi_sigmapi_sets_bitwise_equal_to_per_set_calls(cuda, engine):
     diag = api.prop_diag(tp)
     tr = (1, 3)
     rows = tp[tr[0]:tr[1]].contiguous()
-    got = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(rows, diag, phi_all, sets, d5, d2, engine=engine,
-                                                                     tf_range=tr).items()}
+    with trace_form(0):
+        got = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(rows, diag, phi_all, sets, d5, d2,
+                                                                         engine=engine, tf_range=tr).items()}
     for k, (a, b) in enumerate(sets):
         pa, pb = phi_all[:, a].contiguous(), phi_all[:, b].contiguous()
         for idir in range(3):
@@ -313,6 +344,47 @@ def test_rhopi_sigmapi_sets_bitwise_equal_to_per_set_calls(cuda, engine):
     P.entrywise(got["triangle"][4], ref, tol, ab, "set (1,4) triangle vs oracle")
     ref, ab = ref_hor_fish(prop, phis[moms[1]], phis[moms[4]])
     P.entrywise(got["hor_fish"][4], ref, tol, ab, "set (1,4) hor fish vs oracle")
+
+
+@pytest.mark.parametrize("n", [12, 100])
+def test_rhopi_sigmapi_sets_gram_traces(cuda, n):
+    """ctr_rhopi_sigmapi_sets on the split engine with its closing traces as Gram
+    products (one group per pair and tau column block s2: the sets' X blocks against
+    the sink operators' Z blocks): every set's rho -> pi pi and sigma -> pi pi
+    triangle per entry against the oracle, and against the FP64 closing traces.
+    Nev = 12: one K piece of 144 elements; Nev = 100: 20 pieces, the last one
+    272 elements long."""
+    nt = 3 if n == 100 else 4
+    prop = synth.make_prop(nt, n, seed=1700 + n, decay=0.25)
+    moms = [(0, 0, 0), (1, 1, 0), (-1, -1, 0), (0, 0, 1), (0, 0, -1)]
+    phis = synth.make_phi_momenta(nt, n, moms, seed=1701 + n)
+    cuda_phi = _dev(np.stack([phis[p] for p in moms], axis=1), cuda)
+    rng = np.random.default_rng(1702 + n)
+    mom5 = np.ascontiguousarray(np.stack([synth.make_phi_random(nt, n, rng) for _ in range(5)], axis=1))
+    mom2 = np.ascontiguousarray(np.stack([synth.make_phi_random(nt, n, rng) for _ in range(2)], axis=1))
+    d5, d2 = _dev(mom5, cuda), _dev(mom2, cuda)
+    sets = [(1, 2), (2, 1), (3, 4), (0, 0), (1, 4)]
+    tp = _dev(prop, cuda)
+    diag = api.prop_diag(tp)
+    tr = (1, 3)
+    rows = tp[tr[0]:tr[1]].contiguous()
+    got = {}
+    for form in (0, 1):
+        with trace_form(form):
+            got[form] = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(
+                rows, diag, cuda_phi, sets, d5, d2, engine="split", tf_range=tr).items()}
+    g, f = got[1], got[0]
+    tol = 1e-9 if n == 100 else SPLIT_TOL
+    for k, (a, b) in enumerate(sets):
+        pa, pb = phis[moms[a]], phis[moms[b]]
+        for idir in range(3):
+            ref, ab = ref_rhopi(prop, pa, pb, mom5, idir, range(tr[0], tr[1]))
+            P.entrywise(g["rhopi"][k, idir], ref, tol, ab, "set %d rhopi idir %d, Gram traces" % (k, idir))
+            P.entrywise(g["rhopi"][k, idir], f["rhopi"][k, idir], tol, ab, "set %d idir %d, Gram vs FP64 traces" % (k, idir))
+        ref, ab = ref_triangle(prop, pa, pb, mom2, range(tr[0], tr[1]))
+        P.entrywise(g["triangle"][k], ref, tol, ab, "set %d triangle, Gram traces" % k)
+        # the horizontal fish keeps its per-time-slice FP64 traces
+        assert np.array_equal(g["hor_fish"][k], f["hor_fish"][k])
 
 
 def test_block_product_tasks_split_vs_fp64(cuda):
