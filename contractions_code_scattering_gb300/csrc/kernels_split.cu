@@ -1635,15 +1635,19 @@ __device__ __forceinline__ float abs_rel_f32(double v, int E) {
   return e <= 0 ? 0.f : __int_as_float((e << 23) | ((hi & 0xFFFFF) << 3));
 }
 
-// Gram operand slicing: CTA = (instance ip = group * npiece + piece, operand
-// tile t).  Rows of a tile are blocks flattened to n2 elements (TR = 128 left
-// rows, BN right columns); K is the piece.  Pass 1: warp w takes rows w, w + 8,
-// ...: each lane holds 16 of the piece's elements, the row's scale exponent is
-// the largest bound (plus one: the leading digit halved) and its norm the
-// 2-norm of (|Re| + |Im|) / 2^E.  Pass 2: the piece's K chunks in turn, the
-// next chunk's elements loaded while this one is sliced into a shared-memory
-// stage and copied out.  Right tiles hold conj(Y) in the packed planes
-// (-Im, Re, Im).
+// Gram operand slicing: CTA = (instance ip = group * npiece + piece, 8 rows of
+// an operand tile).  Rows are blocks flattened to n2 elements (tiles of TR =
+// 128 left rows or BN right columns); K is the piece.  The CTA stages its 8
+// rows' pieces in shared memory (one read of each element); warp w then takes
+// row w: its scale exponent is the largest bound (plus one: the leading digit
+// halved), its norm the 2-norm of (|Re| + |Im|) / 2^E.  Last, warp w writes
+// the digits of rows 2 (w % 4) and 2 (w % 4) + 1 (one per half warp, so that
+// each store fills whole 32-byte sectors of the core matrices) over half of
+// the piece, as packed BF16 pairs straight to the tiled operand.  Rows past
+// nrows get their exponent and norm but no digits: their products land in
+// padding rows or columns that are never stored.  Right tiles hold conj(Y) in
+// the packed planes (-Im, Re, Im).
+constexpr int GRAM_SLICE_SMEM = 8 * GRAM_PIECE * 16;
 template <class C, bool RIGHT>
 __global__ void __launch_bounds__(256) slice_gram_kernel(const double2* const* __restrict__ blk, int nrows, int ntile,
                                                          int n2, int npiece, int nchunk, uint8_t* __restrict__ out,
@@ -1651,92 +1655,82 @@ __global__ void __launch_bounds__(256) slice_gram_kernel(const double2* const* _
   constexpr int TR = RIGHT ? C::BN : SPLIT_M;
   constexpr int STAGE = RIGHT ? C::B_STAGE : C::A_STAGE;
   constexpr int SUB = RIGHT ? C::B_SUB : C::A_SUB;
-  constexpr int PER = (TR * SPLIT_K + 255) / 256;
-  constexpr int LPR = GRAM_PIECE / 32;  // elements of a piece a lane holds in pass 1
-  extern __shared__ __align__(128) uint8_t sm[];
-  int* sexp = (int*)sm;                              // [TR]
-  const double2** sptr = (const double2**)(sm + 512);  // [TR]
-  uint8_t* stage = sm + 512 + 8 * SPLIT_M;
+  constexpr int RG = TR / 8;  // CTAs per tile
+  static_assert(TR % 8 == 0, "8 rows a CTA");
+  extern __shared__ __align__(16) double2 sv[];  // [8][GRAM_PIECE]
+  __shared__ int sE[8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ip = blockIdx.x / ntile, t = blockIdx.x - ip * ntile;
+  const int ip = blockIdx.x / (ntile * RG), rest = blockIdx.x - ip * (ntile * RG);
+  const int t = rest / RG, r0 = (rest - t * RG) * 8;  // first row of the CTA within the tile
   const int g = ip / npiece, p = ip - g * npiece;
-  const int piece = nchunk * SPLIT_K, k0 = p * piece;
-  const size_t orow = ((size_t)ip * ntile + t) * TR;
-  for (int r = warp; r < TR; r += 8) {
-    const int row = t * TR + r;
+  const int piece = nchunk * SPLIT_K, k0 = p * piece, kmax = min(piece, n2 - k0);
+  // asynchronous copies (all of a thread's 16 in flight), zeros written directly
+#pragma unroll
+  for (int rr = 0; rr < 8; rr++) {
+    const int row = t * TR + r0 + rr;
     const double2* b = row < nrows ? blk[(size_t)g * nrows + row] : nullptr;
-    double2 v[LPR];
 #pragma unroll
-    for (int u = 0; u < LPR; u++) {
-      const int k = lane + 32 * u;
-      v[u] = (b && k < piece && k0 + k < n2) ? b[k0 + k] : make_double2(0.0, 0.0);
+    for (int u = 0; u < GRAM_PIECE / 256; u++) {
+      const int k = threadIdx.x + 256 * u;
+      if (k >= piece) continue;
+      if (b && k < kmax)
+        cp_async16(sv + rr * GRAM_PIECE + k, b + k0 + k);
+      else
+        sv[rr * GRAM_PIECE + k] = make_double2(0.0, 0.0);
     }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  {
+    const double2* x = sv + warp * GRAM_PIECE;
     int m = -30000;
-#pragma unroll
-    for (int u = 0; u < LPR; u++) m = max(m, max(f64_exp_bound(v[u].x), f64_exp_bound(v[u].y)));
+    for (int k = lane; k < piece; k += 32) m = max(m, max(f64_exp_bound(x[k].x), f64_exp_bound(x[k].y)));
     for (int off = 16; off; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
     const int E = (m < -1000 ? 0 : m) + 1;
     float nn = 0.f;
-#pragma unroll
-    for (int u = 0; u < LPR; u++) {
-      const float a = abs_rel_f32(v[u].x, E) + abs_rel_f32(v[u].y, E);
+    for (int k = lane; k < piece; k += 32) {
+      const float a = abs_rel_f32(x[k].x, E) + abs_rel_f32(x[k].y, E);
       nn = fmaf(a, a, nn);
     }
     for (int off = 16; off; off >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, off);
     if (lane == 0) {
-      sexp[r] = E;
-      sptr[r] = b;
-      exps[orow + r] = E;
-      norms[orow + r] = m < -1000 ? 0.f : sqrtf(nn);
+      const size_t orow = ((size_t)ip * ntile + t) * TR + r0 + warp;
+      exps[orow] = E;
+      norms[orow] = m < -1000 ? 0.f : sqrtf(nn);
+      sE[warp] = E;
     }
   }
   __syncthreads();
-  auto load = [&](int kc, double2* v) {
+  const int rr = 2 * (warp & 3) + (lane >> 4);
+  if (t * TR + r0 + rr >= nrows) return;
+  const int E = sE[rr];
+  const double2* x = sv + rr * GRAM_PIECE;
+  uint8_t* tile = out + ((size_t)ip * ntile + t) * nchunk * STAGE;
+  for (int q = (warp >> 2) * (GRAM_PIECE / 4) + (lane & 15); q < (warp >> 2) * (GRAM_PIECE / 4) + GRAM_PIECE / 4;
+       q += 16) {
+    const int k = 2 * q;
+    if (k >= piece) break;
+    bool nr0, ni0, nr1, ni1;
+    uint64_t Ur0, Ui0, Ur1, Ui1;
+    weighted_fixed(x[k], 0, false, RIGHT, E, Ur0, nr0, Ui0, ni0);
+    weighted_fixed(x[k + 1], 0, false, RIGHT, E, Ur1, nr1, Ui1, ni1);
+    Ur0 = round_fixed<C::NS>(Ur0);
+    Ui0 = round_fixed<C::NS>(Ui0);
+    Ur1 = round_fixed<C::NS>(Ur1);
+    Ui1 = round_fixed<C::NS>(Ui1);
+    uint8_t* d = tile + (size_t)(k >> 4) * STAGE + core_offset(r0 + rr, k & 15);
 #pragma unroll
-    for (int u = 0; u < PER; u++) {
-      const int e = threadIdx.x + u * 256;
-      const int rr = e >> 4, k = k0 + kc * SPLIT_K + (e & 15);
-      const double2* b = e < TR * SPLIT_K ? sptr[rr] : nullptr;
-      v[u] = (b && k < n2) ? b[k] : make_double2(0.0, 0.0);
-    }
-  };
-  double2 cur[PER], nxt[PER];
-  load(0, cur);
-  uint8_t* dst0 = out + orow / TR * (size_t)nchunk * STAGE;
-  for (int kc = 0; kc < nchunk; kc++) {
-    if (kc + 1 < nchunk) load(kc + 1, nxt);
-#pragma unroll
-    for (int u = 0; u < PER; u++) {
-      const int e = threadIdx.x + u * 256;
-      if (e >= TR * SPLIT_K) break;
-      const int rr = e >> 4, kk = e & 15;
-      const int E = sexp[rr];
-      bool nr, ni;
-      uint64_t Ur, Ui;
-      weighted_fixed(cur[u], 0, false, RIGHT, E, Ur, nr, Ui, ni);
-      Ur = round_fixed<C::NS>(Ur);
-      Ui = round_fixed<C::NS>(Ui);
-      const uint32_t off = core_offset(rr, kk);
-#pragma unroll
-      for (int s = 0; s < C::NS; s++) {
-        if constexpr (RIGHT) {
-          const __nv_bfloat16 bi = slice_bf16(Ui, s, ni);
-          *(__nv_bfloat16*)(stage + (s * 3 + 0) * SUB + off) = bf16_neg(bi);
-          *(__nv_bfloat16*)(stage + (s * 3 + 1) * SUB + off) = slice_bf16(Ur, s, nr);
-          *(__nv_bfloat16*)(stage + (s * 3 + 2) * SUB + off) = bi;
-        } else {
-          *(__nv_bfloat16*)(stage + (s * 2 + 0) * SUB + off) = slice_bf16(Ur, s, nr);
-          *(__nv_bfloat16*)(stage + (s * 2 + 1) * SUB + off) = slice_bf16(Ui, s, ni);
-        }
+    for (int s = 0; s < C::NS; s++) {
+      const uint32_t re = slice_pair(Ur0, nr0, Ur1, nr1, s), im = slice_pair(Ui0, ni0, Ui1, ni1, s);
+      if constexpr (RIGHT) {
+        *(uint32_t*)(d + (s * 3 + 0) * SUB) = im ^ BF16X2_SIGNS;
+        *(uint32_t*)(d + (s * 3 + 1) * SUB) = re;
+        *(uint32_t*)(d + (s * 3 + 2) * SUB) = im;
+      } else {
+        *(uint32_t*)(d + (s * 2 + 0) * SUB) = re;
+        *(uint32_t*)(d + (s * 2 + 1) * SUB) = im;
       }
     }
-    __syncthreads();
-    int4* d = (int4*)(dst0 + (size_t)kc * STAGE);
-    const int4* src = (const int4*)stage;
-    for (int i = threadIdx.x; i < STAGE / 16; i += 256) d[i] = src[i];
-    __syncthreads();
-#pragma unroll
-    for (int u = 0; u < PER; u++) cur[u] = nxt[u];
   }
 }
 
@@ -1919,18 +1913,17 @@ int launch_slice_gram(bool right, const double2* const* d_blk, int ngroup, int n
   if (nchunk < 1 || nchunk * SPLIT_K > GRAM_PIECE || (long long)npiece * nchunk * SPLIT_K < n2)
     return fail(CTR_ERR_ARG, "Gram slicer: %d chunks x %d pieces do not cover %d elements", nchunk, npiece, n2);
   const long long grid = (long long)ngroup * npiece * ntile;
-  if (grid > 0x7fffffffLL) return fail(CTR_ERR_ARG, "Gram slicer: grid too large");
-  const size_t head = 512 + 8 * SPLIT_M;
+  if (grid * (SPLIT_M / 8) > 0x7fffffffLL) return fail(CTR_ERR_ARG, "Gram slicer: grid too large");
   if (right) {
-    CTR_TRY(ensure_smem(slice_gram_kernel<CfgHP, true>, head + CfgHP::B_STAGE, g_attr_gr));
+    CTR_TRY(ensure_smem(slice_gram_kernel<CfgHP, true>, GRAM_SLICE_SMEM, g_attr_gr));
     TimedLaunch tl(s, "slice_gram_right");
-    slice_gram_kernel<CfgHP, true><<<(unsigned)grid, 256, head + CfgHP::B_STAGE, s>>>(d_blk, nrows, ntile, n2, npiece,
-                                                                                      nchunk, out, exps, norms);
+    slice_gram_kernel<CfgHP, true><<<(unsigned)(grid * (CfgHP::BN / 8)), 256, GRAM_SLICE_SMEM, s>>>(
+        d_blk, nrows, ntile, n2, npiece, nchunk, out, exps, norms);
   } else {
-    CTR_TRY(ensure_smem(slice_gram_kernel<CfgHP, false>, head + CfgHP::A_STAGE, g_attr_gl));
+    CTR_TRY(ensure_smem(slice_gram_kernel<CfgHP, false>, GRAM_SLICE_SMEM, g_attr_gl));
     TimedLaunch tl(s, "slice_gram_left");
-    slice_gram_kernel<CfgHP, false><<<(unsigned)grid, 256, head + CfgHP::A_STAGE, s>>>(d_blk, nrows, ntile, n2, npiece,
-                                                                                       nchunk, out, exps, norms);
+    slice_gram_kernel<CfgHP, false><<<(unsigned)(grid * (SPLIT_M / 8)), 256, GRAM_SLICE_SMEM, s>>>(
+        d_blk, nrows, ntile, n2, npiece, nchunk, out, exps, norms);
   }
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
