@@ -605,13 +605,14 @@ __global__ void __launch_bounds__(256) slice_task_left_kernel(const SliceTaskLJo
 }
 
 // Stacked left operand slices: CTA = (job, M tile, K chunk).  Row g of the stack
-// is row g % nev of slab g / nev; 128 rows x 16 k, 8 elements a thread.
+// is row g % nev of slab g / nev; 128 rows x 16 k.  A thread slices 4 pairs of
+// adjacent k and stores each slice's pair as one packed BF16 word straight to
+// the tiled operand: a warp covers 4 rows x 8 pairs, i.e. whole 32-byte
+// sectors (two rows' 16-byte runs) of the core matrices.
 template <class C>
 __global__ void __launch_bounds__(256) slice_stack_left_kernel(const SliceStackLJob* __restrict__ jobs, int nev,
                                                                int nchunk, int mtiles, const int* __restrict__ bexp) {
-  extern __shared__ __align__(128) uint8_t sm[];
-  int* sexp = (int*)sm;
-  uint8_t* stage = sm + 512;
+  __shared__ int sexp[SPLIT_M];
   const int kc = blockIdx.x % nchunk, t = blockIdx.x / nchunk;
   const SliceStackLJob& J = jobs[t / mtiles];
   const int mt = t % mtiles;
@@ -630,42 +631,45 @@ __global__ void __launch_bounds__(256) slice_stack_left_kernel(const SliceStackL
     sexp[threadIdx.x] = E;
     if (kc == 0) J.exps[g] = E;
   }
-  constexpr int PER = SPLIT_M * SPLIT_K / 256;
-  double2 v[PER];
+  constexpr int PER = SPLIT_M * SPLIT_K / 2 / 256;
+  double2 v[PER][2];
 #pragma unroll
   for (int u = 0; u < PER; u++) {
     const int e = threadIdx.x + u * 256;
-    const int rr = e >> 4, k = kc * SPLIT_K + (e & 15);
-    const int g = mt * SPLIT_M + rr;
-    v[u] = make_double2(0.0, 0.0);
-    if (k < K && g < rows) {
-      const int sl = g / nev, r = g - sl * nev, q = k / nev, j = k - q * nev;
-      v[u] = ((J.dag >> q) & 1) ? J.a[sl][q][(size_t)j * nev + r] : J.a[sl][q][(size_t)r * nev + j];
+    const int rr = e >> 3, g = mt * SPLIT_M + rr;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int k = kc * SPLIT_K + 2 * (e & 7) + h;
+      v[u][h] = make_double2(0.0, 0.0);
+      if (k < K && g < rows) {
+        const int sl = g / nev, r = g - sl * nev, q = k / nev, j = k - q * nev;
+        v[u][h] = ((J.dag >> q) & 1) ? J.a[sl][q][(size_t)j * nev + r] : J.a[sl][q][(size_t)r * nev + j];
+      }
     }
   }
   __syncthreads();
+  uint8_t* d0 = J.out + ((size_t)mt * nchunk + kc) * C::A_STAGE;
 #pragma unroll
   for (int u = 0; u < PER; u++) {
     const int e = threadIdx.x + u * 256;
-    const int rr = e >> 4, kk = e & 15;
-    const int q = min((kc * SPLIT_K + kk) / nev, J.nterm - 1);
+    const int rr = e >> 3, kp = e & 7;
     const int E = sexp[rr];
-    bool nr, ni;
-    uint64_t Ur, Ui;
-    weighted_fixed(v[u], J.wexp[q], J.w[q] < 0.f, (J.dag >> q) & 1, E, Ur, nr, Ui, ni);
-    Ur = round_fixed<C::NS>(Ur);
-    Ui = round_fixed<C::NS>(Ui);
-    const uint32_t off = core_offset(rr, kk);
+    uint64_t Ur[2], Ui[2];
+    bool nr[2], ni[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int q = min((kc * SPLIT_K + 2 * kp + h) / nev, J.nterm - 1);
+      weighted_fixed(v[u][h], J.wexp[q], J.w[q] < 0.f, (J.dag >> q) & 1, E, Ur[h], nr[h], Ui[h], ni[h]);
+      Ur[h] = round_fixed<C::NS>(Ur[h]);
+      Ui[h] = round_fixed<C::NS>(Ui[h]);
+    }
+    uint8_t* d = d0 + core_offset(rr, 2 * kp);
 #pragma unroll
     for (int s = 0; s < C::NS; s++) {
-      *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::A_SUB + off) = slice_bf16(Ur, s, nr);
-      *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::A_SUB + off) = slice_bf16(Ui, s, ni);
+      *(uint32_t*)(d + (s * 2 + 0) * C::A_SUB) = slice_pair(Ur[0], nr[0], Ur[1], nr[1], s);
+      *(uint32_t*)(d + (s * 2 + 1) * C::A_SUB) = slice_pair(Ui[0], ni[0], Ui[1], ni[1], s);
     }
   }
-  __syncthreads();
-  int4* d = (int4*)(J.out + ((size_t)mt * nchunk + kc) * C::A_STAGE);
-  const int4* src = (const int4*)stage;
-  for (int i = threadIdx.x; i < C::A_STAGE / 16; i += 256) d[i] = src[i];
 }
 
 // Right operand slices: CTA = (job, N tile, K chunk); BN columns x 16 k.
@@ -1780,7 +1784,7 @@ static int ensure_smem(K kernel, size_t smem, bool& done) {
 }
 static bool g_attr_sls = false, g_attr_srs = false, g_attr_tg = false, g_attr_sld = false, g_attr_srd = false;
 static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr = false, g_attr_std = false,
-            g_attr_hp = false, g_attr_stl = false;
+            g_attr_hp = false;
 static int g_nsm = 0;
 
 template <class C>
@@ -1812,7 +1816,6 @@ int split_kernels_prepare() {
   CTR_TRY(ensure_smem(trace_groups_kernel, trace_groups_max_smem(), g_attr_tg));
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
   CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
-  CTR_TRY(ensure_smem(slice_stack_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_stl));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
   return CTR_OK;
@@ -1884,12 +1887,10 @@ int launch_slice_task_left(const SliceTaskLJob* d_jobs, int njobs, int nev, int 
 int launch_slice_stack_left(const SliceStackLJob* d_jobs, int njobs, int nev, int nchunk, int mtiles, const int* bexp,
                             cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
-  const size_t smem = 512 + CfgHP::A_STAGE;
-  CTR_TRY(ensure_smem(slice_stack_left_kernel<CfgHP>, smem, g_attr_stl));
   const long long grid = (long long)njobs * mtiles * nchunk;
   if (grid > 0x7fffffffLL) return fail(CTR_ERR_ARG, "stacked slicer: grid too large");
   TimedLaunch tl(s, "slice_stack_left");
-  slice_stack_left_kernel<CfgHP><<<(unsigned)grid, 256, smem, s>>>(d_jobs, nev, nchunk, mtiles, bexp);
+  slice_stack_left_kernel<CfgHP><<<(unsigned)grid, 256, 0, s>>>(d_jobs, nev, nchunk, mtiles, bexp);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }
