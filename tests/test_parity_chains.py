@@ -385,6 +385,25 @@ def test_rhopi_sigmapi_sets_gram_traces(cuda, n):
         P.entrywise(g["triangle"][k], ref, tol, ab, "set %d triangle, Gram traces" % k)
         # the horizontal fish keeps its per-time-slice FP64 traces
         assert np.array_equal(g["hor_fish"][k], f["hor_fish"][k])
+    if n != 12:
+        return
+    # refinement with the Gram traces' error scales: a tolerance below the engine's
+    # error flags every entry, and the FP64 reruns give the FP64 engine's accuracy
+    from contractions_code_scattering_gb300._lib import lib
+    try:
+        _refine(1e-15)
+        with trace_form(1):
+            rf = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(
+                rows, diag, cuda_phi, sets, d5, d2, engine="split", tf_range=tr).items()}
+        assert lib().ctr_split_refined() > 0
+    finally:
+        _refine(1e-9)
+    for k, (a, b) in enumerate(sets):
+        pa, pb = phis[moms[a]], phis[moms[b]]
+        ref, ab = ref_rhopi(prop, pa, pb, mom5, 2, range(tr[0], tr[1]))
+        P.entrywise(rf["rhopi"][k, 2], ref, TOL, ab, "set %d rhopi idir 2, refined" % k)
+        ref, ab = ref_triangle(prop, pa, pb, mom2, range(tr[0], tr[1]))
+        P.entrywise(rf["triangle"][k], ref, TOL, ab, "set %d triangle, refined" % k)
 
 
 def test_block_product_tasks_split_vs_fp64(cuda):
