@@ -193,6 +193,9 @@ bool tune_lookup(const std::string& key, int* choice);
 void tune_store(const std::string& key, int choice, const std::vector<double>& ms);
 int tune_resolve(const char* knob, const std::string& shape, int ncand, int dflt, cudaStream_t s,
                  const std::function<int(int)>& run, int* choice);
+// The choice tune_resolve will return when it will not measure (forced, cached or
+// mode 0): true and *choice set; false when it would measure the candidates.
+bool tune_peek(const char* knob, const std::string& shape, int ncand, int dflt, int* choice);
 
 // Upload a host array into a workspace slot (async on stream, host buffer is
 // kept alive by a pinned staging copy owned by the slot).

@@ -451,9 +451,11 @@ struct Planner {
 // Closing traces of a batch; add() returns the slot of the value.
 struct TracePlan {
   std::vector<TraceTask> tt;
+  int n = 0;
+  bool keep = true;  // false: number the slots only (the traces run in another form)
   int add(const double2* x, const double2* y, float cre, float cim, int mode) {
-    tt.push_back(tr(x, y, nullptr, cre, cim, mode));
-    return (int)tt.size() - 1;
+    if (keep) tt.push_back(tr(x, y, nullptr, cre, cim, mode));
+    return n++;
   }
 };
 
@@ -1396,6 +1398,13 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
   const size_t tr_pair = (size_t)nset * (uniq.size() + (tri ? 32 : 0));
   const size_t per_pair = blk_pair * N2 * sizeof(double2) + tr_pair * (sizeof(double2) + sizeof(double));
   const int batch = std::max(1, std::min(npairs, (int)(sets_budget() / std::max<size_t>(per_pair, 1))));
+  // closing-trace form on the split engine (chains.trace_form): when it is known
+  // to be the Gram products, the FP64 trace tasks are not built
+  const std::string trace_shape =
+      "nev=" + std::to_string(N) + ",m=" + std::to_string(4 * nC) + ",n=" + std::to_string(4 * nops);
+  int known_form = 0;
+  const bool fp64_traces_needed = c.engine != CTR_ENGINE_SPLIT ||
+                                  !tune_peek("chains.trace_form", trace_shape, 2, 1, &known_form) || known_form == 0;
   Refine rf_rp, rf_tr;
   if (rhopi) CTR_TRY(refine_begin(c, (size_t)nset * 3 * npairs * 4, WS_REFINE, rf_rp));
   if (tri) CTR_TRY(refine_begin(c, (size_t)nset * npairs * 2, WS_SPLITJOBS3, rf_tr));
@@ -1487,6 +1496,8 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
     if (used * sizeof(double2) + ntr * (sizeof(double2) + sizeof(double)) > (size_t)np * per_pair)
       return fail(CTR_ERR_ALLOC, "ctr_rhopi_sigmapi_sets: batch arena overflow");
     TracePlan tp;
+    tp.keep = fp64_traces_needed;
+    if (tp.keep) tp.tt.reserve((size_t)np * tr_pair);
     // on the split engine the same traces as Gram products: group i * 4 + s2 of
     // pair i pairs the X blocks (set combination ci, row block s5, column block
     // s2) with the Z blocks (sink operator slab, tau block (s3, s2)); every trace
@@ -1494,6 +1505,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
     GramPlan gp;
     const bool gram = c.engine == CTR_ENGINE_SPLIT;
     if (gram) {
+      gp.tr.reserve((size_t)np * tr_pair);
       gp.ngroup = 4 * np;
       gp.mrows = 4 * nC;
       gp.ncols = 4 * nops;
@@ -1525,7 +1537,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
         if (rhopi) {
           // Tr-Had(X_{s5 s2}, Phi_ip^dag tau_{s3 s2}) without its coefficient, once for the three
           // polarisations (those of ip = 0, 1 are shared); the row sums apply the coefficients
-          const int base = (int)tp.tt.size();
+          const int base = tp.n;
           for (const auto& u : uniq) {
             const int xb = std::get<1>(u), zb = std::get<2>(u);
             const int slot = tp.add(Xblk(ci, i, xb / 4, xb % 4), Zblk(std::get<0>(u), i, zb), 1.f, 0.f, 0);
@@ -1556,9 +1568,8 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
       // 0: the FP64 trace kernel, 1: Gram products on the tensor cores
       int form = 1;
       auto run = [&](int f) { return f ? trace_gram(N, gp, trv, tra, c.s) : run_traces(c, tp.tt); };
-      CTR_TRY(tune_resolve("chains.trace_form", "nev=" + std::to_string(N) + ",m=" + std::to_string(gp.mrows) +
-                                                    ",n=" + std::to_string(gp.ncols),
-                           2, 1, c.s, run, &form));
+      CTR_TRY(tune_resolve("chains.trace_form", trace_shape, 2, 1, c.s, run, &form));
+      if (form == 0 && !tp.keep) return fail(CTR_ERR_ARG, "chains.trace_form: FP64 traces chosen but not planned");
       CTR_TRY(run(form));
     } else {
       CTR_TRY(run_traces(c, tp.tt));

@@ -62,6 +62,20 @@ void tune_store(const std::string& key, int choice, const std::vector<double>& m
   g_fresh.insert(key);
 }
 
+bool tune_peek(const char* knob, const std::string& shape, int ncand, int dflt, int* choice) {
+  const int forced = tune_forced(knob);
+  if (forced >= 0) {
+    *choice = forced;
+    return forced < ncand;
+  }
+  if (tune_lookup(tune_key(knob, shape), choice) && *choice < ncand) return true;
+  if (tune_mode() == 0) {
+    *choice = dflt;
+    return true;
+  }
+  return false;
+}
+
 int tune_resolve(const char* knob, const std::string& shape, int ncand, int dflt, cudaStream_t s,
                  const std::function<int(int)>& run, int* choice) {
   const int forced = tune_forced(knob);
