@@ -487,14 +487,6 @@ __device__ __forceinline__ double2 task_right_raw(const SliceTaskRJob& J, int ne
   return ((J.dag >> (4 * jb + q)) & 1) ? B[(size_t)c * nev + i] : B[(size_t)i * nev + c];
 }
 
-// Every (block, term) of a right job conjugate-transposed.
-__device__ __forceinline__ bool task_right_all_dag(const SliceTaskRJob& J) {
-  const int m = (1 << J.nterm) - 1;
-  for (int j = 0; j < J.nb; j++)
-    if (((J.dag >> (4 * j)) & m) != m) return false;
-  return true;
-}
-
 // Task-form slicing runs in two launches: the exponent bounds of every distinct
 // block of the launch (one read of each block), then one CTA per (operand tile,
 // K chunk), which combines the bounds of its operand's blocks into the row or
@@ -672,13 +664,15 @@ __global__ void __launch_bounds__(256) slice_stack_left_kernel(const SliceStackL
   }
 }
 
-// Right operand slices: CTA = (job, N tile, K chunk); BN columns x 16 k.
+// Right operand slices: CTA = (job, N tile, K chunk); BN columns x 16 k.  A
+// thread slices pairs of adjacent k of one column and stores each slice's pair
+// as one packed BF16 word per plane straight to the tiled operand: a warp
+// covers 4 adjacent columns x 8 pairs, i.e. whole 32-byte sectors (two
+// columns' 16-byte runs) of the core matrices.
 template <class C>
-__global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
+__global__ void __launch_bounds__(128) slice_task_right_kernel(const SliceTaskRJob* __restrict__ jobs, int nev,
                                                                int nchunk, int ntiles, const int* __restrict__ bexp) {
-  extern __shared__ __align__(128) uint8_t sm[];
-  int* sexp = (int*)sm;
-  uint8_t* stage = sm + 512;
+  __shared__ int sexp[C::BN];
   const int kc = blockIdx.x % nchunk, t = blockIdx.x / nchunk;
   const SliceTaskRJob& J = jobs[t / ntiles];
   const int nt = t % ntiles;
@@ -699,50 +693,50 @@ __global__ void __launch_bounds__(256) slice_task_right_kernel(const SliceTaskRJ
     sexp[threadIdx.x] = E;
     if (kc == 0) J.exps[n] = E;  // exps sized ntiles * BN (padding columns get 0)
   }
-  // consecutive threads along the columns, or, for conjugate-transposed blocks
-  // (contiguous in k), along k
-  const bool tr = task_right_all_dag(J);
-  constexpr int PER = (C::BN * SPLIT_K + 255) / 256;
-  double2 v[PER];
+  constexpr int PER = C::BN * SPLIT_K / 2 / 128;
+  static_assert(C::BN * SPLIT_K / 2 % 128 == 0, "column pairs a thread");
+  double2 v[PER][2];
 #pragma unroll
   for (int u = 0; u < PER; u++) {
-    const int e = threadIdx.x + u * 256;
-    const int nn = tr ? (e >> 4) : (e % C::BN), kk = tr ? (e & 15) : (e / C::BN);
-    const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
-    v[u] = (e < C::BN * SPLIT_K && n < ncols && k < K) ? task_right_raw(J, nev, k, n) : make_double2(0.0, 0.0);
-  }
-  __syncthreads();
+    const int e = threadIdx.x + u * 128;
+    const int n = nt * C::BN + (e >> 3);
 #pragma unroll
-  for (int u = 0; u < PER; u++) {
-    const int e = threadIdx.x + u * 256;
-    if (e >= C::BN * SPLIT_K) break;
-    const int nn = tr ? (e >> 4) : (e % C::BN), kk = tr ? (e & 15) : (e / C::BN);
-    const int n = nt * C::BN + nn, k = kc * SPLIT_K + kk;
-    const int jb = min(n / nev, J.nb - 1), q = min(k / nev, J.nterm - 1);
-    const int E = sexp[nn];
-    bool nr, ni;
-    uint64_t Ur, Ui;
-    weighted_fixed(v[u], 0, false, (J.dag >> (4 * jb + q)) & 1, E, Ur, nr, Ui, ni);
-    Ur = round_fixed<C::NS>(Ur);
-    Ui = round_fixed<C::NS>(Ui);
-    const uint32_t off = core_offset(nn, kk);
-#pragma unroll
-    for (int s = 0; s < C::NS; s++) {
-      if (C::PACK) {
-        const __nv_bfloat16 bi = slice_bf16(Ui, s, ni);
-        *(__nv_bfloat16*)(stage + (s * 3 + 0) * C::B_SUB + off) = bf16_neg(bi);
-        *(__nv_bfloat16*)(stage + (s * 3 + 1) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 3 + 2) * C::B_SUB + off) = bi;
-      } else {
-        *(__nv_bfloat16*)(stage + (s * 2 + 0) * C::B_SUB + off) = slice_bf16(Ur, s, nr);
-        *(__nv_bfloat16*)(stage + (s * 2 + 1) * C::B_SUB + off) = slice_bf16(Ui, s, ni);
-      }
+    for (int h = 0; h < 2; h++) {
+      const int k = kc * SPLIT_K + 2 * (e & 7) + h;
+      v[u][h] = (n < ncols && k < K) ? task_right_raw(J, nev, k, n) : make_double2(0.0, 0.0);
     }
   }
   __syncthreads();
-  int4* d = (int4*)(J.out + ((size_t)nt * nchunk + kc) * C::B_STAGE);
-  const int4* src = (const int4*)stage;
-  for (int i = threadIdx.x; i < C::B_STAGE / 16; i += 256) d[i] = src[i];
+  uint8_t* d0 = J.out + ((size_t)nt * nchunk + kc) * C::B_STAGE;
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int e = threadIdx.x + u * 128;
+    const int nn = e >> 3, kp = e & 7, n = nt * C::BN + nn;
+    const int jb = min(n / nev, J.nb - 1);
+    const int E = sexp[nn];
+    uint64_t Ur[2], Ui[2];
+    bool nr[2], ni[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int q = min((kc * SPLIT_K + 2 * kp + h) / nev, J.nterm - 1);
+      weighted_fixed(v[u][h], 0, false, (J.dag >> (4 * jb + q)) & 1, E, Ur[h], nr[h], Ui[h], ni[h]);
+      Ur[h] = round_fixed<C::NS>(Ur[h]);
+      Ui[h] = round_fixed<C::NS>(Ui[h]);
+    }
+    uint8_t* d = d0 + core_offset(nn, 2 * kp);
+#pragma unroll
+    for (int s = 0; s < C::NS; s++) {
+      const uint32_t re = slice_pair(Ur[0], nr[0], Ur[1], nr[1], s), im = slice_pair(Ui[0], ni[0], Ui[1], ni[1], s);
+      if (C::PACK) {
+        *(uint32_t*)(d + (s * 3 + 0) * C::B_SUB) = im ^ BF16X2_SIGNS;
+        *(uint32_t*)(d + (s * 3 + 1) * C::B_SUB) = re;
+        *(uint32_t*)(d + (s * 3 + 2) * C::B_SUB) = im;
+      } else {
+        *(uint32_t*)(d + (s * 2 + 0) * C::B_SUB) = re;
+        *(uint32_t*)(d + (s * 2 + 1) * C::B_SUB) = im;
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------------------ GEMM
@@ -1783,7 +1777,7 @@ static int ensure_smem(K kernel, size_t smem, bool& done) {
   return CTR_OK;
 }
 static bool g_attr_sls = false, g_attr_srs = false, g_attr_tg = false, g_attr_sld = false, g_attr_srd = false;
-static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_tr = false, g_attr_std = false,
+static bool g_attr_sl = false, g_attr_sr = false, g_attr_tl = false, g_attr_std = false,
             g_attr_hp = false;
 static int g_nsm = 0;
 
@@ -1815,7 +1809,6 @@ int split_kernels_prepare() {
   CTR_TRY(ensure_smem(slice_right_staged_kernel<true>, slice_staged_smem(SPLIT_MAXK, 0), g_attr_srd));
   CTR_TRY(ensure_smem(trace_groups_kernel, trace_groups_max_smem(), g_attr_tg));
   CTR_TRY(ensure_smem(slice_task_left_kernel<CfgHP>, 512 + CfgHP::A_STAGE, g_attr_tl));
-  CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, 512 + CfgHP::B_STAGE, g_attr_tr));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgStd>, gemm_smem_bytes<CfgStd>(), g_attr_std));
   CTR_TRY(ensure_smem(split_gemm_kernel<CfgHP>, gemm_smem_bytes<CfgHP>(), g_attr_hp));
   return CTR_OK;
@@ -1898,10 +1891,8 @@ int launch_slice_stack_left(const SliceStackLJob* d_jobs, int njobs, int nev, in
 int launch_slice_task_right(const SliceTaskRJob* d_jobs, int njobs, int nev, int nchunk, int ntiles, const int* bexp,
                             cudaStream_t s) {
   if (njobs == 0) return CTR_OK;
-  const size_t smem = 512 + CfgHP::B_STAGE;
-  CTR_TRY(ensure_smem(slice_task_right_kernel<CfgHP>, smem, g_attr_tr));
   TimedLaunch tl(s, "slice_task_right");
-  slice_task_right_kernel<CfgHP><<<njobs * ntiles * nchunk, 256, smem, s>>>(d_jobs, nev, nchunk, ntiles, bexp);
+  slice_task_right_kernel<CfgHP><<<njobs * ntiles * nchunk, 128, 0, s>>>(d_jobs, nev, nchunk, ntiles, bexp);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

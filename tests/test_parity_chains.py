@@ -406,6 +406,43 @@ def test_rhopi_sigmapi_sets_gram_traces(cuda, n):
         P.entrywise(rf["triangle"][k], ref, TOL, ab, "set %d triangle, refined" % k)
 
 
+def test_rhopi_sigmapi_sets_gram_traces_two_m_tiles(cuda):
+    """36 momentum sets over 7 elementals: 36 set combinations, so each Gram group has
+    144 X blocks, two M tiles of its instances.  Every set's rho -> pi pi and triangle
+    with Gram traces per entry against the FP64 closing traces, and one set against the
+    oracle."""
+    nt, n = 3, 12
+    prop = synth.make_prop(nt, n, seed=1800, decay=0.25)
+    moms = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+    phis = synth.make_phi_momenta(nt, n, moms, seed=1801)
+    cuda_phi = _dev(np.stack([phis[p] for p in moms], axis=1), cuda)
+    rng = np.random.default_rng(1802)
+    mom5 = np.ascontiguousarray(np.stack([synth.make_phi_random(nt, n, rng) for _ in range(5)], axis=1))
+    mom2 = np.ascontiguousarray(mom5[:, :2])
+    d5, d2 = _dev(mom5, cuda), _dev(mom2, cuda)
+    sets = [(a, b) for a in range(1, 7) for b in range(1, 7)]
+    tp = _dev(prop, cuda)
+    diag = api.prop_diag(tp)
+    got = {}
+    for form in (0, 1):
+        with trace_form(form):
+            got[form] = {k: _np(v) for k, v in api.run_contract_rhopi_sigmapi_sets(
+                tp, diag, cuda_phi, sets, d5, d2, engine="split").items()}
+    g, f = got[1], got[0]
+    for k, (a, b) in enumerate(sets):
+        pa, pb = phis[moms[a]], phis[moms[b]]
+        for idir in range(3):
+            ref, ab = ref_rhopi(prop, pa, pb, mom5, idir)
+            P.entrywise(g["rhopi"][k, idir], f["rhopi"][k, idir], SPLIT_TOL, ab,
+                        "set %d idir %d, Gram vs FP64 traces" % (k, idir))
+            if (a, b) == (3, 6):
+                P.entrywise(g["rhopi"][k, idir], ref, SPLIT_TOL, ab, "set (3, 6) rhopi idir %d, Gram traces" % idir)
+        ref, ab = ref_triangle(prop, pa, pb, mom2)
+        P.entrywise(g["triangle"][k], f["triangle"][k], SPLIT_TOL, ab, "set %d triangle, Gram vs FP64 traces" % k)
+        if (a, b) == (3, 6):
+            P.entrywise(g["triangle"][k], ref, SPLIT_TOL, ab, "set (3, 6) triangle, Gram traces")
+
+
 def test_block_product_tasks_split_vs_fp64(cuda):
     """The task form directly (include/ctr.h: ctr_zgemm_tasks): four-term
     gamma_5-weighted block products with conjugate transposes, as in X = M1 G M2^dagger,
