@@ -91,7 +91,7 @@ int ctr_sigma(int engine, int nev, int nt, int tf_begin, int tf_end, const doubl
  * lib/contract.cpp:549-570).  Elementals [Nt][N][N] unless noted.  With
  * CTR_ENGINE_SPLIT every block product of the chains runs on the tensor-core
  * split engine (Nev <= 128); the closing traces and the loop-unity traces are
- * FP64 on both engines. */
+ * FP64 on both engines (except the rho -> pi pi / sigma -> pi pi set call's, below). */
 
 /* rho -> pi pi for gamma_idir (run_ContractRhoPi, lib/contract_kernels_rhopi.cu:64-137):
  * mom5_p1p2 [Nt][5][N][N]; corr [tf_end-tf_begin][Nt][4] (one entry per rho operator). */
@@ -125,7 +125,11 @@ int ctr_pipi_sets(int engine, int nev, int nt, int tf_begin, int tf_end, int iso
  * R = Phi_P2 taud Phi_P1: X is computed once per set and pair and multiplied by all the
  * sink operators the outputs need in one stacked launch.  Outputs (each may be NULL; then
  * its operands may be NULL too): rhopi [nset][3][tf_end-tf_begin][Nt][4] (idir 0..2, as
- * ctr_rhopi), triangle [nset][tf_end-tf_begin][Nt][2] and hor_fish [nset][Nt] (as ctr_sigmapi). */
+ * ctr_rhopi), triangle [nset][tf_end-tf_begin][Nt][2] and hor_fish [nset][Nt] (as ctr_sigmapi).
+ * On the split engine the rho -> pi pi and triangle traces of a pair run as Gram products
+ * on the tensor cores (the tuning knob "chains.trace_form" = 1, the default; each entry
+ * within the engine's per-entry tolerance); with the knob forced to 0 they run as FP64
+ * traces and every set's entries are bitwise those of its own ctr_rhopi / ctr_sigmapi. */
 int ctr_rhopi_sigmapi_sets(int engine, int nev, int nt, int tf_begin, int tf_end, const double* prop_rows,
                            const double* prop_diag, const double* phi, int nphi, const double* mom5_p1p2,
                            const double* mom2_p1p2, int nset, const int32_t* sets, double* rhopi, double* triangle,
