@@ -99,7 +99,8 @@ enum {
   WS_BLOCKEXP,      // their row / column exponent bounds
   WS_TRACEGROUPS,   // grouped closing traces of a two-sided call
   WS_GRAM,          // sliced operands and partial products of Gram traces
-  WS_GRAMJOBS,      // their block, instance and trace tables
+  WS_GRAMJOBS,      // their block, instance and pointer tables
+  WS_GRAMTRACES,    // their trace lists
   WS_COUNT
 };
 
@@ -160,6 +161,9 @@ struct GramPlan {
     float cre, cim;
   };
   int ngroup = 0, mrows = 0, ncols = 0;
+  // groups come in runs of group_run whose traces may interleave in tr, runs in
+  // order: a launch then takes whole runs, and its traces are one range of tr
+  int group_run = 1;
   std::vector<const double2*> left, right;
   std::vector<Tr> tr;
 };

@@ -1507,6 +1507,7 @@ int rhopi_sigmapi_sets(int N, int Nt, int tf_begin, int tf_end, const double* pr
     if (gram) {
       gp.tr.reserve((size_t)np * tr_pair);
       gp.ngroup = 4 * np;
+      gp.group_run = 4;  // a pair's traces interleave its four s2 groups
       gp.mrows = 4 * nC;
       gp.ncols = 4 * nops;
       gp.left.resize((size_t)gp.ngroup * gp.mrows);

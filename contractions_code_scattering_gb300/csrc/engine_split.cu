@@ -2,6 +2,7 @@
 // contractions and batched block products.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -978,6 +979,11 @@ int zgemm_split_grids(int N, const std::vector<GridTask>& grids, cudaStream_t st
 // complex128 partial product written row-major (rows padded to M tiles,
 // columns to N tiles).  Groups run in launches sized to a 4 GB arena; each
 // launch slices its operands, runs the GEMM and sums its traces' pieces.
+static_assert(sizeof(GramPlan::Tr) == sizeof(GramTrace) && offsetof(GramPlan::Tr, g) == offsetof(GramTrace, g) &&
+                  offsetof(GramPlan::Tr, slot) == offsetof(GramTrace, slot) &&
+                  offsetof(GramPlan::Tr, cre) == offsetof(GramTrace, coef),
+              "a plan's traces upload as GramTrace");
+
 int trace_gram(int N, const GramPlan& P, double2* trv, double* tra, cudaStream_t stream) {
   if (P.tr.empty()) return CTR_OK;
   if (N > SPLIT_MAXK) return fail(CTR_ERR_UNSUPPORTED, "split engine supports Nev <= %d (got %d)", SPLIT_MAXK, N);
@@ -996,15 +1002,27 @@ int trace_gram(int N, const GramPlan& P, double2* trv, double* tra, cudaStream_t
   const size_t p_b = (size_t)lrows * rcols * sizeof(double2);
   const size_t per_inst = l_b + r_b + p_b + (size_t)(lrows + rcols) * (sizeof(int) + sizeof(float));
   const size_t per_group = (size_t)npiece * per_inst;
-  const int G = (int)std::max<size_t>(1, std::min<size_t>(P.ngroup, ((size_t)4 << 30) / per_group));
-  for (const GramPlan::Tr& t : P.tr)
+  const int run = std::max(1, P.group_run);
+  int G = (int)std::max<size_t>(1, std::min<size_t>(P.ngroup, ((size_t)4 << 30) / per_group));
+  if (G < P.ngroup) G = std::max(run, G / run * run);
+  const int nl = cdiv(P.ngroup, G);
+  // the traces of each launch: a range of the plan's list when the launches
+  // follow it (start[li] .. start[li + 1]), else copies bucketed by launch
+  std::vector<size_t> start(nl + 1, 0);
+  bool ranges = true;
+  for (size_t k = 0; k < P.tr.size(); k++) {
+    const GramPlan::Tr& t = P.tr[k];
     if (t.g < 0 || t.g >= P.ngroup || t.r < 0 || t.r >= P.mrows || t.c < 0 || t.c >= P.ncols)
       return fail(CTR_ERR_ARG, "Gram traces: trace (%d, %d, %d) outside the plan", t.g, t.r, t.c);
-  // traces by launch, in plan order
-  const int nl = cdiv(P.ngroup, G);
-  std::vector<std::vector<GramTrace>> by(nl);
-  for (const GramPlan::Tr& t : P.tr)
-    by[t.g / G].push_back(GramTrace{t.g % G, t.r, t.c, t.slot, {t.cre, t.cim}});
+    if (k && t.g / G < P.tr[k - 1].g / G) ranges = false;
+    start[t.g / G + 1]++;
+  }
+  for (int li = 0; li < nl; li++) start[li + 1] += start[li];
+  std::vector<std::vector<GramTrace>> by;
+  if (!ranges) {
+    by.resize(nl);
+    for (const GramPlan::Tr& t : P.tr) by[t.g / G].push_back(GramTrace{t.g, t.r, t.c, t.slot, {t.cre, t.cim}});
+  }
   for (int li = 0; li < nl; li++) {
     const int g0 = li * G, ng = std::min(G, P.ngroup - g0), ni = ng * npiece;
     void* mem;
@@ -1023,14 +1041,16 @@ int trace_gram(int N, const GramPlan& P, double2* trv, double* tra, cudaStream_t
       gi[ip] = SplitGemmInst{lsl + (size_t)ip * l_b, rsl + (size_t)ip * r_b, lexp + (size_t)ip * lrows,
                              rexp + (size_t)ip * rcols, nullptr, nullptr};
     }
-    const std::vector<GramTrace>& tl = by[li];
-    void* d[4];
+    const GramTrace* tl = ranges ? (const GramTrace*)P.tr.data() + start[li] : by[li].data();
+    const size_t ntl = start[li + 1] - start[li];
+    void* d[3];
     CTR_TRY(upload_group(WS_GRAMJOBS,
                          {{P.left.data() + (size_t)g0 * P.mrows, (size_t)ng * P.mrows * sizeof(const double2*)},
                           {P.right.data() + (size_t)g0 * P.ncols, (size_t)ng * P.ncols * sizeof(const double2*)},
-                          {outs.data(), outs.size() * sizeof(double2*)},
-                          {tl.data(), tl.size() * sizeof(GramTrace)}},
+                          {outs.data(), outs.size() * sizeof(double2*)}},
                          d, stream));
+    void* d_tr;
+    CTR_TRY(upload(WS_GRAMTRACES, tl, ntl * sizeof(GramTrace), &d_tr, stream));
     for (int ip = 0; ip < ni; ip++) gi[ip].outs = (double2* const*)d[2] + ip;
     void* d_gi;
     CTR_TRY(upload(WS_GEMM_B, gi.data(), gi.size() * sizeof(SplitGemmInst), &d_gi, stream));
@@ -1041,7 +1061,7 @@ int trace_gram(int N, const GramPlan& P, double2* trv, double* tra, cudaStream_t
     SplitGemmBatch B{(const SplitGemmInst*)d_gi, mtiles, ntiles, nchunk, P.mrows, P.ncols, lrows, nullptr, 1, rcols, 1};
     B.order = 0;
     CTR_TRY(launch_split_gemm(B, ni, d_err, stream, true));
-    CTR_TRY(launch_gram_trace_sum((const GramTrace*)d[3], (int)tl.size(), part, npiece, lrows, rcols, lexp, rexp, lnorm,
+    CTR_TRY(launch_gram_trace_sum((const GramTrace*)d_tr, (int)ntl, g0, part, npiece, lrows, rcols, lexp, rexp, lnorm,
                                   rnorm, trv, tra, stream));
   }
   if (!capturing()) g_gram_traces += (double)P.tr.size();

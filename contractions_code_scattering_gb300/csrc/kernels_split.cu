@@ -1738,7 +1738,7 @@ __global__ void __launch_bounds__(256) slice_gram_kernel(const double2* const* _
 // over the piece) and the truncation of the slices (~2^-54 of the scales an
 // element, 2^-48 over a piece's 512 of them with random signs); a piece whose
 // row or column is all zeros adds neither.
-__global__ void __launch_bounds__(128) gram_trace_sum_kernel(const GramTrace* __restrict__ tr, int ntr,
+__global__ void __launch_bounds__(128) gram_trace_sum_kernel(const GramTrace* __restrict__ tr, int ntr, int g0,
                                                              const double2* __restrict__ part, int npiece, int lrows,
                                                              int rcols, const int* __restrict__ lexp,
                                                              const int* __restrict__ rexp,
@@ -1750,7 +1750,7 @@ __global__ void __launch_bounds__(128) gram_trace_sum_kernel(const GramTrace* __
   const GramTrace T = tr[i];
   double re = 0.0, im = 0.0, ab = 0.0;
   for (int p = 0; p < npiece; p++) {
-    const size_t ip = (size_t)T.g * npiece + p;
+    const size_t ip = (size_t)(T.g - g0) * npiece + p;
     const double2 v = part[(ip * lrows + T.r) * rcols + T.c];
     re += v.x;
     im += v.y;
@@ -1921,13 +1921,13 @@ int launch_slice_gram(bool right, const double2* const* d_blk, int ngroup, int n
   return CTR_OK;
 }
 
-int launch_gram_trace_sum(const GramTrace* d_tr, int ntr, const double2* part, int npiece, int lrows, int rcols,
+int launch_gram_trace_sum(const GramTrace* d_tr, int ntr, int g0, const double2* part, int npiece, int lrows, int rcols,
                           const int* lexp, const int* rexp, const float* lnorm, const float* rnorm, double2* trv,
                           double* tra, cudaStream_t s) {
   if (ntr == 0) return CTR_OK;
   TimedLaunch tl(s, "gram_trace_sum");
-  gram_trace_sum_kernel<<<(ntr + 127) / 128, 128, 0, s>>>(d_tr, ntr, part, npiece, lrows, rcols, lexp, rexp, lnorm,
-                                                          rnorm, trv, tra);
+  gram_trace_sum_kernel<<<(ntr + 127) / 128, 128, 0, s>>>(d_tr, ntr, g0, part, npiece, lrows, rcols, lexp, rexp,
+                                                          lnorm, rnorm, trv, tra);
   CTR_CUDA(cudaGetLastError());
   return CTR_OK;
 }

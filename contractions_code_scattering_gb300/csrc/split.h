@@ -168,7 +168,7 @@ struct TraceGroup {
 // up to K = 512); the pieces' complex128 partial products are summed per trace.
 constexpr int GRAM_PIECE = 512;
 struct GramTrace {
-  int g, r, c;   // group (within the launch), left row, right column
+  int g, r, c;   // group (of the plan; the launch's first group is subtracted), left row, right column
   int slot;      // output slot: trv[slot], tra[slot]
   float coef[2]; // complex coefficient of the trace
 };
@@ -218,12 +218,13 @@ int launch_split_gemm(const SplitGemmBatch& g, int ninst, int* d_err, cudaStream
 // (-Im, Re, Im) of a K-major B.
 int launch_slice_gram(bool right, const double2* const* d_blk, int ngroup, int nrows, int ntile, int n2, int npiece,
                       int nchunk, uint8_t* out, int* exps, float* norms, cudaStream_t s);
-// Trace values of a Gram launch: trv[slot] = coef * sum over the pieces of the
-// partial product (r, c) (instance ip's at part + ip * lrows * rcols, row-major
+// Trace values of a Gram launch whose first group is g0: trv[slot] = coef * sum
+// over the pieces of the partial product (r, c) of group g - g0 (instance ip's
+// at part + ip * lrows * rcols, row-major
 // rcols), tra[slot] (when not null) = |coef| * sum over the pieces of
 // (|x_p| |y_p| + 8) 2^(E_x + E_y), a bound of sum |x|_1 |y|_1 and of the slices'
 // truncation error (rows or columns of zeros add nothing).
-int launch_gram_trace_sum(const GramTrace* d_tr, int ntr, const double2* part, int npiece, int lrows, int rcols,
+int launch_gram_trace_sum(const GramTrace* d_tr, int ntr, int g0, const double2* part, int npiece, int lrows, int rcols,
                           const int* lexp, const int* rexp, const float* lnorm, const float* rnorm, double2* trv,
                           double* tra, cudaStream_t s);
 // A bounded wait that runs out (timeout_ns) on an mbarrier nothing arrives at,
